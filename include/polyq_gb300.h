@@ -1,0 +1,181 @@
+/*
+ * polyq_gb300.h -- C-ABI of the GB300 amplitude-evaluation path for polyq.
+ *
+ * Drop-in boundary for the reference crate's Simulator API (src/sim.rs).  A Rust,
+ * Python (ctypes) or C++ host binds these plain-C entry points; the library owns all
+ * device memory, streams and kernels.  Every entry point returns a pq_status and never
+ * aborts; pq_last_error() returns the message of the calling thread's last failure.
+ *
+ * Conventions
+ *   gate codes   0 H, 1 X, 2 Y, 3 Z, 4 S, 5 SDG, 6 T, 7 TDG, 8 P(phase), 9 CZ(q0,q1),
+ *                10 CX(control q0, target q1), 11 SWAP(q0,q1), 12 GPHASE(phase)
+ *                (src/circuit.rs:25-42)
+ *   phase        uint32 k meaning the angle 2*pi*k/2^32 (src/phase.rs:22-24)
+ *   bitstrings   ceil(num_qubits/64) little-endian uint64 words per bitstring,
+ *                qubit q = bit q (src/sim.rs:74-76)
+ *   complex      interleaved (re, im) doubles
+ *   strategy     0 Auto, 1 Cached, 2 Pairs(pairs) (src/sim.rs:41-48)
+ *
+ * An amplitude that is exactly zero (contradictory boundary, inconsistent radical
+ * system) is a value, not an error (src/sim.rs:172-174, src/engine.rs:595-597).
+ */
+#ifndef POLYQ_GB300_H
+#define POLYQ_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define PQ_API __attribute__((visibility("default")))
+#else
+#define PQ_API
+#endif
+
+typedef enum pq_status {
+    PQ_OK = 0,
+    PQ_ERR_INVALID_ARG = 1,        /* malformed circuit, boundary or handle (the reference panics) */
+    PQ_ERR_OUT_OF_MEMORY = 2,      /* device or host allocation failed */
+    PQ_ERR_ADMISSION_REFUSED = 3,  /* branch dimension above the cap, or memory budget exceeded */
+    PQ_ERR_TIMEOUT = 4,            /* a bounded wait expired */
+    PQ_ERR_DEVICE = 5,             /* CUDA error (message in pq_last_error) */
+    PQ_ERR_UNSUPPORTED = 6,        /* structure outside the kernels' limits (d > 62 or > 64 pivots) */
+    PQ_ERR_NO_DEVICE = 7,          /* no CUDA device visible */
+    PQ_ERR_INTERNAL = 8
+} pq_status;
+
+typedef struct pq_sim pq_sim;
+typedef struct pq_batch pq_batch;
+typedef struct pq_server pq_server;
+
+/* Circuit description; the arrays stay owned by the caller (read during the call only). */
+typedef struct pq_circuit_desc {
+    int32_t num_qubits;
+    int32_t num_gates;
+    const uint8_t *op;
+    const int32_t *q0;
+    const int32_t *q1;
+    const uint32_t *phase;
+} pq_circuit_desc;
+
+/* Engine statistics: EngineStats of branch 0 (src/engine.rs:64-79) + pairs (src/sim.rs:161-168). */
+typedef struct pq_stats {
+    int64_t free_vars, planes, lines, radical, terms, branch_dim;
+    int64_t pairs;          /* decomposed T-pairs p */
+    int64_t num_branches;   /* 2^p branch engines */
+    int64_t branches_per_amplitude; /* sum over branch engines of 2^d */
+    int64_t device_bytes;   /* HBM held by the simulator's resident structures */
+    double build_seconds;   /* host compile + elimination + upload time */
+} pq_stats;
+
+/* Enumeration tuning (0 fields take the library defaults / autotuned values). */
+typedef struct pq_tuning {
+    int32_t inner_dims;      /* Gray steps per lane chunk = 2^inner_dims (4..14) */
+    int32_t chunks_per_lane; /* chunks a lane walks per work item (1..64) */
+    int32_t block_warps;     /* warps per CTA of the enumeration kernel (1..16) */
+    int32_t max_branch_dim;  /* admission cap on d per branch engine (<= 62) */
+} pq_tuning;
+
+/* ---- library ------------------------------------------------------------------------ */
+PQ_API const char *pq_version(void);
+PQ_API const char *pq_last_error(void);
+/* Select the CUDA device used by subsequently created objects (default 0). */
+PQ_API pq_status pq_init(int32_t device);
+PQ_API pq_status pq_set_default_tuning(const pq_tuning *t);
+PQ_API pq_status pq_get_default_tuning(pq_tuning *t);
+
+/* ---- Simulator (src/sim.rs:139-198) --------------------------------------------------- */
+/* Simulator::with_options(circuit, SimOptions{strategy, ..}) -- sim.rs:144-148.
+ * Compiles, eliminates and uploads every branch engine; structures stay resident in HBM. */
+PQ_API pq_status pq_sim_create(const pq_circuit_desc *circuit, int32_t strategy, int32_t pairs, pq_sim **out);
+/* Host-only analysis: compile, eliminate and build every branch engine without a device
+ * (stats, canonical dumps; evaluation calls on it return PQ_ERR_NO_DEVICE). */
+PQ_API pq_status pq_analyze(const pq_circuit_desc *circuit, int32_t strategy, int32_t pairs, pq_sim **out);
+PQ_API void pq_sim_destroy(pq_sim *sim);
+/* Simulator::stats / pairs -- sim.rs:161-168 */
+PQ_API pq_status pq_sim_stats(const pq_sim *sim, pq_stats *out);
+
+/* Simulator::amplitude / amplitude_index for n boundaries -- sim.rs:171-182.
+ * x, y: n bitstrings each (host memory).  out: 2n doubles.  errbound (optional, n doubles):
+ * bound on |out - exact| from FP32 branch weights (compensated accumulation, FP64 reduction). */
+PQ_API pq_status pq_amplitudes(pq_sim *sim, int64_t n, const uint64_t *x, const uint64_t *y, double *out,
+                               double *errbound);
+/* Simulator::probability -- sim.rs:196-198: |amplitude|^2, n doubles. */
+PQ_API pq_status pq_probabilities(pq_sim *sim, int64_t n, const uint64_t *x, const uint64_t *y, double *out);
+/* Simulator::marginal_probability -- sim.rs:225-231, for one input x and nmeas (qubit, outcome)
+ * pairs.  The sandwich engine of each distinct measured-qubit set is built once and cached. */
+PQ_API pq_status pq_marginal(pq_sim *sim, const uint64_t *x, int32_t nmeas, const int32_t *qubits,
+                             const uint8_t *outcomes, double *out);
+/* Device-resident variant of pq_amplitudes: x, y, out, errbound are device pointers and the
+ * work is enqueued on `stream` (cudaStream_t, NULL = the simulator's stream) without a host
+ * synchronisation. */
+PQ_API pq_status pq_amplitudes_device(pq_sim *sim, int64_t n, const uint64_t *x, const uint64_t *y, double *out,
+                                      double *errbound, void *stream);
+/* Same evaluation split into one launch sequence per boundary (the plain one-circuit,
+ * one-boundary-per-launch path, kept as the comparison baseline for batching). */
+PQ_API pq_status pq_amplitudes_plain(pq_sim *sim, int64_t n, const uint64_t *x, const uint64_t *y, double *out);
+
+/* ---- batched multi-circuit launch (one persistent, graph-captured launch) ------------ */
+/* Amplitudes of counts[i] boundaries on sims[i], all i, in one CUDA-graph launch of a
+ * persistent kernel whose warps pull (circuit, boundary, chunk-range) work items. */
+PQ_API pq_status pq_batch_create(int32_t nsims, pq_sim *const *sims, const int64_t *counts, pq_batch **out);
+PQ_API void pq_batch_destroy(pq_batch *b);
+/* x, y: boundaries of sims[0] then sims[1] ... with words_per_bitstring words each
+ * (= ceil(max num_qubits / 64)); out: 2*sum(counts) doubles. */
+PQ_API pq_status pq_batch_run(pq_batch *b, const uint64_t *x, const uint64_t *y, double *out, double *errbound);
+PQ_API pq_status pq_batch_run_device(pq_batch *b, const uint64_t *x, const uint64_t *y, double *out,
+                                     double *errbound, void *stream);
+PQ_API int32_t pq_batch_words(const pq_batch *b);
+PQ_API int64_t pq_batch_branches(const pq_batch *b);
+
+/* ---- serving loop (continuous batching) --------------------------------------------- */
+/* Requests against resident simulators are admitted while device slots and the memory
+ * budget allow; admitted requests are launched in waves on a pool of streams, so work of
+ * requests that arrive while others run overlaps on the device. */
+typedef enum pq_req_kind { PQ_REQ_AMPLITUDE = 0, PQ_REQ_PROBABILITY = 1, PQ_REQ_MARGINAL = 2 } pq_req_kind;
+typedef struct pq_request {
+    int32_t sim;          /* index into the server's simulator table */
+    int32_t kind;         /* pq_req_kind */
+    uint64_t x[2];        /* input bitstring (num_qubits <= 128) */
+    uint64_t y[2];        /* output bitstring (AMPLITUDE/PROBABILITY) */
+    int32_t qubit;        /* measured qubit (MARGINAL) */
+    int32_t outcome;      /* measured outcome (MARGINAL) */
+    int64_t tag;          /* caller's identifier, returned with the result */
+} pq_request;
+typedef struct pq_result {
+    int64_t tag;
+    int32_t status;       /* pq_status of this request */
+    int32_t kind;
+    double re, im;        /* amplitude, or probability in re */
+    double errbound;
+    double submit_s, done_s;  /* seconds on the server's monotonic clock */
+} pq_result;
+PQ_API pq_status pq_server_create(int32_t nsims, pq_sim *const *sims, int32_t max_slots, int64_t mem_budget_bytes,
+                                  int32_t max_branch_dim, pq_server **out);
+PQ_API void pq_server_destroy(pq_server *s);
+/* Non-blocking: queues n requests; refused requests complete immediately with a status. */
+PQ_API pq_status pq_server_submit(pq_server *s, int64_t n, const pq_request *reqs);
+/* Collects up to cap finished results; waits up to timeout_s for at least one. */
+PQ_API int64_t pq_server_poll(pq_server *s, pq_result *out, int64_t cap, double timeout_s);
+PQ_API double pq_server_now(const pq_server *s);
+PQ_API pq_status pq_server_drain(pq_server *s, double timeout_s);
+
+/* ---- checks (bit-exact comparisons against a CPU restatement) ------------------------ */
+/* Canonical dump of branch engine `branch`: normal form, diagonal masks, kernel and
+ * boundary columns, RREF; returns the word count (out = NULL to size), < 0 on error. */
+PQ_API int64_t pq_debug_engine_dump(const pq_sim *sim, int32_t branch, uint64_t *out, int64_t cap);
+/* Z8 index of every branch s < 2^d of branch engine `branch` for boundary (x, y), as the
+ * enumeration kernel computes it on the device.  Returns d, or -1 (vanishing boundary),
+ * or -2 (error). */
+PQ_API int32_t pq_debug_branch_phases(pq_sim *sim, int32_t branch, const uint64_t *x, const uint64_t *y,
+                                      uint8_t *out);
+/* Same amplitudes as pq_amplitudes with FP64 branch weights and FP64 accumulation on the
+ * device (verification mode). */
+PQ_API pq_status pq_amplitudes_fp64(pq_sim *sim, int64_t n, const uint64_t *x, const uint64_t *y, double *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

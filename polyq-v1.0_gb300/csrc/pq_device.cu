@@ -1,0 +1,891 @@
+// pq_device.cu -- device runtime and C-ABI of the GB300 amplitude path.
+//
+// Objects
+//   Target   branch engines of one fixed-variable set (a Simulator's <y|C|x> engines, or the
+//            sandwich engines of one measured-qubit set), resident in HBM, plus its
+//            boundary map.
+//   Plan     the job/item layout of one launch shape (targets x boundary counts), its
+//            device buffers and the captured CUDA graph (prepare -> counter reset ->
+//            persistent enumeration -> job reduce -> output reduce).  Simulator calls
+//            cache one plan per boundary count; pq_batch owns one plan over many targets.
+//   pq_sim   Simulator::with_options (src/sim.rs:144-148): compiled path sum, rank
+//            strategy, main target, cached marginal targets, stream.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "pq_host.hpp"
+#include "pq_kernels.cuh"
+#include "polyq_gb300.h"
+
+namespace pq {
+
+thread_local std::string g_err;
+static std::mutex g_mu;
+static int g_device = 0;
+static pq_tuning g_tuning = {10, 4, 8, 48};
+
+static pq_status fail(pq_status s, const std::string &m) {
+    g_err = m;
+    return s;
+}
+static pq_status cuda_fail(cudaError_t e, const char *what) {
+    return fail(e == cudaErrorMemoryAllocation ? PQ_ERR_OUT_OF_MEMORY : PQ_ERR_DEVICE,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define CU(x)                                           \
+    do {                                                \
+        cudaError_t e_ = (x);                           \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #x); \
+    } while (0)
+
+static double now_s() {
+    using namespace std::chrono;
+    return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+// ------------------------------------------------------------------------ device memory
+struct DevMem {
+    void *p = nullptr;
+    size_t n = 0;
+    DevMem() = default;
+    DevMem(const DevMem &) = delete;
+    DevMem &operator=(const DevMem &) = delete;
+    ~DevMem() { reset(); }
+    void reset() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    cudaError_t alloc(size_t bytes) {
+        reset();
+        n = std::max<size_t>(bytes, 16);
+        return cudaMalloc(&p, n);
+    }
+    template <class T> T *as() const { return reinterpret_cast<T *>(p); }
+};
+struct HostPinned {
+    void *p = nullptr;
+    size_t n = 0;
+    HostPinned() = default;
+    HostPinned(const HostPinned &) = delete;
+    HostPinned &operator=(const HostPinned &) = delete;
+    ~HostPinned() {
+        if (p) cudaFreeHost(p);
+    }
+    cudaError_t alloc(size_t bytes) {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = std::max<size_t>(bytes, 16);
+        return cudaMallocHost(&p, n);
+    }
+    template <class T> T *as() const { return reinterpret_cast<T *>(p); }
+};
+template <class T> static cudaError_t upload(DevMem &m, const std::vector<T> &v) {
+    cudaError_t e = m.alloc(v.size() * sizeof(T));
+    if (e != cudaSuccess) return e;
+    if (!v.empty()) e = cudaMemcpy(m.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+    return e;
+}
+
+// ------------------------------------------------------------------------ targets
+struct Target {
+    RankSet rs;
+    IoMapHost iom;
+    std::vector<std::unique_ptr<DevMem>> mem;  // one blob per branch engine
+    std::vector<EngineDev> dev;                // rebased onto device addresses
+    DevMem iom_mem;
+    IoMapDev iom_dev{};
+    int64_t bytes = 0;
+    double branches_per_amp = 0.0;
+    int max_d = 0, max_rank = 0, max_words = 0;
+};
+
+static pq_status upload_target(Target &T, int di_max) {
+    T.bytes = 0;
+    T.branches_per_amp = 0.0;
+    for (auto &e : T.rs.branches) {
+        EngineTables tb = build_tables(*e, di_max);
+        PackedEngine pk = pack_engine(*e, tb);
+        auto m = std::make_unique<DevMem>();
+        CU(m->alloc(pk.blob.size()));
+        CU(cudaMemcpy(m->p, pk.blob.data(), pk.blob.size(), cudaMemcpyHostToDevice));
+        T.dev.push_back(rebase_engine(pk.off, reinterpret_cast<const uint8_t *>(m->p)));
+        T.bytes += (int64_t)m->n;
+        T.mem.push_back(std::move(m));
+        T.branches_per_amp += std::ldexp(1.0, e->d);
+        T.max_d = std::max(T.max_d, e->d);
+        T.max_rank = std::max(T.max_rank, e->rank);
+        T.max_words = std::max(T.max_words, e->L.full() + e->wf + 2);
+    }
+    // boundary map: src | cf_pos | cf_src in one allocation
+    std::vector<int32_t> blob;
+    blob.insert(blob.end(), T.iom.src.begin(), T.iom.src.end());
+    blob.insert(blob.end(), T.iom.cf_pos.begin(), T.iom.cf_pos.end());
+    blob.insert(blob.end(), T.iom.cf_src.begin(), T.iom.cf_src.end());
+    CU(upload(T.iom_mem, blob));
+    const int32_t *base = T.iom_mem.as<int32_t>();
+    T.iom_dev.nf = (int)T.iom.src.size();
+    T.iom_dev.ncf = (int)T.iom.cf_pos.size();
+    T.iom_dev.src = base;
+    T.iom_dev.cf_pos = base + T.iom.src.size();
+    T.iom_dev.cf_src = base + T.iom.src.size() + T.iom.cf_pos.size();
+    T.bytes += (int64_t)T.iom_mem.n;
+    for (auto &e : T.rs.branches)
+        if ((int)T.iom.src.size() != e->nf) return fail(PQ_ERR_INTERNAL, "boundary map does not match engine");
+    return PQ_OK;
+}
+
+// ------------------------------------------------------------------------ plans
+struct Segment {
+    Target *tg;
+    int64_t count;
+};
+
+struct Plan {
+    int nw = 1;
+    int64_t nreq = 0;
+    int njobs = 0, nout = 0;
+    long long nitems = 0;
+    double branches = 0.0;  // branches enumerated per run (vanishing boundaries included)
+    int smem_words = 8;
+    int grid_prep = 1, grid_enum = 1, block_enum = 256;
+    bool graph_ready = false;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    DevMem engines, maps, jobs, perm, kinv, istart, jdl, jcpi, jnch, partials, counter, job_vals, job_err, out_jobs,
+        x, y, out, err, errflag;
+    HostPinned hx, hy, hout, herr, herrflag;
+    std::vector<int> job_engine_d;
+    std::vector<JobDev> jobs_host;
+    KArgs args{};
+    ~Plan() {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        if (graph) cudaGraphDestroy(graph);
+        if (own_stream && stream) cudaStreamDestroy(stream);
+    }
+};
+
+static int sm_count() {
+    static int n = 0;
+    if (!n) {
+        cudaDeviceProp p;
+        if (cudaGetDeviceProperties(&p, g_device) == cudaSuccess) n = p.multiProcessorCount;
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+// Work decomposition of one job (fixed per job, so a boundary's result does not depend on
+// what else shares the launch): chunks of 2^dl Gray steps, 32 * cpl chunks per item.
+static void job_shape(int d, int DI, int cpl, int &dl, unsigned long long &nch, unsigned &cpi) {
+    dl = d <= 5 ? 0 : std::min(d - 5, DI);
+    nch = 1ull << (d - dl);
+    unsigned long long per = 32ull * (unsigned long long)cpl;
+    // at most 2^16 items per job so partial buffers stay bounded
+    while ((nch + per - 1) / per > (1ull << 16)) per *= 2;
+    cpi = (unsigned)std::min<unsigned long long>(nch, per);
+}
+
+static pq_status build_plan(const std::vector<Segment> &segs, int nw, cudaStream_t stream, const pq_tuning &tu,
+                            Plan &P) {
+    P.nw = nw;
+    P.stream = stream;
+    if (!P.stream) {
+        CU(cudaStreamCreateWithFlags(&P.stream, cudaStreamNonBlocking));
+        P.own_stream = true;
+    }
+    std::vector<EngineDev> eng;
+    std::vector<IoMapDev> maps;
+    std::vector<JobDev> jobs;
+    std::vector<int> out_jobs;
+    std::vector<int> jd;
+    int64_t req = 0;
+    int maxw = 8;
+    for (size_t si = 0; si < segs.size(); si++) {
+        Target *T = segs[si].tg;
+        const int ebase = (int)eng.size();
+        for (auto &e : T->dev) {
+            if (e.d > kMaxD || e.rank > kMaxPivots) return fail(PQ_ERR_UNSUPPORTED, "branch engine outside kernel limits");
+            if (e.d > tu.max_branch_dim)
+                return fail(PQ_ERR_ADMISSION_REFUSED, "branch dimension " + std::to_string(e.d) + " above the cap " +
+                                                          std::to_string(tu.max_branch_dim));
+            eng.push_back(e);
+        }
+        maps.push_back(T->iom_dev);
+        maxw = std::max(maxw, T->max_words);
+        for (int64_t r = 0; r < segs[si].count; r++, req++) {
+            out_jobs.push_back((int)jobs.size());
+            for (size_t b = 0; b < T->dev.size(); b++) {
+                JobDev J;
+                std::memset(&J, 0, sizeof(J));
+                J.engine = ebase + (int)b;
+                J.iomap = (int)si;
+                J.req = (int)req;
+                J.out = (int)req;
+                jobs.push_back(J);
+                jd.push_back(T->dev[b].d);
+            }
+        }
+    }
+    out_jobs.push_back((int)jobs.size());
+    P.nreq = req;
+    P.njobs = (int)jobs.size();
+    P.nout = (int)req;
+    P.smem_words = maxw;
+    if (P.njobs == 0) return fail(PQ_ERR_INVALID_ARG, "empty launch");
+    // item layout: jobs in decreasing branch dimension (longest work first)
+    std::vector<int> perm((size_t)P.njobs), kinv((size_t)P.njobs), jdl((size_t)P.njobs);
+    std::vector<unsigned> jcpi((size_t)P.njobs);
+    std::vector<unsigned long long> jnch((size_t)P.njobs);
+    for (int j = 0; j < P.njobs; j++) perm[j] = j;
+    std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) { return jd[a] > jd[b]; });
+    std::vector<long long> istart((size_t)P.njobs + 1, 0);
+    P.branches = 0.0;
+    for (int k = 0; k < P.njobs; k++) {
+        int j = perm[k];
+        kinv[j] = k;
+        const EngineDev &E = eng[jobs[j].engine];
+        job_shape(E.d, E.DI, tu.chunks_per_lane, jdl[j], jnch[j], jcpi[j]);
+        istart[k + 1] = istart[k] + (long long)((jnch[j] + jcpi[j] - 1) / jcpi[j]);
+        P.branches += std::ldexp(1.0, E.d);
+    }
+    P.nitems = istart[P.njobs];
+    CU(upload(P.engines, eng));
+    CU(upload(P.maps, maps));
+    CU(upload(P.jobs, jobs));
+    CU(upload(P.perm, perm));
+    CU(upload(P.kinv, kinv));
+    CU(upload(P.istart, istart));
+    CU(upload(P.jdl, jdl));
+    CU(upload(P.jcpi, jcpi));
+    CU(upload(P.jnch, jnch));
+    CU(upload(P.out_jobs, out_jobs));
+    CU(P.partials.alloc((size_t)P.nitems * sizeof(double2)));
+    CU(P.counter.alloc(sizeof(unsigned long long)));
+    CU(P.job_vals.alloc((size_t)P.njobs * sizeof(double2)));
+    CU(P.job_err.alloc((size_t)P.njobs * sizeof(double)));
+    CU(P.x.alloc((size_t)P.nreq * nw * 8));
+    CU(P.y.alloc((size_t)P.nreq * nw * 8));
+    CU(P.out.alloc((size_t)P.nout * 2 * sizeof(double)));
+    CU(P.err.alloc((size_t)P.nout * sizeof(double)));
+    CU(P.errflag.alloc(sizeof(int)));
+    CU(P.hx.alloc((size_t)P.nreq * nw * 8));
+    CU(P.hy.alloc((size_t)P.nreq * nw * 8));
+    CU(P.hout.alloc((size_t)P.nout * 2 * sizeof(double)));
+    CU(P.herr.alloc((size_t)P.nout * sizeof(double)));
+    CU(P.herrflag.alloc(sizeof(int)));
+    P.jobs_host = jobs;
+    KArgs &a = P.args;
+    a.engines = P.engines.as<EngineDev>();
+    a.maps = P.maps.as<IoMapDev>();
+    a.jobs = P.jobs.as<JobDev>();
+    a.njobs = P.njobs;
+    a.perm = P.perm.as<int>();
+    a.kinv = P.kinv.as<int>();
+    a.istart = P.istart.as<long long>();
+    a.jdl = P.jdl.as<int>();
+    a.jcpi = P.jcpi.as<unsigned>();
+    a.jnch = P.jnch.as<unsigned long long>();
+    a.nitems = P.nitems;
+    a.partials = P.partials.as<double2>();
+    a.counter = P.counter.as<unsigned long long>();
+    a.job_vals = P.job_vals.as<double2>();
+    a.job_err = P.job_err.as<double>();
+    a.out_jobs = P.out_jobs.as<int>();
+    a.nout = P.nout;
+    a.out = P.out.as<double>();
+    a.err = P.err.as<double>();
+    a.out_prob = 0;
+    a.xs = P.x.as<uint64_t>();
+    a.ys = P.y.as<uint64_t>();
+    a.nw = nw;
+    a.smem_words = P.smem_words;
+    a.dbg = nullptr;
+    a.errflag = P.errflag.as<int>();
+    const int bw = std::max(1, std::min(8, tu.block_warps));
+    P.block_enum = 32 * bw;
+    int occ = 0;
+    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, enum_kernel<0>, P.block_enum, 0));
+    occ = std::max(occ, 1);
+    long long want = (long long)sm_count() * occ;
+    P.grid_enum = (int)std::max(1LL, std::min<long long>(want, (P.nitems + bw - 1) / bw));
+    P.grid_prep = std::max(1, std::min((P.njobs + 3) / 4, 65535));
+    if ((size_t)4 * P.smem_words * 8 > 48 * 1024) {
+        CU(cudaFuncSetAttribute(prepare_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(4 * P.smem_words * 8)));
+    }
+    return PQ_OK;
+}
+
+// Enqueue the core launch sequence on P.stream (capturable).
+static cudaError_t enqueue_core(Plan &P, int mode) {
+    cudaError_t e;
+    e = cudaMemsetAsync(P.errflag.p, 0, sizeof(int), P.stream);
+    if (e != cudaSuccess) return e;
+    prepare_kernel<<<P.grid_prep, 128, (size_t)4 * P.smem_words * 8, P.stream>>>(P.args);
+    e = cudaMemsetAsync(P.counter.p, 0, sizeof(unsigned long long), P.stream);
+    if (e != cudaSuccess) return e;
+    if (mode == 1) enum_kernel<1><<<P.grid_enum, P.block_enum, 0, P.stream>>>(P.args);
+    else enum_kernel<0><<<P.grid_enum, P.block_enum, 0, P.stream>>>(P.args);
+    job_reduce_kernel<<<(P.njobs + 255) / 256, 256, 0, P.stream>>>(P.args);
+    out_reduce_kernel<<<(P.nout + 255) / 256, 256, 0, P.stream>>>(P.args);
+    return cudaGetLastError();
+}
+
+static pq_status launch_graph(Plan &P) {
+    if (!P.graph_ready) {
+        CU(cudaStreamBeginCapture(P.stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = enqueue_core(P, 0);
+        cudaGraph_t g = nullptr;
+        cudaError_t e2 = cudaStreamEndCapture(P.stream, &g);
+        if (e != cudaSuccess) { if (g) cudaGraphDestroy(g); return cuda_fail(e, "capture"); }
+        if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
+        P.graph = g;
+        CU(cudaGraphInstantiate(&P.gexec, P.graph, 0));
+        P.graph_ready = true;
+    }
+    CU(cudaGraphLaunch(P.gexec, P.stream));
+    return PQ_OK;
+}
+
+// Host-buffer run: H2D boundaries, graph, D2H results, wait.
+static pq_status run_host(Plan &P, const uint64_t *x, const uint64_t *y, double *out, double *err, bool prob) {
+    const size_t bw = (size_t)P.nreq * P.nw * 8;
+    std::memcpy(P.hx.p, x, bw);
+    std::memcpy(P.hy.p, y, bw);
+    CU(cudaMemcpyAsync(P.x.p, P.hx.p, bw, cudaMemcpyHostToDevice, P.stream));
+    CU(cudaMemcpyAsync(P.y.p, P.hy.p, bw, cudaMemcpyHostToDevice, P.stream));
+    pq_status st = launch_graph(P);
+    if (st != PQ_OK) return st;
+    CU(cudaMemcpyAsync(P.hout.p, P.out.p, (size_t)P.nout * 16, cudaMemcpyDeviceToHost, P.stream));
+    CU(cudaMemcpyAsync(P.herr.p, P.err.p, (size_t)P.nout * 8, cudaMemcpyDeviceToHost, P.stream));
+    CU(cudaMemcpyAsync(P.herrflag.p, P.errflag.p, sizeof(int), cudaMemcpyDeviceToHost, P.stream));
+    CU(cudaStreamSynchronize(P.stream));
+    if (*P.herrflag.as<int>()) return fail(PQ_ERR_INTERNAL, "device self-check failed (odd Z8 increment)");
+    const double *ho = P.hout.as<double>();
+    const double *he = P.herr.as<double>();
+    if (prob) {
+        // Probabilities are promised to 1e-12 absolute: when the FP32 bound cannot certify
+        // that, the same launch shape is re-run with FP64 weights and FP64 accumulation.
+        bool escalate = false;
+        for (int o = 0; o < P.nout && !escalate; o++) {
+            double a = std::sqrt(ho[2 * o] * ho[2 * o] + ho[2 * o + 1] * ho[2 * o + 1]);
+            escalate = he[o] * (2.0 * a + he[o]) > 1e-12;
+        }
+        if (escalate) {
+            CU(enqueue_core(P, 1));
+            CU(cudaMemcpyAsync(P.hout.p, P.out.p, (size_t)P.nout * 16, cudaMemcpyDeviceToHost, P.stream));
+            CU(cudaStreamSynchronize(P.stream));
+            double *hw = P.herr.as<double>();
+            for (int o = 0; o < P.nout; o++) hw[o] = 0.0;  // FP64 path: rounding far below 1e-12
+        }
+    }
+    for (int o = 0; o < P.nout; o++) {
+        if (prob) {
+            double re = ho[2 * o], im = ho[2 * o + 1];
+            out[o] = re * re + im * im;
+        } else {
+            out[2 * o] = ho[2 * o];
+            out[2 * o + 1] = ho[2 * o + 1];
+        }
+        if (err) err[o] = prob ? he[o] * (2.0 * std::sqrt(ho[2 * o] * ho[2 * o] + ho[2 * o + 1] * ho[2 * o + 1]) + he[o]) : he[o];
+    }
+    return PQ_OK;
+}
+
+// Device-buffer run on `stream` (no host synchronisation).
+static pq_status run_device(Plan &P, const uint64_t *x, const uint64_t *y, double *out, double *err,
+                            cudaStream_t stream) {
+    const size_t bw = (size_t)P.nreq * P.nw * 8;
+    cudaStream_t s = stream ? stream : P.stream;
+    cudaEvent_t ev = nullptr;
+    if (s != P.stream) {  // order the plan's stream after the caller's
+        CU(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        CU(cudaEventRecord(ev, s));
+        CU(cudaStreamWaitEvent(P.stream, ev, 0));
+    }
+    if (x != P.x.as<uint64_t>()) CU(cudaMemcpyAsync(P.x.p, x, bw, cudaMemcpyDeviceToDevice, P.stream));
+    if (y != P.y.as<uint64_t>()) CU(cudaMemcpyAsync(P.y.p, y, bw, cudaMemcpyDeviceToDevice, P.stream));
+    pq_status st = launch_graph(P);
+    if (st != PQ_OK) return st;
+    if (out && out != P.out.as<double>())
+        CU(cudaMemcpyAsync(out, P.out.p, (size_t)P.nout * 16, cudaMemcpyDeviceToDevice, P.stream));
+    if (err && err != P.err.as<double>())
+        CU(cudaMemcpyAsync(err, P.err.p, (size_t)P.nout * 8, cudaMemcpyDeviceToDevice, P.stream));
+    if (ev) {
+        CU(cudaEventRecord(ev, P.stream));
+        CU(cudaStreamWaitEvent(s, ev, 0));
+        cudaEventDestroy(ev);
+    }
+    return PQ_OK;
+}
+
+}  // namespace pq
+
+using namespace pq;
+
+// ------------------------------------------------------------------------ simulator
+struct pq_sim {
+    int device = 0;
+    Circuit circ;
+    PathSum ps;
+    int strategy = 0, pairs = 0;
+    int di_max = 10;
+    int nw = 1;
+    bool host_only = false;
+    Target main;
+    cudaStream_t stream = nullptr;
+    double build_s = 0.0;
+    std::mutex mu;
+    std::map<int64_t, std::unique_ptr<Plan>> plans;
+    bool have_sw = false;
+    PathSum sw;
+    std::vector<int> junction;
+    std::vector<uint8_t> jneg;
+    struct Marg {
+        Target tg;
+        std::unique_ptr<Plan> plan;
+    };
+    std::map<std::vector<int>, std::unique_ptr<Marg>> marg;
+    ~pq_sim() {
+        plans.clear();
+        marg.clear();
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+struct pq_batch {
+    std::vector<pq_sim *> sims;
+    std::unique_ptr<Plan> plan;
+    std::mutex mu;
+};
+
+static int words_for(int nq) { return std::max(1, (nq + 63) / 64); }
+
+// puts for <y|C|x> (src/pathsum.rs:430-450)
+static IoMapHost main_iomap(const PathSum &ps) {
+    std::vector<std::pair<int, int32_t>> puts;
+    for (int q = 0; q < ps.nq; q++) puts.push_back({q, io_src(q, 0, 0)});
+    for (int q = 0; q < ps.nq; q++) puts.push_back({ps.outputs[q], io_src(q, 1, ps.out_neg[q])});
+    return build_iomap(puts);
+}
+
+extern "C" {
+
+PQ_API const char *pq_version(void) { return "polyq-gb300 1.0 (sm_103a)"; }
+PQ_API const char *pq_last_error(void) { return g_err.c_str(); }
+
+PQ_API pq_status pq_init(int32_t device) {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) return fail(PQ_ERR_NO_DEVICE, "no CUDA device visible");
+    if (device < 0 || device >= n) return fail(PQ_ERR_INVALID_ARG, "device index out of range");
+    g_device = device;
+    CU(cudaSetDevice(device));
+    return PQ_OK;
+}
+
+PQ_API pq_status pq_set_default_tuning(const pq_tuning *t) {
+    if (!t) return fail(PQ_ERR_INVALID_ARG, "null tuning");
+    std::lock_guard<std::mutex> lk(g_mu);
+    pq_tuning n = g_tuning;
+    if (t->inner_dims) {
+        if (t->inner_dims < 4 || t->inner_dims > 14) return fail(PQ_ERR_INVALID_ARG, "inner_dims must be in 4..14");
+        n.inner_dims = t->inner_dims;
+    }
+    if (t->chunks_per_lane) {
+        if (t->chunks_per_lane < 1 || t->chunks_per_lane > 64) return fail(PQ_ERR_INVALID_ARG, "chunks_per_lane in 1..64");
+        n.chunks_per_lane = t->chunks_per_lane;
+    }
+    if (t->block_warps) {
+        if (t->block_warps < 1 || t->block_warps > 8) return fail(PQ_ERR_INVALID_ARG, "block_warps in 1..8");
+        n.block_warps = t->block_warps;
+    }
+    if (t->max_branch_dim) {
+        if (t->max_branch_dim < 1 || t->max_branch_dim > kMaxD) return fail(PQ_ERR_INVALID_ARG, "max_branch_dim in 1..62");
+        n.max_branch_dim = t->max_branch_dim;
+    }
+    g_tuning = n;
+    return PQ_OK;
+}
+PQ_API pq_status pq_get_default_tuning(pq_tuning *t) {
+    if (!t) return fail(PQ_ERR_INVALID_ARG, "null tuning");
+    std::lock_guard<std::mutex> lk(g_mu);
+    *t = g_tuning;
+    return PQ_OK;
+}
+
+static pq_status sim_build_host(const pq_circuit_desc *c, int32_t strategy, int32_t pairs, std::unique_ptr<pq_sim> &S) {
+    if (!c) return fail(PQ_ERR_INVALID_ARG, "null argument");
+    if (strategy < 0 || strategy > 2) return fail(PQ_ERR_INVALID_ARG, "strategy must be 0 (auto), 1 (cached) or 2 (pairs)");
+    if (strategy == 2 && pairs < 0) return fail(PQ_ERR_INVALID_ARG, "negative pair count");
+    std::string why = validate_circuit(c->num_qubits, c->num_gates, c->op, c->q0, c->q1);
+    if (!why.empty()) return fail(PQ_ERR_INVALID_ARG, why);
+    if (c->num_gates > 0 && !c->phase) return fail(PQ_ERR_INVALID_ARG, "null phase array");
+    S = std::make_unique<pq_sim>();
+    S->device = g_device;
+    S->circ.nq = c->num_qubits;
+    for (int i = 0; i < c->num_gates; i++) S->circ.gates.push_back(Gate{c->op[i], c->q0[i], c->q1[i], c->phase[i]});
+    S->strategy = strategy;
+    S->pairs = pairs;
+    S->nw = words_for(c->num_qubits);
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        S->di_max = g_tuning.inner_dims;
+    }
+    try {
+        S->ps = PathSum::compile(S->circ);
+        S->main.iom = main_iomap(S->ps);
+        S->main.rs = build_rank(S->ps, S->main.iom.fixed, strategy, pairs);
+    } catch (const std::exception &e) {
+        return fail(PQ_ERR_INTERNAL, std::string("engine build: ") + e.what());
+    }
+    S->main.branches_per_amp = 0.0;
+    for (auto &e : S->main.rs.branches) S->main.branches_per_amp += std::ldexp(1.0, e->d);
+    return PQ_OK;
+}
+
+PQ_API pq_status pq_sim_create(const pq_circuit_desc *c, int32_t strategy, int32_t pairs, pq_sim **out) {
+    if (!c || !out) return fail(PQ_ERR_INVALID_ARG, "null argument");
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(PQ_ERR_NO_DEVICE, "no CUDA device visible");
+    const double t0 = now_s();
+    std::unique_ptr<pq_sim> S;
+    pq_status st = sim_build_host(c, strategy, pairs, S);
+    if (st != PQ_OK) return st;
+    CU(cudaSetDevice(S->device));
+    st = upload_target(S->main, S->di_max);
+    if (st != PQ_OK) return st;
+    CU(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
+    S->build_s = now_s() - t0;
+    *out = S.release();
+    return PQ_OK;
+}
+
+PQ_API pq_status pq_analyze(const pq_circuit_desc *c, int32_t strategy, int32_t pairs, pq_sim **out) {
+    if (!c || !out) return fail(PQ_ERR_INVALID_ARG, "null argument");
+    *out = nullptr;
+    const double t0 = now_s();
+    std::unique_ptr<pq_sim> S;
+    pq_status st = sim_build_host(c, strategy, pairs, S);
+    if (st != PQ_OK) return st;
+    S->host_only = true;
+    S->build_s = now_s() - t0;
+    *out = S.release();
+    return PQ_OK;
+}
+
+PQ_API void pq_sim_destroy(pq_sim *s) {
+    if (!s) return;
+    if (s->host_only) {
+        delete s;
+        return;
+    }
+    cudaSetDevice(s->device);
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    delete s;
+}
+
+PQ_API pq_status pq_sim_stats(const pq_sim *s, pq_stats *o) {
+    if (!s || !o) return fail(PQ_ERR_INVALID_ARG, "null argument");
+    const HostEngine &e = *s->main.rs.branches[0];
+    o->free_vars = e.m;
+    o->planes = e.L.g;
+    o->lines = e.L.nodd;
+    o->radical = e.L.neven;
+    o->terms = e.t;
+    o->branch_dim = e.d;
+    o->pairs = s->main.rs.pairs;
+    o->num_branches = (int64_t)s->main.rs.branches.size();
+    o->branches_per_amplitude = (int64_t)s->main.branches_per_amp;
+    o->device_bytes = s->main.bytes;
+    o->build_seconds = s->build_s;
+    return PQ_OK;
+}
+
+static pq_status sim_plan(pq_sim *s, int64_t n, Plan **out) {
+    if (s->host_only) return fail(PQ_ERR_NO_DEVICE, "simulator was created by pq_analyze (host structures only)");
+    auto it = s->plans.find(n);
+    if (it != s->plans.end()) {
+        *out = it->second.get();
+        return PQ_OK;
+    }
+    pq_tuning tu;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        tu = g_tuning;
+    }
+    auto P = std::make_unique<Plan>();
+    std::vector<Segment> segs{{&s->main, n}};
+    pq_status st = build_plan(segs, s->nw, s->stream, tu, *P);
+    if (st != PQ_OK) return st;
+    *out = P.get();
+    s->plans[n] = std::move(P);
+    return PQ_OK;
+}
+
+static pq_status check_n(int64_t n) {
+    if (n <= 0 || n > (1LL << 24)) return fail(PQ_ERR_INVALID_ARG, "boundary count must be in 1..2^24");
+    return PQ_OK;
+}
+
+PQ_API pq_status pq_amplitudes(pq_sim *s, int64_t n, const uint64_t *x, const uint64_t *y, double *out,
+                               double *errbound) {
+    if (!s || !x || !y || !out) return fail(PQ_ERR_INVALID_ARG, "null argument");
+    pq_status st = check_n(n);
+    if (st != PQ_OK) return st;
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->host_only) return fail(PQ_ERR_NO_DEVICE, "simulator was created by pq_analyze (host structures only)");
+    CU(cudaSetDevice(s->device));
+    Plan *P = nullptr;
+    st = sim_plan(s, n, &P);
+    if (st != PQ_OK) return st;
+    return run_host(*P, x, y, out, errbound, false);
+}
+
+PQ_API pq_status pq_probabilities(pq_sim *s, int64_t n, const uint64_t *x, const uint64_t *y, double *out) {
+    if (!s || !x || !y || !out) return fail(PQ_ERR_INVALID_ARG, "null argument");
+    pq_status st = check_n(n);
+    if (st != PQ_OK) return st;
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->host_only) return fail(PQ_ERR_NO_DEVICE, "simulator was created by pq_analyze (host structures only)");
+    CU(cudaSetDevice(s->device));
+    Plan *P = nullptr;
+    st = sim_plan(s, n, &P);
+    if (st != PQ_OK) return st;
+    return run_host(*P, x, y, out, nullptr, true);
+}
+
+PQ_API pq_status pq_amplitudes_device(pq_sim *s, int64_t n, const uint64_t *x, const uint64_t *y, double *out,
+                                      double *errbound, void *stream) {
+    if (!s || !x || !y || !out) return fail(PQ_ERR_INVALID_ARG, "null argument");
+    pq_status st = check_n(n);
+    if (st != PQ_OK) return st;
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->host_only) return fail(PQ_ERR_NO_DEVICE, "simulator was created by pq_analyze (host structures only)");
+    CU(cudaSetDevice(s->device));
+    Plan *P = nullptr;
+    st = sim_plan(s, n, &P);
+    if (st != PQ_OK) return st;
+    return run_device(*P, x, y, out, errbound, (cudaStream_t)stream);
+}
+
+PQ_API pq_status pq_amplitudes_plain(pq_sim *s, int64_t n, const uint64_t *x, const uint64_t *y, double *out) {
+    if (!s || !x || !y || !out) return fail(PQ_ERR_INVALID_ARG, "null argument");
+    pq_status st = check_n(n);
+    if (st != PQ_OK) return st;
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->host_only) return fail(PQ_ERR_NO_DEVICE, "simulator was created by pq_analyze (host structures only)");
+    CU(cudaSetDevice(s->device));
+    Plan *P = nullptr;
+    st = sim_plan(s, 1, &P);
+    if (st != PQ_OK) return st;
+    for (int64_t i = 0; i < n; i++) {
+        st = run_host(*P, x + (size_t)i * s->nw, y + (size_t)i * s->nw, out + 2 * i, nullptr, false);
+        if (st != PQ_OK) return st;
+    }
+    return PQ_OK;
+}
+
+PQ_API pq_status pq_amplitudes_fp64(pq_sim *s, int64_t n, const uint64_t *x, const uint64_t *y, double *out) {
+    if (!s || !x || !y || !out) return fail(PQ_ERR_INVALID_ARG, "null argument");
+    pq_status st = check_n(n);
+    if (st != PQ_OK) return st;
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->host_only) return fail(PQ_ERR_NO_DEVICE, "simulator was created by pq_analyze (host structures only)");
+    CU(cudaSetDevice(s->device));
+    Plan *P = nullptr;
+    st = sim_plan(s, n, &P);
+    if (st != PQ_OK) return st;
+    const size_t bw = (size_t)n * s->nw * 8;
+    CU(cudaMemcpyAsync(P->x.p, x, bw, cudaMemcpyHostToDevice, P->stream));
+    CU(cudaMemcpyAsync(P->y.p, y, bw, cudaMemcpyHostToDevice, P->stream));
+    CU(enqueue_core(*P, 1));
+    CU(cudaMemcpyAsync(out, P->out.p, (size_t)n * 16, cudaMemcpyDeviceToHost, P->stream));
+    CU(cudaStreamSynchronize(P->stream));
+    return PQ_OK;
+}
+
+PQ_API pq_status pq_marginal(pq_sim *s, const uint64_t *x, int32_t nmeas, const int32_t *qubits,
+                             const uint8_t *outcomes, double *out) {
+    if (!s || !x || !out || nmeas < 0 || (nmeas > 0 && (!qubits || !outcomes)))
+        return fail(PQ_ERR_INVALID_ARG, "null argument");
+    const int nq = s->circ.nq;
+    if (s->host_only) return fail(PQ_ERR_NO_DEVICE, "simulator was created by pq_analyze (host structures only)");
+    for (int i = 0; i < nmeas; i++)
+        if (qubits[i] < 0 || qubits[i] >= nq) return fail(PQ_ERR_INVALID_ARG, "measured qubit out of range");
+    std::lock_guard<std::mutex> lk(s->mu);
+    CU(cudaSetDevice(s->device));
+    if (!s->have_sw) {
+        s->sw = PathSum::sandwich(s->circ, s->junction, s->jneg);
+        s->have_sw = true;
+    }
+    // puts of Sandwich::assignment (src/sim.rs:105-124); the engine's fixed set is the
+    // first-occurrence order of these variables (= io_vars + measured junctions, sim.rs:95-103)
+    std::vector<std::pair<int, int32_t>> puts;
+    for (int q = 0; q < nq; q++) puts.push_back({q, io_src(q, 0, 0)});
+    for (int q = 0; q < nq; q++) puts.push_back({s->sw.outputs[q], io_src(q, 0, s->sw.out_neg[q])});
+    std::vector<int> key;
+    for (int i = 0; i < nmeas; i++) {
+        puts.push_back({s->junction[qubits[i]], io_src(qubits[i], 1, s->jneg[qubits[i]])});
+        key.push_back(qubits[i]);
+    }
+    auto it = s->marg.find(key);
+    if (it == s->marg.end()) {
+        auto M = std::make_unique<pq_sim::Marg>();
+        M->tg.iom = build_iomap(puts);
+        try {
+            M->tg.rs = build_rank(s->sw, M->tg.iom.fixed, s->strategy, s->pairs);
+        } catch (const std::exception &e) {
+            return fail(PQ_ERR_INTERNAL, std::string("marginal engine build: ") + e.what());
+        }
+        pq_status st = upload_target(M->tg, s->di_max);
+        if (st != PQ_OK) return st;
+        pq_tuning tu;
+        {
+            std::lock_guard<std::mutex> lk2(g_mu);
+            tu = g_tuning;
+        }
+        M->plan = std::make_unique<Plan>();
+        std::vector<Segment> segs{{&M->tg, 1}};
+        st = build_plan(segs, s->nw, s->stream, tu, *M->plan);
+        if (st != PQ_OK) return st;
+        it = s->marg.emplace(key, std::move(M)).first;
+    }
+    std::vector<uint64_t> yv((size_t)s->nw, 0ull);
+    for (int i = 0; i < nmeas; i++)
+        if (outcomes[i]) yv[qubits[i] >> 6] |= 1ull << (qubits[i] & 63);
+    // repeated measured qubits with different outcomes contradict: the map's check makes it 0
+    double amp[2];
+    pq_status st = run_host(*it->second->plan, x, yv.data(), amp, nullptr, false);
+    if (st != PQ_OK) return st;
+    *out = amp[0] > 0.0 ? amp[0] : 0.0;
+    return PQ_OK;
+}
+
+// ---------------------------------------------------------------- batches
+PQ_API pq_status pq_batch_create(int32_t nsims, pq_sim *const *sims, const int64_t *counts, pq_batch **out) {
+    if (nsims <= 0 || !sims || !counts || !out) return fail(PQ_ERR_INVALID_ARG, "null argument");
+    *out = nullptr;
+    auto B = std::make_unique<pq_batch>();
+    std::vector<Segment> segs;
+    int nw = 1;
+    int64_t tot = 0;
+    for (int i = 0; i < nsims; i++) {
+        if (!sims[i] || counts[i] < 0) return fail(PQ_ERR_INVALID_ARG, "bad simulator or count");
+        if (sims[i]->host_only) return fail(PQ_ERR_NO_DEVICE, "host-only simulator in a batch");
+        if (sims[i]->device != g_device) return fail(PQ_ERR_INVALID_ARG, "simulators on different devices");
+        B->sims.push_back(sims[i]);
+        segs.push_back({&sims[i]->main, counts[i]});
+        nw = std::max(nw, sims[i]->nw);
+        tot += counts[i];
+    }
+    if (tot <= 0 || tot > (1LL << 24)) return fail(PQ_ERR_INVALID_ARG, "total boundary count must be in 1..2^24");
+    pq_tuning tu;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        tu = g_tuning;
+    }
+    CU(cudaSetDevice(g_device));
+    B->plan = std::make_unique<Plan>();
+    pq_status st = build_plan(segs, nw, nullptr, tu, *B->plan);
+    if (st != PQ_OK) return st;
+    *out = B.release();
+    return PQ_OK;
+}
+PQ_API void pq_batch_destroy(pq_batch *b) {
+    if (!b) return;
+    if (b->plan && b->plan->stream) cudaStreamSynchronize(b->plan->stream);
+    delete b;
+}
+PQ_API int32_t pq_batch_words(const pq_batch *b) { return b ? b->plan->nw : 0; }
+PQ_API int64_t pq_batch_branches(const pq_batch *b) { return b ? (int64_t)b->plan->branches : 0; }
+PQ_API pq_status pq_batch_run(pq_batch *b, const uint64_t *x, const uint64_t *y, double *out, double *err) {
+    if (!b || !x || !y || !out) return fail(PQ_ERR_INVALID_ARG, "null argument");
+    std::lock_guard<std::mutex> lk(b->mu);
+    return run_host(*b->plan, x, y, out, err, false);
+}
+PQ_API pq_status pq_batch_run_device(pq_batch *b, const uint64_t *x, const uint64_t *y, double *out, double *err,
+                                     void *stream) {
+    if (!b || !x || !y || !out) return fail(PQ_ERR_INVALID_ARG, "null argument");
+    std::lock_guard<std::mutex> lk(b->mu);
+    return run_device(*b->plan, x, y, out, err, (cudaStream_t)stream);
+}
+
+// ---------------------------------------------------------------- checks
+PQ_API int64_t pq_debug_engine_dump(const pq_sim *s, int32_t branch, uint64_t *out, int64_t cap) {
+    if (!s || branch < 0 || branch >= (int)s->main.rs.branches.size()) {
+        g_err = "bad simulator or branch";
+        return -1;
+    }
+    std::vector<uint64_t> v = engine_dump(*s->main.rs.branches[branch]);
+    if (out) std::memcpy(out, v.data(), sizeof(uint64_t) * (size_t)std::min<int64_t>(cap, (int64_t)v.size()));
+    return (int64_t)v.size();
+}
+
+PQ_API int32_t pq_debug_branch_phases(pq_sim *s, int32_t branch, const uint64_t *x, const uint64_t *y, uint8_t *out) {
+    if (!s || !x || !y || !out || branch < 0 || branch >= (int)s->main.rs.branches.size()) {
+        g_err = "bad argument";
+        return -2;
+    }
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->host_only) {
+        g_err = "simulator was created by pq_analyze (host structures only)";
+        return -2;
+    }
+    if (cudaSetDevice(s->device) != cudaSuccess) return -2;
+    const int d = s->main.rs.branches[branch]->d;
+    if (d > 24) {
+        g_err = "branch dimension above 24";
+        return -2;
+    }
+    // a single-engine target view of branch `branch`
+    Target view;
+    view.dev.push_back(s->main.dev[branch]);
+    view.iom_dev = s->main.iom_dev;
+    view.max_words = s->main.max_words;
+    pq_tuning tu;
+    {
+        std::lock_guard<std::mutex> lk2(g_mu);
+        tu = g_tuning;
+    }
+    tu.max_branch_dim = kMaxD;
+    Plan P;
+    std::vector<Segment> segs{{&view, 1}};
+    if (build_plan(segs, s->nw, s->stream, tu, P) != PQ_OK) return -2;
+    DevMem dbg;
+    if (dbg.alloc((size_t)1 << d) != cudaSuccess) return -2;
+    P.args.dbg = dbg.as<uint8_t>();
+    const size_t bw = (size_t)s->nw * 8;
+    if (cudaMemcpyAsync(P.x.p, x, bw, cudaMemcpyHostToDevice, P.stream) != cudaSuccess) return -2;
+    if (cudaMemcpyAsync(P.y.p, y, bw, cudaMemcpyHostToDevice, P.stream) != cudaSuccess) return -2;
+    prepare_kernel<<<P.grid_prep, 128, (size_t)4 * P.smem_words * 8, P.stream>>>(P.args);
+    cudaMemsetAsync(P.counter.p, 0, sizeof(unsigned long long), P.stream);
+    enum_kernel<2><<<P.grid_enum, P.block_enum, 0, P.stream>>>(P.args);
+    JobDev J;
+    if (cudaMemcpyAsync(&J, P.jobs.p, sizeof(JobDev), cudaMemcpyDeviceToHost, P.stream) != cudaSuccess) return -2;
+    if (cudaMemcpyAsync(out, dbg.p, (size_t)1 << d, cudaMemcpyDeviceToHost, P.stream) != cudaSuccess) return -2;
+    cudaError_t e = cudaStreamSynchronize(P.stream);
+    if (e != cudaSuccess) {
+        g_err = cudaGetErrorString(e);
+        return -2;
+    }
+    return J.vanish ? -1 : d;
+}
+
+}  // extern "C"

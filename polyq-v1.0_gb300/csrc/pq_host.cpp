@@ -1,0 +1,752 @@
+// pq_host.cpp -- circuit compiler, symmetric F2 elimination and branch-engine build.
+// See pq_host.hpp for the role of each structure; every function names the reference
+// function whose semantics it keeps.
+#include "pq_host.hpp"
+
+#include <algorithm>
+#include <atomic>
+#include <cstring>
+#include <cmath>
+#include <map>
+#include <set>
+#include <stdexcept>
+#include <thread>
+
+namespace pq {
+
+static inline int words_of(int n) { return (n + 63) / 64; }
+
+// ---------------------------------------------------------------- phase ring (src/phase.rs)
+static const double kRootHalf = 0.70710678118654752440;
+static Cplx root8(int k) {
+    static const Cplx R[8] = {{1, 0}, {kRootHalf, kRootHalf}, {0, 1}, {-kRootHalf, kRootHalf},
+                              {-1, 0}, {-kRootHalf, -kRootHalf}, {0, -1}, {kRootHalf, -kRootHalf}};
+    return R[k & 7];
+}
+static Cplx phase_complex(uint32_t p) {  // src/phase.rs:60-66
+    if ((p & ((1u << 29) - 1)) == 0) return root8((int)(p >> 29));
+    double th = 2.0 * M_PI * (double)p / 4294967296.0;
+    return {std::cos(th), std::sin(th)};
+}
+static int clifford_level(uint32_t p) { return (p & ((1u << 30) - 1)) == 0 ? (int)(p >> 30) : -1; }
+static inline uint32_t z4_phase(unsigned k) { return (uint32_t)(k & 3u) << 30; }
+
+// ---------------------------------------------------------------- circuits (src/circuit.rs)
+int Circuit::h_count() const {
+    int h = 0;
+    for (const auto& g : gates) h += g.op == H ? 1 : (g.op == CX ? 2 : 0);
+    return h;
+}
+Circuit Circuit::inverse() const {  // src/circuit.rs:46-56, :189-191
+    Circuit r;
+    r.nq = nq;
+    for (auto it = gates.rbegin(); it != gates.rend(); ++it) {
+        Gate g = *it;
+        switch (g.op) {
+            case S: g.op = SDG; break;
+            case SDG: g.op = S; break;
+            case T: g.op = TDG; break;
+            case TDG: g.op = T; break;
+            case P: case GPHASE: g.ph = 0u - g.ph; break;
+            default: break;
+        }
+        r.gates.push_back(g);
+    }
+    return r;
+}
+std::string validate_circuit(int nq, int ng, const uint8_t* op, const int32_t* q0, const int32_t* q1) {
+    if (nq < 0 || ng < 0) return "negative size";
+    if (ng > 0 && (!op || !q0 || !q1)) return "null gate array";
+    for (int i = 0; i < ng; i++) {
+        if (op[i] >= NUM_GATES) return "unknown gate code at index " + std::to_string(i);
+        if (op[i] == GPHASE) continue;
+        if (q0[i] < 0 || q0[i] >= nq) return "qubit out of range at gate " + std::to_string(i);
+        if (op[i] == CZ || op[i] == CX || op[i] == SWAP) {
+            if (q1[i] < 0 || q1[i] >= nq) return "qubit out of range at gate " + std::to_string(i);
+            if (q1[i] == q0[i]) return "two-qubit gate on one wire at gate " + std::to_string(i);
+        }
+    }
+    return "";
+}
+
+// ---------------------------------------------------------------- compiler (src/pathsum.rs:100-324)
+namespace {
+struct Compiler {
+    int n, nvars, num_h = 0, cap;
+    std::vector<int> wire;
+    std::vector<uint8_t> neg;
+    std::vector<Bits> adj;
+    std::vector<uint8_t> v;
+    std::vector<uint32_t> theta;
+    uint32_t global = 0;
+
+    Compiler(int nq, int extra) : n(nq), nvars(nq), cap(std::max(1, nq + extra)), wire(nq), neg(nq, 0) {
+        for (int i = 0; i < nq; i++) wire[i] = i;
+        adj.assign((size_t)cap, Bits(cap));
+        v.assign((size_t)cap, 0);
+        theta.assign((size_t)cap, 0);
+    }
+    int new_var() {
+        if (nvars == cap) {  // capacity is only a hint (pathsum.rs:120-129)
+            int nc = std::max(cap * 2, 8);
+            std::vector<Bits> na((size_t)nc, Bits(nc));
+            for (int i = 0; i < cap; i++) std::copy(adj[i].w.begin(), adj[i].w.end(), na[i].w.begin());
+            adj.swap(na);
+            v.resize((size_t)nc, 0);
+            theta.resize((size_t)nc, 0);
+            cap = nc;
+        }
+        v[nvars] = 0;
+        theta[nvars] = 0;
+        return nvars++;
+    }
+    void flip_sym(int i, int j) { adj[i].flip(j); adj[j].flip(i); }
+    void add_v(int z, unsigned k) { v[z] = (uint8_t)((v[z] + k) & 3u); }
+    void rotate(int q, uint32_t th) {  // pathsum.rs:215-224
+        int z = wire[q];
+        if (neg[q]) { theta[z] -= th; global += th; }
+        else theta[z] += th;
+    }
+    void apply(const Gate& g) {  // pathsum.rs:136-213
+        int q = g.a;
+        switch (g.op) {
+            case H: {
+                int z = wire[q], zp = new_var();
+                flip_sym(z, zp);
+                num_h++;
+                if (neg[q]) { add_v(zp, 2); neg[q] = 0; }
+                wire[q] = zp;
+            } break;
+            case X: neg[q] ^= 1; break;
+            case Z: add_v(wire[q], 2); if (neg[q]) global += 1u << 31; break;
+            case S:
+                if (neg[q]) { add_v(wire[q], 3); global += 1u << 30; } else add_v(wire[q], 1);
+                break;
+            case SDG:
+                if (neg[q]) { add_v(wire[q], 1); global -= 1u << 30; } else add_v(wire[q], 3);
+                break;
+            case T: rotate(q, 1u << 29); break;
+            case TDG: rotate(q, 0u - (1u << 29)); break;
+            case P: rotate(q, g.ph); break;
+            case Y: apply(Gate{Z, q, 0, 0}); apply(Gate{X, q, 0, 0}); global += 1u << 30; break;
+            case CZ: {
+                int a = g.a, b = g.b, za = wire[a], zb = wire[b];
+                flip_sym(za, zb);
+                if (neg[b]) add_v(za, 2);
+                if (neg[a]) add_v(zb, 2);
+                if (neg[a] && neg[b]) global += 1u << 31;
+            } break;
+            case CX:
+                apply(Gate{H, g.b, 0, 0});
+                apply(Gate{CZ, g.a, g.b, 0});
+                apply(Gate{H, g.b, 0, 0});
+                break;
+            case SWAP: std::swap(wire[g.a], wire[g.b]); std::swap(neg[g.a], neg[g.b]); break;
+            case GPHASE: global += g.ph; break;
+        }
+    }
+    PathSum snapshot() const {  // pathsum.rs:236-261
+        PathSum p;
+        int nv = nvars;
+        p.nq = n; p.nv = nv; p.num_h = num_h;
+        p.b.assign((size_t)nv, Bits(nv));
+        for (int i = 0; i < nv; i++) {
+            for (int wi = 0; wi < p.b[i].nw(); wi++) p.b[i].w[wi] = adj[i].w[wi];
+            if (nv & 63) p.b[i].w.back() &= (1ull << (nv & 63)) - 1;  // columns >= nv are never set
+        }
+        p.v.assign(v.begin(), v.begin() + nv);
+        p.theta.assign(theta.begin(), theta.begin() + nv);
+        p.global = global;
+        p.dead.assign((size_t)nv, 0);
+        p.outputs = wire;
+        p.out_neg = neg;
+        for (int k = 0; k < nv; k++) {  // normalize: pathsum.rs:317-324
+            int l = clifford_level(p.theta[k]);
+            if (l >= 0) { p.v[k] = (uint8_t)((p.v[k] + l) & 3); p.theta[k] = 0; }
+        }
+        return p;
+    }
+};
+}  // namespace
+
+PathSum PathSum::compile(const Circuit& c) {
+    Compiler comp(c.nq, c.h_count());
+    for (const auto& g : c.gates) comp.apply(g);
+    return comp.snapshot();
+}
+PathSum PathSum::sandwich(const Circuit& c, std::vector<int>& junction, std::vector<uint8_t>& jneg) {
+    Compiler comp(c.nq, 2 * c.h_count());
+    for (const auto& g : c.gates) comp.apply(g);
+    junction = comp.wire;
+    jneg = comp.neg;
+    Circuit inv = c.inverse();
+    for (const auto& g : inv.gates) comp.apply(g);
+    return comp.snapshot();
+}
+std::vector<int> PathSum::io_vars() const {  // pathsum.rs:328-336
+    std::vector<int> f;
+    for (int q = 0; q < nq; q++) f.push_back(q);
+    for (int q = 0; q < nq; q++)
+        if (std::find(f.begin(), f.end(), outputs[q]) == f.end()) f.push_back(outputs[q]);
+    return f;
+}
+void PathSum::substitute(int a, int bb, bool c) {  // pathsum.rs:360-394
+    bool bab = b[a].get(bb);
+    uint32_t ta = theta[a], tb = theta[bb];
+    uint8_t vb = v[bb];
+    Bits nb = b[bb];
+    nb.set(a, false);
+    if (!c) {
+        v[a] = (uint8_t)((v[a] + vb + 2 * (int)bab) & 3);
+        theta[a] = ta + tb;
+    } else {
+        v[a] = (uint8_t)((v[a] + 4 - vb) & 3);
+        theta[a] = ta - tb;
+        global += z4_phase(vb) + tb;
+        nb.for_each_one([&](int k) { v[k] = (uint8_t)((v[k] + 2) & 3); });
+    }
+    nb.for_each_one([&](int k) { b[a].flip(k); b[k].flip(a); });
+    b[bb].for_each_one([&](int k) { b[k].set(bb, false); });
+    b[bb].clear();
+    v[bb] = 0;
+    theta[bb] = 0;
+    dead[bb] = 1;
+    int l = clifford_level(theta[a]);
+    if (l >= 0) { v[a] = (uint8_t)((v[a] + l) & 3); theta[a] = 0; }
+}
+void PathSum::trace_closure() {  // pathsum.rs:399-425
+    std::vector<int> rep((size_t)nv);
+    std::vector<uint8_t> par((size_t)nv, 0);
+    for (int i = 0; i < nv; i++) rep[i] = i;
+    for (int q = 0; q < nq; q++) {
+        int ra = q, pa = 0, rb = outputs[q], pb = 0;
+        while (rep[ra] != ra) { pa ^= par[ra]; ra = rep[ra]; }
+        while (rep[rb] != rb) { pb ^= par[rb]; rb = rep[rb]; }
+        int c = pa ^ pb ^ out_neg[q];
+        if (ra == rb) { if (c) zero = true; continue; }
+        substitute(ra, rb, c);
+        rep[rb] = ra;
+        par[rb] = (uint8_t)c;
+    }
+}
+
+// ---------------------------------------------------------------- elimination (src/normal_form.rs:58-336)
+// Symmetric LDL^T over F2 with the MinWeight pivot rule: the lightest alive row with a
+// diagonal bit is a 1x1 pivot; otherwise the lightest row with an off-diagonal bit is a
+// 2x2 pivot with its lowest alive neighbour.  Ties break on the row index.
+Structure eliminate(const std::vector<Bits>& bmat, const Bits& parity) {
+    const int m = (int)bmat.size();
+    std::vector<Bits> gram(bmat);
+    std::vector<Bits> basis((size_t)m, Bits(m));
+    for (int i = 0; i < m; i++) { gram[i].set(i, parity.get(i)); basis[i].set(i, true); }
+    Bits alive(m);
+    for (int i = 0; i < m; i++) alive.set(i, true);
+    Structure st;
+    st.m = m;
+    // key[a] = (class, weight): class 1 = diagonal set, 2 = off-diagonal only, 0 = neither
+    std::vector<std::pair<uint8_t, uint32_t>> key((size_t)m, {0, 0});
+    std::set<std::pair<uint32_t, int>> dset, oset;
+    auto reclass = [&](int a) {
+        if (key[a].first == 1) dset.erase({key[a].second, a});
+        else if (key[a].first == 2) oset.erase({key[a].second, a});
+        if (!alive.get(a)) { key[a] = {0, 0}; return; }
+        uint32_t w = gram[a].and_count(alive);
+        if (gram[a].get(a)) { key[a] = {1, w}; dset.insert({w, a}); }
+        else if (w > 0) { key[a] = {2, w}; oset.insert({w, a}); }
+        else key[a] = {0, 0};
+    };
+    for (int a = 0; a < m; a++) reclass(a);
+    while (true) {
+        if (!dset.empty()) {  // single_step (normal_form.rs:61-82)
+            int a = dset.begin()->second;
+            Bits s = gram[a];
+            s.and_with(alive);
+            s.set(a, false);
+            const Bits pa = basis[a];
+            s.for_each_one([&](int bi) { gram[bi].xor_with(s); basis[bi].xor_with(pa); });
+            alive.set(a, false);
+            st.odd.push_back(pa);
+            reclass(a);
+            s.for_each_one([&](int bi) { reclass(bi); });
+            continue;
+        }
+        if (!oset.empty()) {  // hyper_step (normal_form.rs:87-129)
+            int a = oset.begin()->second;
+            Bits sa = gram[a];
+            sa.and_with(alive);
+            int b = sa.first_one();
+            sa.set(b, false);
+            Bits sb = gram[b];
+            sb.and_with(alive);
+            sb.set(a, false);
+            const Bits pa = basis[a], pb = basis[b];
+            Bits touched = sa;
+            for (int i = 0; i < touched.nw(); i++) touched.w[i] |= sb.w[i];
+            touched.for_each_one([&](int k) {
+                if (sa.get(k)) { gram[k].xor_with(sb); basis[k].xor_with(pb); }
+                if (sb.get(k)) { gram[k].xor_with(sa); basis[k].xor_with(pa); }
+            });
+            alive.set(a, false);
+            alive.set(b, false);
+            st.pa.push_back(pa);
+            st.pb.push_back(pb);
+            reclass(a);
+            reclass(b);
+            touched.for_each_one([&](int k) { reclass(k); });
+            continue;
+        }
+        break;
+    }
+    alive.for_each_one([&](int r) { st.even.push_back(basis[r]); });
+    return st;
+}
+
+// z4 value of a basis vector (normal_form.rs:339-348)
+static unsigned z4_value(const std::vector<Bits>& b, const Bits& v0, const Bits& v1, const Bits& p) {
+    unsigned lin = p.and_count(v0) + 2 * p.and_count(v1);
+    unsigned t = 0;
+    p.for_each_one([&](int j) { t += b[j].and_count(p); });
+    return (lin + 2 * ((t / 2) & 1)) & 3u;
+}
+
+int HostEngine::phase8(const uint64_t* u) const {  // normal_form.rs:479-493
+    int pc1 = 0, pc3 = 0;
+    const uint64_t* uo = u + L.off_o();
+    for (int i = 0; i < L.wo; i++) {
+        pc1 += __builtin_popcountll(uo[i] & dg.o1.w[i]);
+        pc3 += __builtin_popcountll(uo[i] & dg.o3.w[i]);
+    }
+    int n = sigma - 2 * (pc1 - pc3);
+    unsigned cnt = 0;
+    for (int i = 0; i < L.wg; i++)
+        cnt += (unsigned)__builtin_popcountll((dg.wa.w[i] ^ u[L.off_a() + i]) & (dg.wb.w[i] ^ u[L.off_b() + i]));
+    if (cnt & 1) n += 4;
+    return ((n % 8) + 8) % 8;
+}
+
+// ---------------------------------------------------------------- engine build (src/engine.rs:289-390)
+std::unique_ptr<HostEngine> build_engine(const PathSum& ps, const std::vector<int>& fixed) {
+    auto E = std::make_unique<HostEngine>();
+    const int nv = ps.nv, nf = (int)fixed.size();
+    E->nv = nv;
+    E->nf = nf;
+    E->fixed = fixed;
+    std::vector<int> fixed_pos((size_t)nv, -1);
+    for (int i = 0; i < nf; i++) {
+        int f = fixed[i];
+        if (f < 0 || f >= nv || ps.dead[f]) throw std::invalid_argument("fixed variable is not live");
+        if (fixed_pos[f] != -1) throw std::invalid_argument("duplicate fixed variable");
+        fixed_pos[f] = i;
+    }
+    std::vector<int> fidx((size_t)nv, -1);
+    for (int i = 0; i < nv; i++)
+        if (!ps.dead[i] && fixed_pos[i] < 0) { fidx[i] = (int)E->freev.size(); E->freev.push_back(i); }
+    const int m = (int)E->freev.size();
+    E->m = m;
+    std::vector<Bits> bff((size_t)m, Bits(m));
+    Bits parity(m);
+    for (int i = 0; i < m; i++) {
+        ps.b[E->freev[i]].for_each_one([&](int j) { if (fidx[j] >= 0) bff[i].set(fidx[j], true); });
+        parity.set(i, ps.v[E->freev[i]] & 1);
+    }
+    E->wf = words_of(nf);
+    E->bfixed.assign((size_t)nf * std::max(1, E->wf), 0ull);
+    for (int i = 0; i < nf; i++)
+        ps.b[fixed[i]].for_each_one([&](int j) {
+            int p = fixed_pos[j];
+            if (p >= 0) E->bfixed[(size_t)i * E->wf + (p >> 6)] |= 1ull << (p & 63);
+        });
+    E->st = eliminate(bff, parity);
+    const Structure& st = E->st;
+    Layout& Lo = E->L;
+    Lo.g = st.g(); Lo.nodd = (int)st.odd.size(); Lo.neven = (int)st.even.size();
+    Lo.wg = words_of(Lo.g); Lo.wo = words_of(Lo.nodd); Lo.we = words_of(Lo.neven);
+    const int W = Lo.full();
+
+    // basis columns for the variables that need them (normal_form.rs:413-433)
+    std::vector<uint8_t> needed((size_t)m, 0);
+    for (int f : fixed) ps.b[f].for_each_one([&](int j) { if (fidx[j] >= 0) needed[fidx[j]] = 1; });
+    for (int i = 0; i < m; i++) if (ps.theta[E->freev[i]] != 0) needed[i] = 1;
+    std::vector<int> colpos((size_t)m, -1);
+    int ncol = 0;
+    for (int i = 0; i < m; i++) if (needed[i]) colpos[i] = ncol++;
+    std::vector<uint64_t> cols((size_t)ncol * std::max(1, W), 0ull);
+    auto scan = [&](const std::vector<Bits>& vecs, int off) {
+        for (size_t l = 0; l < vecs.size(); l++)
+            vecs[l].for_each_one([&](int j) {
+                if (colpos[j] >= 0) cols[(size_t)colpos[j] * W + off + (l >> 6)] |= 1ull << (l & 63);
+            });
+    };
+    scan(st.pa, Lo.off_a());
+    scan(st.pb, Lo.off_b());
+    scan(st.odd, Lo.off_o());
+    scan(st.even, Lo.off_e());
+    E->ucols.assign((size_t)nf * std::max(1, W), 0ull);
+    for (int i = 0; i < nf; i++)
+        ps.b[fixed[i]].for_each_one([&](int j) {
+            int fj = fidx[j];
+            if (fj < 0) return;
+            const uint64_t* c = &cols[(size_t)colpos[fj] * W];
+            for (int w = 0; w < W; w++) E->ucols[(size_t)i * W + w] ^= c[w];
+        });
+    // branching (engine.rs:372-378)
+    for (int i = 0; i < m; i++) if (ps.theta[E->freev[i]] != 0) E->term_vars.push_back(i);
+    const int t = (int)E->term_vars.size();
+    E->t = t;
+    E->mcols.assign((size_t)t * std::max(1, W), 0ull);
+    for (int k = 0; k < t; k++) {
+        const uint64_t* c = &cols[(size_t)colpos[E->term_vars[k]] * W];
+        std::copy(c, c + W, E->mcols.begin() + (size_t)k * W);
+    }
+    // Elim::new (engine.rs:119-184): RREF of K = M|_even, tracking the row operations R
+    const int ne = Lo.neven;
+    std::vector<Bits> rk((size_t)ne, Bits(t)), rr((size_t)ne, Bits(ne));
+    for (int r = 0; r < ne; r++) {
+        rr[r].set(r, true);
+        for (int c = 0; c < t; c++)
+            if ((E->mcols[(size_t)c * W + Lo.off_e() + (r >> 6)] >> (r & 63)) & 1ull) rk[r].set(c, true);
+    }
+    int rank = 0;
+    for (int col = 0; col < t; col++) {
+        int r = -1;
+        for (int i = rank; i < ne; i++) if (rk[i].get(col)) { r = i; break; }
+        if (r < 0) continue;
+        std::swap(rk[rank], rk[r]);
+        std::swap(rr[rank], rr[r]);
+        for (int r2 = 0; r2 < ne; r2++)
+            if (r2 != rank && rk[r2].get(col)) { rk[r2].xor_with(rk[rank]); rr[r2].xor_with(rr[rank]); }
+        E->piv_col.push_back(col);
+        rank++;
+    }
+    E->rank = rank;
+    for (int i = 0; i < rank; i++) E->piv_row.push_back(rr[i]);
+    for (int i = rank; i < ne; i++) E->cons.push_back(rr[i]);
+    E->ncons = ne - rank;
+    std::vector<uint8_t> is_piv((size_t)t, 0);
+    for (int c : E->piv_col) is_piv[c] = 1;
+    const int abo = Lo.abo();
+    for (int j = 0; j < t; j++) {
+        if (is_piv[j]) continue;
+        Bits kv(t);
+        kv.set(j, true);
+        uint64_t rmask = 0;
+        for (int i = 0; i < rank; i++)
+            if (rk[i].get(j)) { kv.set(E->piv_col[i], true); if (i < 64) rmask |= 1ull << i; }
+        std::vector<uint64_t> u((size_t)W, 0ull);
+        kv.for_each_one([&](int k) { for (int w = 0; w < W; w++) u[w] ^= E->mcols[(size_t)k * W + w]; });
+        for (int w = Lo.off_e(); w < W; w++)
+            if (u[w]) throw std::logic_error("kernel column with a radical component");
+        E->ku.insert(E->ku.end(), u.begin(), u.begin() + abo);
+        E->kernel.push_back(kv);
+        E->R.push_back(rmask);
+        E->free_col.push_back(j);
+    }
+    E->d = (int)E->kernel.size();
+    // Z4 diagonal (normal_form.rs:354-391)
+    Bits v0(m), v1(m);
+    for (int i = 0; i < m; i++) { uint8_t x = ps.v[E->freev[i]]; v0.set(i, x & 1); v1.set(i, (x & 2) != 0); }
+    Diag& dg = E->dg;
+    dg.wa = Bits(Lo.g); dg.wb = Bits(Lo.g); dg.o1 = Bits(Lo.nodd); dg.o3 = Bits(Lo.nodd); dg.we = Bits(Lo.neven);
+    for (int j = 0; j < Lo.g; j++) {
+        dg.wa.set(j, z4_value(bff, v0, v1, st.pa[j]) == 2);
+        dg.wb.set(j, z4_value(bff, v0, v1, st.pb[j]) == 2);
+    }
+    dg.sigma = 0;
+    for (int l = 0; l < Lo.nodd; l++) {
+        if (z4_value(bff, v0, v1, st.odd[l]) == 1) { dg.o1.set(l, true); dg.sigma++; }
+        else { dg.o3.set(l, true); dg.sigma--; }
+    }
+    for (int l = 0; l < Lo.neven; l++) dg.we.set(l, z4_value(bff, v0, v1, st.even[l]) == 2);
+    E->sigma = dg.sigma;
+    E->mag2 = 2 * Lo.g + 2 * Lo.neven + Lo.nodd;
+    // terms (engine.rs:232-238), FP64
+    for (int k = 0; k < t; k++) {
+        Cplx e = phase_complex(ps.theta[E->freev[E->term_vars[k]]]);
+        E->alpha.push_back({(1.0 + e.re) * 0.5, (0.0 + e.im) * 0.5});
+        E->beta.push_back({(1.0 - e.re) * 0.5, (0.0 - e.im) * 0.5});
+    }
+    for (int i = 0; i < nf; i++) { E->fixed_v.push_back(ps.v[fixed[i]]); E->fixed_th.push_back(ps.theta[fixed[i]]); }
+    E->num_h = ps.num_h;
+    E->global = ps.global;
+    E->zero = ps.zero;
+    // quadratic part of the Z8 phase over kernel coordinates: 4*G_ij is the second finite
+    // difference of phase8 along kernel columns i and j, which does not depend on the base point
+    const int d = E->d;
+    E->G.assign((size_t)d, 0ull);
+    if (d <= 64) {
+        std::vector<uint64_t> z((size_t)abo, 0ull), uij((size_t)abo);
+        const int p0 = E->phase8(z.data());
+        std::vector<int> p1((size_t)d);
+        for (int j = 0; j < d; j++) p1[j] = E->phase8(&E->ku[(size_t)j * abo]);
+        for (int i = 0; i < d; i++)
+            for (int j = i + 1; j < d; j++) {
+                for (int w = 0; w < abo; w++) uij[w] = E->ku[(size_t)i * abo + w] ^ E->ku[(size_t)j * abo + w];
+                int dd = ((E->phase8(uij.data()) - p1[i] - p1[j] + p0) % 8 + 16) % 8;
+                if (dd != 0 && dd != 4) throw std::logic_error("phase is not quadratic over the kernel");
+                if (dd == 4) { E->G[i] |= 1ull << j; E->G[j] |= 1ull << i; }
+            }
+    }
+    // error-bound factor: sum_s |c(s)| <= prod_j (|a0|+|a1|)(free cols) * prod_i max(|a0|,|a1|)(pivots)
+    double bound = 1.0;
+    for (int j = 0; j < d; j++) {
+        int k = E->free_col[j];
+        bound *= std::hypot(E->alpha[k].re, E->alpha[k].im) + std::hypot(E->beta[k].re, E->beta[k].im);
+    }
+    for (int i = 0; i < rank; i++) {
+        int k = E->piv_col[i];
+        bound *= std::max(std::hypot(E->alpha[k].re, E->alpha[k].im), std::hypot(E->beta[k].re, E->beta[k].im));
+    }
+    E->sum_abs_bound = bound;
+    return E;
+}
+
+// ---------------------------------------------------------------- strategy layer (src/rank.rs)
+static const int kMaxPairs = 14;
+static const uint32_t kMask30 = (1u << 30) - 1;
+
+static std::vector<std::pair<int, int>> pair_candidates(const PathSum& ps, const std::vector<int>& fixed, int& ntclass) {
+    std::map<uint32_t, std::vector<int>> groups;  // rank.rs:62-84
+    for (int k = 0; k < ps.nv; k++) {
+        if (ps.dead[k] || ps.theta[k] == 0) continue;
+        if (std::find(fixed.begin(), fixed.end(), k) != fixed.end()) continue;
+        uint32_t r = ps.theta[k] & kMask30;
+        uint32_t o = (uint32_t)(((uint64_t)kMask30 + 1 - r) & kMask30);
+        groups[std::min(r, o)].push_back(k);
+    }
+    std::vector<std::pair<int, int>> tp, gp;
+    for (auto& kv : groups) {
+        auto& target = kv.first == (1u << 29) ? tp : gp;
+        for (size_t i = 0; i + 1 < kv.second.size(); i += 2) target.push_back({kv.second[i], kv.second[i + 1]});
+    }
+    ntclass = (int)tp.size();
+    tp.insert(tp.end(), gp.begin(), gp.end());
+    return tp;
+}
+
+int best_pairs(const HostEngine& base, int available, int tclass) {  // rank.rs:205-222
+    double m = (double)base.m;
+    double words = (double)(base.m / 64 + 1);
+    double ldl = 2.0 * m * m * m / 64.0 + 50.0 * m + 2000.0;
+    double step = 20.0 + 4.0 * words + (double)base.t / 2.0;
+    int best = 0;
+    double bestc = INFINITY;
+    for (int p = 0; p <= std::min(available, kMaxPairs); p++) {
+        int removed = 2 * std::min(p, tclass) + std::max(0, p - tclass);
+        int d = std::max(0, base.d - removed);
+        double cost = std::pow(2.0, (double)p) * ((p == 0 ? 0.0 : ldl) + std::pow(2.0, (double)d) * step);
+        if (cost < bestc) { best = p; bestc = cost; }
+    }
+    return best;
+}
+
+// 2^p branch engines built on host threads (rank.rs:88-103 builds them with rayon)
+static RankSet rank_new(const PathSum& ps, const std::vector<int>& fixed, int pairs) {
+    int nt = 0;
+    auto cands = pair_candidates(ps, fixed, nt);
+    int p = std::min(std::min(pairs, (int)cands.size()), kMaxPairs);
+    RankSet rs;
+    rs.pairs = p;
+    const int nb = 1 << p;
+    rs.branches.resize((size_t)nb);
+    std::atomic<int> next{0};
+    std::vector<std::string> errs((size_t)nb);
+    auto work = [&]() {
+        for (int pat = next++; pat < nb; pat = next++) {
+            try {
+                PathSum b = ps;
+                for (int i = 0; i < p; i++) b.substitute(cands[i].first, cands[i].second, (pat >> i) & 1);
+                rs.branches[pat] = build_engine(b, fixed);
+            } catch (const std::exception& e) {
+                errs[pat] = e.what();
+            }
+        }
+    };
+    int nth = (int)std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()), (unsigned)nb);
+    if (nth <= 1) work();
+    else {
+        std::vector<std::thread> th;
+        for (int i = 0; i < nth; i++) th.emplace_back(work);
+        for (auto& x : th) x.join();
+    }
+    for (auto& e : errs) if (!e.empty()) throw std::runtime_error(e);
+    return rs;
+}
+
+RankSet build_rank(const PathSum& ps, const std::vector<int>& fixed, int strategy, int pairs) {
+    if (strategy == STRAT_CACHED) return rank_new(ps, fixed, 0);
+    if (strategy == STRAT_PAIRS) return rank_new(ps, fixed, pairs);
+    // Auto (rank.rs:115-123)
+    auto base = build_engine(ps, fixed);
+    int nt = 0;
+    auto cands = pair_candidates(ps, fixed, nt);
+    int p = best_pairs(*base, (int)cands.size(), nt);
+    if (p == 0) {
+        RankSet rs;
+        rs.pairs = 0;
+        rs.branches.push_back(std::move(base));
+        return rs;
+    }
+    return rank_new(ps, fixed, p);
+}
+
+// ---------------------------------------------------------------- weight tables
+static inline Cplx cmul(Cplx a, Cplx b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
+
+EngineTables build_tables(const HostEngine& e, int di_max) {
+    EngineTables T;
+    const int d = e.d;
+    T.DI = std::min(d, di_max);
+    T.joint = e.rank <= kJointMaxPivots;
+    if (T.joint && T.DI + e.rank > kJointMaxBits) T.DI = std::max(0, kJointMaxBits - e.rank);
+    auto xw = [&](int j, int bit) { int k = e.free_col[j]; return bit ? e.beta[k] : e.alpha[k]; };
+    auto pw = [&](int i, int bit) { int k = e.piv_col[i]; return bit ? e.beta[k] : e.alpha[k]; };
+    const size_t nlo = (size_t)1 << T.DI;
+    T.tlo.resize(nlo);
+    for (size_t s = 0; s < nlo; s++) {
+        Cplx c{1.0, 0.0};
+        for (int j = 0; j < T.DI; j++) c = cmul(c, xw(j, (int)((s >> j) & 1)));
+        T.tlo[s] = c;
+    }
+    T.nsl_tp = (e.rank + 7) / 8;
+    T.tp.resize((size_t)T.nsl_tp * 256);
+    for (int sl = 0; sl < T.nsl_tp; sl++)
+        for (int b = 0; b < 256; b++) {
+            Cplx c{1.0, 0.0};
+            for (int k = 0; k < 8 && 8 * sl + k < e.rank; k++) c = cmul(c, pw(8 * sl + k, (b >> k) & 1));
+            T.tp[(size_t)sl * 256 + b] = c;
+        }
+    T.nsl_th = (d - T.DI + 7) / 8;
+    T.th.resize((size_t)T.nsl_th * 256);
+    for (int sl = 0; sl < T.nsl_th; sl++)
+        for (int b = 0; b < 256; b++) {
+            Cplx c{1.0, 0.0};
+            for (int k = 0; k < 8 && T.DI + 8 * sl + k < d; k++) c = cmul(c, xw(T.DI + 8 * sl + k, (b >> k) & 1));
+            T.th[(size_t)sl * 256 + b] = c;
+        }
+    if (T.joint) {
+        T.w.resize((size_t)1 << (T.DI + e.rank));
+        for (size_t y = 0; y < ((size_t)1 << e.rank); y++) {
+            Cplx tpv{1.0, 0.0};
+            for (int i = 0; i < e.rank; i++) tpv = cmul(tpv, pw(i, (int)((y >> i) & 1)));
+            for (size_t s = 0; s < nlo; s++) T.w[(y << T.DI) | s] = cmul(T.tlo[s], tpv);
+        }
+    }
+    return T;
+}
+
+// ---------------------------------------------------------------- packing for upload
+namespace {
+struct Packer {
+    std::vector<uint8_t> blob;
+    size_t put(const void* p, size_t bytes) {
+        size_t off = (blob.size() + 15) & ~(size_t)15;
+        blob.resize(off + std::max<size_t>(bytes, 16), 0);
+        if (bytes) std::memcpy(blob.data() + off, p, bytes);
+        return off;
+    }
+    template <class T> size_t vec(const std::vector<T>& v) { return put(v.data(), v.size() * sizeof(T)); }
+};
+template <class T> const T* as_off(size_t o) { return reinterpret_cast<const T*>(o); }
+template <class T> const T* shift(const T* p, const uint8_t* base) {
+    return reinterpret_cast<const T*>(base + reinterpret_cast<size_t>(p));
+}
+}  // namespace
+
+PackedEngine pack_engine(const HostEngine& e, const EngineTables& T) {
+    PackedEngine P;
+    Packer k;
+    EngineDev& d = P.off;
+    std::memset(&d, 0, sizeof(d));
+    const Layout& L = e.L;
+    d.nf = e.nf; d.t = e.t; d.d = e.d; d.rank = e.rank; d.ncons = e.ncons;
+    d.wg = L.wg; d.wo = L.wo; d.we = L.we; d.wf = e.wf; d.W = L.full(); d.abo = L.abo();
+    d.sigma = e.sigma; d.mag2 = e.mag2; d.num_h = e.num_h; d.global = e.global; d.zero = e.zero ? 1 : 0;
+    d.DI = T.DI; d.nsl_tp = T.nsl_tp; d.nsl_th = T.nsl_th;
+    d.sum_abs_bound = e.sum_abs_bound;
+    d.o1 = as_off<uint64_t>(k.vec(e.dg.o1.w));
+    d.o3 = as_off<uint64_t>(k.vec(e.dg.o3.w));
+    d.wa = as_off<uint64_t>(k.vec(e.dg.wa.w));
+    d.wb = as_off<uint64_t>(k.vec(e.dg.wb.w));
+    d.wem = as_off<uint64_t>(k.vec(e.dg.we.w));
+    d.ucols = as_off<uint64_t>(k.vec(e.ucols));
+    d.mcols = as_off<uint64_t>(k.vec(e.mcols));
+    d.ku = as_off<uint64_t>(k.vec(e.ku));
+    d.bfixed = as_off<uint64_t>(k.vec(e.bfixed));
+    d.fixed_v = as_off<uint8_t>(k.vec(e.fixed_v));
+    d.fixed_th = as_off<uint32_t>(k.vec(e.fixed_th));
+    std::vector<uint64_t> pr, cs;
+    for (const auto& r : e.piv_row) pr.insert(pr.end(), r.w.begin(), r.w.end());
+    for (const auto& r : e.cons) cs.insert(cs.end(), r.w.begin(), r.w.end());
+    d.pivrow = as_off<uint64_t>(k.vec(pr));
+    d.cons = as_off<uint64_t>(k.vec(cs));
+    std::vector<int32_t> pc(e.piv_col.begin(), e.piv_col.end());
+    d.pivcol = as_off<int32_t>(k.vec(pc));
+    d.G = as_off<uint64_t>(k.vec(e.G));
+    d.R = as_off<uint64_t>(k.vec(e.R));
+    std::vector<float> tlo32, tp32;
+    for (const auto& c : T.tlo) { tlo32.push_back((float)c.re); tlo32.push_back((float)c.im); }
+    for (const auto& c : T.tp) { tp32.push_back((float)c.re); tp32.push_back((float)c.im); }
+    d.tlo = as_off<float2>(k.vec(tlo32));
+    d.tp = as_off<float2>(k.vec(tp32));
+    d.th = as_off<double2>(k.vec(T.th));
+    d.tlo64 = as_off<double2>(k.vec(T.tlo));
+    d.tp64 = as_off<double2>(k.vec(T.tp));
+    d.joint = T.joint ? 1 : 0;
+    std::vector<float> w32;  // hi.re, hi.im, lo.re, lo.im with hi + lo = the FP64 weight
+    for (const auto& c : T.w) {
+        float hr = (float)c.re, hi = (float)c.im;
+        w32.push_back(hr);
+        w32.push_back(hi);
+        w32.push_back((float)(c.re - (double)hr));
+        w32.push_back((float)(c.im - (double)hi));
+    }
+    d.wtab = as_off<float4>(k.vec(w32));
+    P.blob.swap(k.blob);
+    return P;
+}
+
+EngineDev rebase_engine(const EngineDev& o, const uint8_t* base) {
+    EngineDev d = o;
+    d.o1 = shift(o.o1, base); d.o3 = shift(o.o3, base); d.wa = shift(o.wa, base); d.wb = shift(o.wb, base);
+    d.wem = shift(o.wem, base); d.ucols = shift(o.ucols, base); d.mcols = shift(o.mcols, base);
+    d.ku = shift(o.ku, base); d.bfixed = shift(o.bfixed, base); d.fixed_v = shift(o.fixed_v, base);
+    d.fixed_th = shift(o.fixed_th, base); d.pivrow = shift(o.pivrow, base); d.cons = shift(o.cons, base);
+    d.pivcol = shift(o.pivcol, base); d.G = shift(o.G, base); d.R = shift(o.R, base);
+    d.tlo = shift(o.tlo, base); d.tp = shift(o.tp, base); d.th = shift(o.th, base);
+    d.tlo64 = shift(o.tlo64, base); d.tp64 = shift(o.tp64, base); d.wtab = shift(o.wtab, base);
+    return d;
+}
+
+IoMapHost build_iomap(const std::vector<std::pair<int, int32_t>>& puts) {
+    IoMapHost m;
+    for (const auto& p : puts) {
+        auto it = std::find(m.fixed.begin(), m.fixed.end(), p.first);
+        if (it == m.fixed.end()) { m.fixed.push_back(p.first); m.src.push_back(p.second); }
+        else { m.cf_pos.push_back((int32_t)(it - m.fixed.begin())); m.cf_src.push_back(p.second); }
+    }
+    return m;
+}
+
+// ---------------------------------------------------------------- canonical dump
+std::vector<uint64_t> engine_dump(const HostEngine& e) {
+    std::vector<uint64_t> o;
+    const Layout& L = e.L;
+    o.push_back((uint64_t)e.m); o.push_back((uint64_t)L.g); o.push_back((uint64_t)L.nodd); o.push_back((uint64_t)L.neven);
+    o.push_back((uint64_t)e.t); o.push_back((uint64_t)e.d); o.push_back((uint64_t)(int64_t)e.sigma); o.push_back((uint64_t)e.nf);
+    auto put = [&](const Bits& b) { o.insert(o.end(), b.w.begin(), b.w.end()); };
+    for (auto& b : e.st.pa) put(b);
+    for (auto& b : e.st.pb) put(b);
+    for (auto& b : e.st.odd) put(b);
+    for (auto& b : e.st.even) put(b);
+    put(e.dg.wa); put(e.dg.wb); put(e.dg.o1); put(e.dg.o3); put(e.dg.we);
+    const int abo = L.abo(), W = L.full();
+    o.insert(o.end(), e.ku.begin(), e.ku.begin() + (size_t)e.d * abo);
+    for (auto& k : e.kernel) put(k);
+    o.insert(o.end(), e.mcols.begin(), e.mcols.begin() + (size_t)e.t * W);
+    o.insert(o.end(), e.ucols.begin(), e.ucols.begin() + (size_t)e.nf * W);
+    for (int i = 0; i < e.rank; i++) { o.push_back((uint64_t)e.piv_col[i]); put(e.piv_row[i]); }
+    for (auto& c : e.cons) put(c);
+    return o;
+}
+
+}  // namespace pq

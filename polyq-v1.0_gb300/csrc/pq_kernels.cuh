@@ -1,0 +1,324 @@
+// pq_kernels.cuh -- sm_103a kernels of the amplitude path.
+//
+//   prepare_kernel   one warp per (branch engine, boundary) job: boundary values, fixed
+//                    constants, boundary shift u0 = xor of resident boundary columns, radical
+//                    consistency + particular solution (pivot bits y0), start shift, Z8 index
+//                    k0 and the Z4 linear coefficients Lp_j        (src/engine.rs:569-610)
+//   enum_kernel      persistent: each warp pulls work items (a job's contiguous chunk range)
+//                    from an atomic counter; lane l walks chunks l, l+32, ... of the item in
+//                    Gray order: one AND+POPC Z8 update, one table weight, compensated FP32
+//                    accumulation; FP64 scaling of each chunk and an FP64 warp-shuffle reduce
+//                    (src/engine.rs:669-722, normal_form.rs:479-493)
+//   job_reduce       FP64 sum of a job's item partials in item order, times the Z8 root of k0,
+//                    e^{i phase} and 2^{(mag2 - h)/2}                  (src/engine.rs:557-565)
+//   out_reduce       FP64 sum over the 2^p branch engines of each boundary (src/rank.rs:184-190)
+#pragma once
+#include <cuda_runtime.h>
+
+#include "pq_core.cuh"
+
+namespace pq {
+
+#define PQ_FULL 0xffffffffu
+
+__constant__ double c_root8[16] = {1.0, 0.0, 0.70710678118654752440, 0.70710678118654752440, 0.0, 1.0,
+                                   -0.70710678118654752440, 0.70710678118654752440, -1.0, 0.0,
+                                   -0.70710678118654752440, -0.70710678118654752440, 0.0, -1.0,
+                                   0.70710678118654752440, -0.70710678118654752440};
+
+struct KArgs {
+    const EngineDev *engines;
+    const IoMapDev *maps;
+    JobDev *jobs;
+    int njobs;
+    const int *perm;            // job id of the k-th job in item order
+    const int *kinv;            // position of job j in item order
+    const long long *istart;    // njobs + 1 prefix sums of item counts (item order)
+    const int *jdl;             // per job: Gray steps per chunk (log2)
+    const unsigned *jcpi;       // per job: chunks per item
+    const unsigned long long *jnch;  // per job: chunks
+    long long nitems;
+    double2 *partials;
+    unsigned long long *counter;
+    double2 *job_vals;
+    double *job_err;
+    const int *out_jobs;        // nout + 1: jobs of output o are [out_jobs[o], out_jobs[o+1])
+    int nout;
+    double *out;                // 2 * nout
+    double *err;                // nout or null
+    int out_prob;               // write |amp|^2 instead of amp
+    const uint64_t *xs;
+    const uint64_t *ys;
+    int nw;
+    int smem_words;             // per-warp words of the prepare kernel
+    uint8_t *dbg;               // per-branch Z8 indices (debug mode)
+    int *errflag;
+};
+
+__device__ __forceinline__ int warp_sum_i(int v) {
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(PQ_FULL, v, o);
+    return v;
+}
+__device__ __forceinline__ unsigned warp_sum_u(unsigned v) {
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(PQ_FULL, v, o);
+    return v;
+}
+
+// ------------------------------------------------------------------------------ prepare
+__global__ void __launch_bounds__(128) prepare_kernel(KArgs a) {
+    extern __shared__ uint64_t psm[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    uint64_t *u = psm + (size_t)wib * a.smem_words;
+    for (int jid = blockIdx.x * wpb + wib; jid < a.njobs; jid += gridDim.x * wpb) {
+        JobDev *J = &a.jobs[jid];
+        const EngineDev &E = a.engines[J->engine];
+        const IoMapDev &M = a.maps[J->iomap];
+        const uint64_t *x = a.xs + (size_t)J->req * a.nw;
+        const uint64_t *y = a.ys + (size_t)J->req * a.nw;
+        uint64_t *vals = u + E.W;
+        // fixed-variable values from the boundary bits
+        for (int base = 0; base < E.nf; base += 64) {
+            int i0 = base + lane, i1 = base + 32 + lane;
+            int b0 = i0 < E.nf ? src_bit(M.src[i0], x, y) : 0;
+            int b1 = i1 < E.nf ? src_bit(M.src[i1], x, y) : 0;
+            unsigned lo = __ballot_sync(PQ_FULL, b0), hi = __ballot_sync(PQ_FULL, b1);
+            if (lane == 0) vals[base >> 6] = (uint64_t)lo | ((uint64_t)hi << 32);
+        }
+        __syncwarp();
+        int bad = 0;
+        for (int c = lane; c < M.ncf; c += 32) bad |= bit_at(vals, M.cf_pos[c]) != src_bit(M.cf_src[c], x, y);
+        bad = __any_sync(PQ_FULL, bad) || E.zero;
+        // constants from fixed-fixed terms (engine.rs:575-588)
+        uint32_t z4 = 0, th = 0;
+        fixed_constants_partial(E, vals, lane, 32, z4, th);
+        z4 = warp_sum_u(z4);
+        th = warp_sum_u(th);
+        // u0 = xor of boundary columns (engine.rs:589-592)
+        boundary_shift_partial(E, vals, u, lane, 32);
+        __syncwarp();
+        // radical system K s = kappa (engine.rs:593-597, :188-201)
+        int badc = 0;
+        for (int r = lane; r < E.ncons; r += 32) badc |= kappa_dot(E, E.cons + (size_t)r * E.we, u);
+        bad = bad || __any_sync(PQ_FULL, badc);
+        uint64_t y0 = 0;
+        for (int base = 0; base < E.rank; base += 32) {
+            int i = base + lane;
+            int bit = i < E.rank ? kappa_dot(E, E.pivrow + (size_t)i * E.we, u) : 0;
+            y0 |= (uint64_t)__ballot_sync(PQ_FULL, bit) << base;
+        }
+        // start shift u = u0 ^ sum of the pivot columns (engine.rs:598-607)
+        apply_pivots_partial(E, y0, u, lane, 32);
+        __syncwarp();
+        int n1 = 0, cnt = 0;
+        phase8_partial(E, u, nullptr, lane, 32, n1, cnt);
+        n1 = warp_sum_i(n1);
+        cnt = warp_sum_i(cnt);
+        const uint32_t k0 = phase8_finish(E, n1, cnt);
+        int lerr = 0;
+        for (int j = lane; j < E.d; j += 32) {
+            int a1 = 0, c1 = 0;
+            phase8_partial(E, u, E.ku + (size_t)j * E.abo, 0, 1, a1, c1);
+            uint32_t L = (phase8_finish(E, a1, c1) - k0) & 7u;
+            lerr |= (int)(L & 1u);
+            J->Lp[j] = (uint8_t)(L >> 1);
+        }
+        lerr = __any_sync(PQ_FULL, lerr);
+        if (lane == 0) {
+            J->vanish = bad ? 1 : 0;
+            J->phase = E.global + th + ((z4 & 3u) << 30);
+            J->k0 = k0;
+            J->y0 = y0;
+            J->err = (uint32_t)lerr;
+            if (lerr) atomicOr(a.errflag, 1);
+        }
+        __syncwarp();
+    }
+}
+
+// ------------------------------------------------------------------------------ enumerate
+// MODE 0: FP32 weights, compensated accumulation.  MODE 1: FP64 weights and accumulation.
+// MODE 2: record the Z8 index of every branch into dbg (single-job debug launches).
+template <int MODE>
+__global__ void __launch_bounds__(256) enum_kernel(KArgs a) {
+    __shared__ uint64_t sG[8][64];
+    __shared__ uint64_t sR[8][64];
+    __shared__ uint8_t sLp[8][64];
+    __shared__ uint8_t sLm[8][64];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    uint64_t *G = sG[wib];
+    uint64_t *R = sR[wib];
+    uint8_t *Lp = sLp[wib];
+    uint8_t *Lm = sLm[wib];
+    int cur_k = -1;  // position (item order) of the job whose data is staged
+    long long kbeg = 0, kend = 0;
+    while (true) {
+        unsigned long long it0 = 0;
+        if (lane == 0) it0 = atomicAdd(a.counter, 1ull);
+        const long long it = (long long)__shfl_sync(PQ_FULL, it0, 0);
+        if (it >= a.nitems) break;
+        if (!(it >= kbeg && it < kend)) {
+            int lo = 0, hi = a.njobs - 1;  // last k with istart[k] <= it
+            while (lo < hi) {
+                int mid = (lo + hi + 1) >> 1;
+                if (a.istart[mid] <= it) lo = mid; else hi = mid - 1;
+            }
+            cur_k = lo;
+            kbeg = a.istart[lo];
+            kend = a.istart[lo + 1];
+            const int jb = a.perm[lo];
+            const JobDev &J = a.jobs[jb];
+            const EngineDev &E = a.engines[J.engine];
+            __syncwarp();
+            for (int j = lane; j < E.d; j += 32) {
+                G[j] = E.G[j];
+                R[j] = E.R[j];
+                Lp[j] = J.Lp[j];
+                Lm[j] = (uint8_t)((4u - J.Lp[j]) & 3u);
+            }
+            __syncwarp();
+        }
+        const int job = a.perm[cur_k];
+        const JobDev &J = a.jobs[job];
+        const EngineDev &E = a.engines[J.engine];
+        const long long iin = it - kbeg;
+        double accx = 0.0, accy = 0.0;
+        if (!J.vanish) {
+            const int dl = a.jdl[job];
+            const unsigned cpi = a.jcpi[job];
+            const unsigned long long nch = a.jnch[job];
+            const unsigned long long c0 = (unsigned long long)iin * cpi;
+            unsigned long long cend = c0 + cpi;
+            if (cend > nch) cend = nch;
+            const uint64_t lomask = (E.DI >= 64) ? ~0ull : ((1ull << E.DI) - 1ull);
+            const uint32_t steps = 1u << dl;
+            for (unsigned long long ch = c0 + lane; ch < cend; ch += 32) {
+                const uint64_t s = (uint64_t)ch << dl;
+                uint32_t m;
+                uint64_t yy;
+                chunk_start(Lp, G, R, J.y0, s, m, yy);
+                const double2 chi = chunk_high_weight(E, s);
+                uint64_t ss = s;
+                if (MODE == 1 || !E.joint) {
+                    // FP64 weights and accumulation (verification mode, and engines with more
+                    // pivots than the joint table holds)
+                    double sx = 0.0, sy = 0.0;
+                    for (uint32_t i = 1;; ++i) {
+                        if (MODE == 2) a.dbg[ss] = (uint8_t)((J.k0 + 2u * m) & 7u);
+                        double2 w = E.tlo64[ss & lomask];
+                        for (int sl = 0; sl < E.nsl_tp; sl++) w = cmul_d(w, E.tp64[sl * 256 + (int)((yy >> (8 * sl)) & 255ull)]);
+                        w = rot4d(w, m & 3u);
+                        sx += w.x;
+                        sy += w.y;
+                        if (i == steps) break;
+                        const int j = ctz32(i);
+                        m += (((ss >> j) & 1ull) ? Lm[j] : Lp[j]) + 2u * (uint32_t)(popc64(G[j] & ss) & 1);
+                        ss ^= 1ull << j;
+                        yy ^= R[j];
+                    }
+                    accx += sx * chi.x - sy * chi.y;
+                    accy += sx * chi.y + sy * chi.x;
+                } else {
+                    // FP32: hi parts with TwoSum, lo parts plain (their error is u * u|c|)
+                    float ax = 0.f, ay = 0.f, cx = 0.f, cy = 0.f, lx = 0.f, ly = 0.f;
+                    const float4 *__restrict__ W = E.wtab;
+                    const int DI = E.DI;
+                    for (uint32_t i = 1;; ++i) {
+                        if (MODE == 2) a.dbg[ss] = (uint8_t)((J.k0 + 2u * m) & 7u);
+                        const float4 w = rot4q(__ldg(&W[(yy << DI) | (ss & lomask)]), m & 3u);
+                        two_sum_acc(ax, cx, w.x);
+                        two_sum_acc(ay, cy, w.y);
+                        lx += w.z;
+                        ly += w.w;
+                        if (i == steps) break;
+                        const int j = ctz32(i);
+                        m += (((ss >> j) & 1ull) ? Lm[j] : Lp[j]) + 2u * (uint32_t)(popc64(G[j] & ss) & 1);
+                        ss ^= 1ull << j;
+                        yy ^= R[j];
+                    }
+                    const double vx = (double)ax + (double)cx + (double)lx;
+                    const double vy = (double)ay + (double)cy + (double)ly;
+                    accx += vx * chi.x - vy * chi.y;
+                    accy += vx * chi.y + vy * chi.x;
+                }
+            }
+        }
+        for (int o = 16; o; o >>= 1) {
+            accx += __shfl_xor_sync(PQ_FULL, accx, o);
+            accy += __shfl_xor_sync(PQ_FULL, accy, o);
+        }
+        if (lane == 0) a.partials[it] = make_double2(accx, accy);
+    }
+}
+
+// ------------------------------------------------------------------------------ reductions
+__device__ __forceinline__ double2 phase_to_complex_dev(uint32_t p) {
+    if ((p & ((1u << 29) - 1u)) == 0) {
+        int k = (int)(p >> 29);
+        return make_double2(c_root8[2 * k], c_root8[2 * k + 1]);
+    }
+    double s, c;
+    sincospi((double)p * 4.656612873077392578125e-10, &s, &c);  // angle = pi * p / 2^31
+    return make_double2(c, s);
+}
+
+__global__ void job_reduce_kernel(KArgs a) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= a.njobs) return;
+    const JobDev &J = a.jobs[j];
+    const EngineDev &E = a.engines[J.engine];
+    double2 v = make_double2(0.0, 0.0);
+    double eb = 0.0;
+    if (!J.vanish) {
+        const int k = a.kinv[j];
+        double sx = 0.0, sy = 0.0;
+        for (long long i = a.istart[k]; i < a.istart[k + 1]; i++) {
+            sx += a.partials[i].x;
+            sy += a.partials[i].y;
+        }
+        const double2 r8 = make_double2(c_root8[2 * (J.k0 & 7u)], c_root8[2 * (J.k0 & 7u) + 1]);
+        v = cmul_d(cmul_d(make_double2(sx, sy), r8), phase_to_complex_dev(J.phase));
+        const double mag = pow2_half(E.mag2 - E.num_h);
+        v.x *= mag;
+        v.y *= mag;
+        // Rigorous bound on |computed - exact| relative to sum_s |c(s)| * mag:
+        //  joint table: weights exact to 2^-46 (hi + lo of an FP64 product); TwoSum over a chunk
+        //  of n = 2^dl terms errs by <= gamma_n^2 sum|p| (gamma_n = n u / (1 - n u)); the lo sum
+        //  by <= n u * (u sum|c|); FP64 chunk scaling and reductions by a few 2^-52.
+        //  FP64 path: (n + 2 * nsl_tp + 8) 2^-53.
+        const double u32 = 5.9604644775390625e-08, u64 = 1.1102230246251565e-16;
+        const double n = (double)(1ull << a.jdl[j]);
+        double rel;
+        if (E.joint) {
+            const double g = n * u32 / (1.0 - n * u32);
+            rel = g * g + 2.0 * n * u32 * u32 + 1.5e-14 + 64.0 * u64;
+        } else {
+            rel = (n + 2.0 * E.nsl_tp + 8.0 + (double)E.nsl_th) * 2.0 * u64;
+        }
+        eb = rel * E.sum_abs_bound * mag;
+    }
+    a.job_vals[j] = v;
+    a.job_err[j] = eb;
+}
+
+__global__ void out_reduce_kernel(KArgs a) {
+    const int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= a.nout) return;
+    double sx = 0.0, sy = 0.0, eb = 0.0;
+    for (int j = a.out_jobs[o]; j < a.out_jobs[o + 1]; j++) {
+        sx += a.job_vals[j].x;
+        sy += a.job_vals[j].y;
+        eb += a.job_err[j];
+    }
+    const double mod = sqrt(sx * sx + sy * sy);
+    eb += 4.0 * 1.1102230246251565e-16 * mod;  // FP64 output rounding
+    if (a.out_prob) {
+        a.out[o] = sx * sx + sy * sy;
+        if (a.err) a.err[o] = eb * (2.0 * mod + eb);
+    } else {
+        a.out[2 * o] = sx;
+        a.out[2 * o + 1] = sy;
+        if (a.err) a.err[o] = eb;
+    }
+}
+
+}  // namespace pq

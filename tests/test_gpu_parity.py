@@ -1,0 +1,251 @@
+"""GPU parity: the sm_103a path through the C-ABI against the CPU oracle.
+
+Bit-exact: normal forms (engine dumps) and the Z8 index of every branch.
+Numerical: amplitudes within 1e-6 relative of the FP64 oracle and within the per-result
+error bound the library reports; probabilities within 1e-12 absolute.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from polyq_gb300 import Batch, Simulator, set_tuning, get_tuning
+from polyq_gb300 import _native as N
+from polyq_gb300.circuit import Circuit
+from polyq_gb300.rng import (Rng, random_clifford_t, random_layered, random_outputs, workload_batch,
+                             workload_many_boundaries, workload_small)
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-6  # amplitude tolerance relative to the FP64 oracle
+PROB_ABS = 1e-12
+
+
+def assert_amps(got, want, err=None, rel=REL):
+    """Every result within its reported bound; amplitudes within `rel` of the FP64 value,
+    except ones that cancel (|want| < 1e-3 of the batch scale), which must be within 1e-7 of
+    the scale -- a relative error of an (almost) exactly cancelled sum is not defined."""
+    got = np.asarray(got)
+    want = np.asarray(want)
+    diff = np.abs(got - want)
+    scale = float(np.max(np.abs(want))) if want.size else 0.0
+    floor = 1e-300 + 1e-7 * scale
+    ok = diff <= rel * np.abs(want) + floor
+    big = np.abs(want) >= 1e-3 * scale
+    assert np.all(diff[big] <= rel * np.abs(want[big]) + 1e-300), "relative error above %g" % rel
+    if err is not None:
+        # the FP64 reference carries its own rounding (~1e-16 per term): allow 1e-13 of scale
+        ref_err = 1e-13 * max(1.0, float(np.max(np.abs(want)))) if want.size else 0.0
+        assert np.all(diff <= err + ref_err), "error bound violated: %s" % (diff - err).max()
+    assert np.all(ok), "max rel err %.3e" % float(np.max(diff / np.maximum(np.abs(want), 1e-300)))
+
+
+def test_known_answers(gpu):
+    import json, os
+    with open(os.path.join(os.path.dirname(__file__), "golden", "known_answers.json")) as f:
+        ka = json.load(f)
+    for case in ka["amplitudes"]:
+        c = Circuit(case["num_qubits"])
+        for op in case["ops"]:
+            c.push(*op)
+        s = Simulator(c)
+        xs = [v[0] for v in case["values"]]
+        ys = [v[1] for v in case["values"]]
+        want = np.array([complex(v[2], v[3]) for v in case["values"]])
+        got, err = s.amplitudes(xs, ys, with_error=True)
+        assert np.all(np.abs(got - want) <= np.maximum(REL * np.abs(want), err) + 1e-15), case["source"]
+        p = s.probabilities(xs, ys)
+        assert np.all(np.abs(p - np.abs(want) ** 2) <= PROB_ABS), case["source"]
+
+
+def test_branch_phases_bit_exact(gpu):
+    rng = Rng(21)
+    checked = 0
+    for trial in range(60):
+        n = 1 + rng.below(4)
+        c = random_clifford_t(n, 8 + rng.below(14), rng.below(6), trial % 3 == 0, rng)
+        for strat in ("cached", "auto"):
+            s = Simulator(c, strat)
+            r = O.OracleSim(c, strat)
+            nb = s.stats_full()["num_branches"]
+            for b in range(nb):
+                for x, y in ((0, 0), (1 % (1 << n), (1 << n) - 1)):
+                    want = r.branch_phases(x, y, b)
+                    got = s.branch_phases(x, y, b) if b == 0 else None
+                    if b != 0:
+                        continue
+                    if want is None:
+                        assert got is None
+                        continue
+                    assert got is not None and np.array_equal(got, want)
+                    checked += 1
+    assert checked > 40
+
+
+def test_branch_phases_bit_exact_workloads(gpu):
+    c = workload_small(1)
+    s, r = Simulator(c, "cached"), O.OracleSim(c, "cached")
+    ys = [0] + random_outputs(c.num_qubits, 40, 5)
+    seen = 0
+    for y in ys:
+        want = r.branch_phases(0, y)
+        got = s.branch_phases(0, y)
+        assert (want is None) == (got is None)
+        if want is not None:
+            assert np.array_equal(got, want)
+            seen += 1
+    c = workload_many_boundaries(0)
+    s, r = Simulator(c, "auto"), O.OracleSim(c, "auto")
+    for y in random_outputs(50, 3, 9):
+        want = r.branch_phases(0, y, 0)
+        got = s.branch_phases(0, y, 0)
+        assert want is not None and np.array_equal(got, want)
+
+
+def test_engine_dumps_match_oracle(gpu):
+    for c in (workload_small(1), workload_many_boundaries(0)):
+        s, r = Simulator(c), O.OracleSim(c)
+        for b in range(r.stats()["branches"]):
+            assert np.array_equal(s.engine_dump(b), r.engine_dump(b))
+
+
+def test_engine_matches_brute_force(gpu):
+    # src/engine.rs:746-774 on the GPU path
+    rng = Rng(21)
+    for trial in range(120):
+        n = 1 + rng.below(4)
+        c = random_clifford_t(n, 8 + rng.below(14), rng.below(6), trial % 3 == 0, rng)
+        s = Simulator(c, "cached")
+        r = O.OracleSim(c, "cached")
+        xs = [x for x in range(1 << n) for _ in range(1 << n)]
+        ys = [y for _ in range(1 << n) for y in range(1 << n)]
+        got, err = s.amplitudes(xs, ys, with_error=True)
+        want = np.array([r.brute_force(x, y) for x, y in zip(xs, ys)])
+        assert_amps(got, want, err)
+
+
+def test_statevector_matches_dense_all_strategies(gpu):
+    # src/sim.rs:330-342 on the GPU path
+    rng = Rng(99)
+    for trial in range(50):
+        n = 1 + rng.below(5)
+        if trial % 2 == 0:
+            c = random_clifford_t(n, 25, rng.below(8), trial % 4 == 0, rng)
+        else:
+            c = random_layered(n, 2 + rng.below(2), rng)
+        inp = sum(1 << q for q in range(n) if rng.next_f64() < 0.5)
+        want = O.dense_statevector(c, inp)
+        for strat, p in (("cached", None), ("auto", None), ("auto", 2), ("auto", 100)):
+            s = Simulator(c, strat, p)
+            got, err = s.amplitudes([inp] * (1 << n), list(range(1 << n)), with_error=True)
+            assert_amps(got, want, err)
+            probs = s.probabilities([inp] * (1 << n), list(range(1 << n)))
+            assert np.max(np.abs(probs - np.abs(want) ** 2)) <= PROB_ABS
+
+
+def test_marginals_match_dense(gpu):
+    rng = Rng(3)
+    for _ in range(12):
+        n = 2 + rng.below(3)
+        c = random_layered(n, 2, rng)
+        sv = O.dense_statevector(c, 0)
+        s = Simulator(c)
+        for _ in range(4):
+            k = 1 + rng.below(n)
+            qs = list(range(n))
+            for i in range(n - 1, 0, -1):
+                j = rng.below(i + 1)
+                qs[i], qs[j] = qs[j], qs[i]
+            meas = [(q, rng.next_f64() < 0.5) for q in qs[:k]]
+            want = sum(abs(a) ** 2 for i, a in enumerate(sv) if all(((i >> q) & 1) == b for q, b in meas))
+            assert abs(s.marginal(0, meas) - want) < 1e-6
+
+
+def test_small_workload_vs_oracle_and_dense(gpu):
+    c = workload_small(1)
+    s = Simulator(c)
+    r = O.OracleSim(c)
+    sv = O.dense_statevector(c, 0)
+    ys = [0] + [int(i) for i in np.nonzero(np.abs(sv) > 1e-9)[0][:200]]
+    got, err = s.amplitudes([0] * len(ys), ys, with_error=True)
+    assert_amps(got, r.amplitudes([0] * len(ys), ys), err)
+    assert_amps(got, sv[ys], None, rel=1e-6)
+    p = s.probabilities([0] * len(ys), ys)
+    assert np.max(np.abs(p - np.abs(sv[ys]) ** 2)) <= PROB_ABS
+
+
+def test_many_boundaries_sample_vs_oracle(gpu):
+    c = workload_many_boundaries(0)
+    s = Simulator(c)
+    r = O.OracleSim(c)
+    ys = random_outputs(50, 24, 2024)
+    got, err = s.amplitudes([0] * len(ys), ys, with_error=True)
+    want = r.amplitudes([0] * len(ys), ys)
+    assert_amps(got, want, err)
+
+
+def test_many_boundaries_full_fp32_vs_device_fp64(gpu):
+    # full size: all 4096 boundaries, FP32-compensated against the device FP64 mode
+    c = workload_many_boundaries(0)
+    s = Simulator(c)
+    ys = random_outputs(50, 4096, 1)
+    got, err = s.amplitudes([0] * 4096, ys, with_error=True)
+    ref = s.amplitudes_fp64([0] * 4096, ys)
+    diff = np.abs(got - ref)
+    assert np.all(diff <= err + 1e-300)
+    rel = diff / np.abs(ref)
+    assert np.max(rel) <= REL
+    assert np.median(rel) < 1e-10
+
+
+def test_batch_equals_individual_and_plain(gpu):
+    circs = workload_batch(8, seed=3, t_max=14)
+    sims = [Simulator(c) for c, _ in circs]
+    outs = [random_outputs(c.num_qubits, 5, i) for i, (c, _) in enumerate(circs)]
+    b = Batch(sims, [5] * len(sims))
+    xs, ys = b.pack([[0] * 5] * len(sims), outs)
+    got = b.run(xs, ys)
+    for i, s in enumerate(sims):
+        alone = s.amplitudes([0] * 5, outs[i])
+        assert np.array_equal(got[5 * i:5 * i + 5], alone)  # same work decomposition: bit-identical
+        plain = s.amplitudes_plain([0] * 5, outs[i])
+        assert np.array_equal(plain, alone)
+        r = O.OracleSim(circs[i][0])
+        assert_amps(alone, r.amplitudes([0] * 5, outs[i]))
+
+
+def test_admission_and_invalid_arguments(gpu):
+    c = workload_many_boundaries(0)
+    old = get_tuning()
+    try:
+        set_tuning(max_branch_dim=10)
+        s = Simulator(c, "cached")
+        with pytest.raises(N.PqError) as e:
+            s.amplitudes([0], [1])
+        assert e.value.status == 3
+    finally:
+        set_tuning(max_branch_dim=old["max_branch_dim"])
+    s = Simulator(workload_small(1))
+    with pytest.raises(ValueError):
+        s.amplitudes([0], [1 << 40])
+    with pytest.raises(N.PqError) as e:
+        s.marginal(0, [(99, 1)])
+    assert e.value.status == 1
+
+
+def test_device_resident_path_matches_host_path(gpu):
+    torch = pytest.importorskip("torch")
+    import ctypes as ct
+    c = workload_many_boundaries(0)
+    s = Simulator(c)
+    ys = random_outputs(50, 64, 77)
+    host = s.amplitudes([0] * 64, ys)
+    from polyq_gb300.sim import pack_bits
+    dx = torch.from_numpy(pack_bits([0] * 64, 50).view(np.int64)).cuda()
+    dy = torch.from_numpy(pack_bits(ys, 50).view(np.int64)).cuda()
+    out = torch.zeros(128, dtype=torch.float64, device="cuda")
+    st = torch.cuda.current_stream().cuda_stream
+    N.check(N.lib().pq_amplitudes_device(s.handle, 64, ct.c_void_p(dx.data_ptr()), ct.c_void_p(dy.data_ptr()),
+                                         ct.c_void_p(out.data_ptr()), None, ct.c_void_p(st)))
+    torch.cuda.synchronize()
+    dev = out.cpu().numpy().view(np.complex128)
+    assert np.array_equal(dev, host)
