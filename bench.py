@@ -1,0 +1,355 @@
+"""Throughput of the GB300 amplitude path on the one-circuit, many-boundaries workload.
+
+Workload: a seeded Clifford+T circuit with n=50 qubits, 2000 gates from {H,S,CX,CZ,T}
+(exactly 32 T, seed 0: the radical-constrained branch subspace of the cached engine has
+2^29 > 2^22 branches), 4096 uniform output bitstrings y, x = 0, strategy auto (the
+reference's Simulator::new default: 16 branch engines of d = 19..21).  One step evaluates
+all 4096 amplitudes.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+value      branches/s with boundaries resident in HBM (pq_amplitudes_device), CUDA events on
+           the launching stream, L2 flushed (512 MiB write) between steps outside the events
+e2e        same metric through the public host-buffer call pq_amplitudes (H2D of the
+           boundaries and D2H of amplitudes + error bounds inside the timed region)
+roofline   enumeration kernel: reference-form integer ops (5 W_o + 6 W_g int64 per branch)
+           per launch over its event-timed duration, against the integer-pipe rate measured
+           on the device (lop3 / popc microbenchmark)
+cpu_baseline  the CPU oracle (a restatement of the reference engine) on all host threads
+--impl reference  times the same CPU restatement on the same workload (bounded sample)
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "polyq-v1.0_gb300"))
+
+WORKLOAD = {"n_qubits": 50, "gates": 2000, "t_count": 32, "circuit_seed": 0, "boundaries": 4096,
+            "output_seed": 1, "strategy": "auto"}
+METRIC = "branches/s and amplitudes/s at <=1e-6 rel err vs FP64; served p50/p99 latency"
+
+
+def workload():
+    from polyq_gb300.rng import random_outputs, workload_many_boundaries
+    c = workload_many_boundaries(WORKLOAD["circuit_seed"])
+    ys = random_outputs(WORKLOAD["n_qubits"], WORKLOAD["boundaries"], WORKLOAD["output_seed"])
+    return c, ys
+
+
+def config(extra=None):
+    cfg = {"workload": "one circuit, many boundaries: n=50, 2000 gates, 32 T (seed 0), 4096 uniform y, x=0, "
+                       "strategy auto",
+           **WORKLOAD, "l2": "flushed between steps (512 MiB write)", "parallelism": "replicas"}
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = str(gpu_index)
+        self.lines = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", self.gpu, "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_init(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if args.impl == "gb300" else "gloo")
+        return dist, int(os.environ.get("RANK", "0")), ws, int(os.environ.get("LOCAL_RANK", "0"))
+    return None, 0, 1, 0
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_rate(circ, ys, sample, threads):
+    """CPU restatement of the reference engine on `sample` boundaries (branches/s)."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    sim = oracle.OracleSim(circ, "auto")
+    st = sim.stats()
+    per_amp = None
+    sub = ys[:sample]
+    sim.amplitudes([0], sub[:1], nthreads=threads)  # warm caches
+    t0 = time.perf_counter()
+    sim.amplitudes([0] * len(sub), sub, nthreads=threads)
+    dt = time.perf_counter() - t0
+    return sim, st, dt
+
+
+def branches_per_amp_and_ops(sim):
+    """Sum over branch engines of 2^d and of 2^d * (5 W_o + 6 W_g) reference-form int64 ops,
+    plus the popc64 / logic64 split (src/normal_form.rs:479-493, src/engine.rs:700-718)."""
+    st = sim.stats_full()
+    br = ops = popc = logic = 0.0
+    for b in range(st["num_branches"]):
+        h = sim.engine_dump(b)[:8]
+        g, nodd, d = int(h[1]), int(h[2]), int(h[5])
+        wo, wg = (nodd + 63) // 64, (g + 63) // 64
+        n = float(1 << d)
+        br += n
+        ops += n * (5 * wo + 6 * wg)
+        popc += n * (2 * wo + wg)
+        logic += n * (3 * wo + 5 * wg)
+    return br, ops, popc, logic
+
+
+def run_reference(args):
+    dist, rank, ws, _ = dist_init(args)
+    if rank != 0:
+        return 0
+    circ, ys = workload()
+    threads = cpu_threads()
+    sample = max(4, int(args.ref_sample))
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    sim = oracle.OracleSim(circ, "auto")
+    st = sim.stats()
+    bpa = None
+    # branches per amplitude from the oracle's own engines
+    bpa = 0
+    for b in range(st["branches"]):
+        h = sim.engine_dump(b)[:8]
+        bpa += 1 << int(h[5])
+    for w in range(args.warmup):
+        sim.amplitudes([0] * 2, ys[:2], nthreads=threads)
+    times = []
+    for k in range(args.steps):
+        sub = ys[(k * sample) % len(ys):][:sample]
+        t0 = time.perf_counter()
+        sim.amplitudes([0] * len(sub), sub, nthreads=threads)
+        times.append(time.perf_counter() - t0)
+    ms = 1e3 * sum(times) / len(times)
+    value = sample * bpa / (ms * 1e-3)
+    line = {"metric": METRIC, "impl": "reference", "value": value, "unit": "branches/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64+f64", "data": "synthetic",
+            "amplitudes_per_s": sample / (ms * 1e-3),
+            "config": config({"sample_per_step": sample}),
+            "cpu_baseline": {"value": value, "unit": "branches/s", "cores": threads, "kind": "port",
+                             "sample": "%d of the 4096 boundaries per step, same circuit, strategy auto" % sample},
+            "e2e": {"value": value, "unit": "branches/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gb300(args):
+    import ctypes as ct
+
+    import numpy as np
+    import torch
+
+    dist, rank, ws, local = dist_init(args)
+    torch.cuda.set_device(local)
+    import polyq_gb300 as pq
+    from polyq_gb300 import _native as N
+    from polyq_gb300.sim import pack_bits
+    L = N.lib()
+    N.check(L.pq_init(local))
+    circ, ys = workload()
+    n = len(ys)
+    sim = pq.Simulator(circ, "auto")
+    stats = sim.stats_full()
+    bpa, ops_amp, popc_amp, logic_amp = branches_per_amp_and_ops(sim)
+    branches_step = bpa * n
+    xs_h = pack_bits([0] * n, circ.num_qubits)
+    ys_h = pack_bits(ys, circ.num_qubits)
+    dx = torch.from_numpy(xs_h.view(np.int64)).cuda()
+    dy = torch.from_numpy(ys_h.view(np.int64)).cuda()
+    dout = torch.zeros(2 * n, dtype=torch.float64, device="cuda")
+    derr = torch.zeros(n, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.Stream()
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+
+    def step_device():
+        N.check(L.pq_amplitudes_device(sim.handle, n, ct.c_void_p(dx.data_ptr()), ct.c_void_p(dy.data_ptr()),
+                                       ct.c_void_p(dout.data_ptr()), ct.c_void_p(derr.data_ptr()),
+                                       ct.c_void_p(stream.cuda_stream)))
+
+    kms = (ct.c_float * 3)()
+    with torch.cuda.stream(stream):
+        for _ in range(max(3, args.warmup)):
+            step_device()
+        torch.cuda.synchronize()
+        peaks = (ct.c_double * 4)()
+        N.check(L.pq_measure_peaks(peaks))
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        step_ms, enum_ms = [], []
+        with ClockSampler(local) as clk:
+            t_wall0 = time.perf_counter()
+            for _ in range(args.steps):
+                flush.zero_()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                step_device()
+                e1.record(stream)
+                e1.synchronize()
+                step_ms.append(e0.elapsed_time(e1))
+                N.check(L.pq_sim_kernel_ms(sim.handle, n, kms))
+                enum_ms.append(kms[1])
+            torch.cuda.synchronize()
+            t_wall = time.perf_counter() - t_wall0
+        clocks = clk.summary()
+        ms = sum(step_ms) / len(step_ms)
+        if dist:
+            t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        value = ws * branches_step / (ms * 1e-3)
+        # FP32-compensated results of the last step against the device FP64 mode
+        got = dout.cpu().numpy().view(np.complex128).copy()
+        errb = derr.cpu().numpy().copy()
+    ref = sim.amplitudes_fp64([0] * n, ys)
+    rel = np.abs(got - ref) / np.abs(ref)
+    # e2e through the public host-buffer call
+    for _ in range(2):
+        sim.amplitudes([0] * n, ys)
+    e2e_s = []
+    out_h = np.zeros(2 * n)
+    err_h = np.zeros(n)
+    import ctypes
+    P = lambda a, t: a.ctypes.data_as(ctypes.POINTER(t))  # noqa: E731
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        N.check(L.pq_amplitudes(sim.handle, n, P(xs_h, ct.c_uint64), P(ys_h, ct.c_uint64), P(out_h, ct.c_double),
+                                P(err_h, ct.c_double)))
+        e2e_s.append(time.perf_counter() - t0)
+    e2e_ms = 1e3 * sum(e2e_s) / len(e2e_s)
+    if dist:
+        t = torch.tensor([e2e_ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = ws * branches_step / (e2e_ms * 1e-3)
+    # roofline of the enumeration kernel (reference-form integer work)
+    enum_avg = sum(enum_ms) / len(enum_ms)
+    lop3, popcr = peaks[0], peaks[1]
+    t_branch_at_peak = max(2.0 * popc_amp / popcr, 2.0 * logic_amp / lop3) / bpa  # s per branch
+    ops_branch = ops_amp / bpa
+    peak_ops = ops_branch / t_branch_at_peak
+    achieved = ops_amp * n / (enum_avg * 1e-3)
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        threads = cpu_threads()
+        sample = max(4, int(args.cpu_sample))
+        _, _, dt = cpu_rate(circ, ys, sample, threads)
+        cpu = {"value": sample * bpa / dt, "unit": "branches/s", "cores": threads, "kind": "port",
+               "sample": "%d of the 4096 boundaries, same circuit and strategy (auto), CPU restatement of the "
+                         "reference engine" % sample}
+    line = {
+        "metric": METRIC, "value": value, "unit": "branches/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64+f32", "data": "synthetic",
+        "amplitudes_per_s": ws * n / (ms * 1e-3),
+        "config": config({"branch_engines": stats["num_branches"], "pairs": stats["pairs"],
+                          "branches_per_step": branches_step, "wall_s_timed_region": t_wall}),
+        "precision": {"max_rel_err_vs_fp64": float(np.max(rel)), "median_rel_err_vs_fp64": float(np.median(rel)),
+                      "max_errbound_rel": float(np.max(errb / np.abs(ref)))},
+        "e2e": {"value": e2e_value, "unit": "branches/s", "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": int(xs_h.nbytes + ys_h.nbytes),
+                "d2h_bytes_per_step": int(out_h.nbytes + err_h.nbytes + 4)},
+        "gpu_launches": 4 * args.steps,
+        "roofline": {"bound": "int", "achieved": achieved / 1e12, "peak": peak_ops / 1e12, "unit": "Tops/s",
+                     "frac": achieved / peak_ops, "traffic": None,
+                     "kernel": "enum_kernel", "kernel_ms": enum_avg, "ops": "reference-form int64 ops/branch %.1f" %
+                     ops_branch, "peak_source": "measured lop3.b32 %.3e/s, popc.b32 %.3e/s on this device" %
+                     (lop3, popcr)},
+        "clocks": clocks,
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-sample", type=int, default=48)
+    ap.add_argument("--ref-sample", type=int, default=24)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--boundaries", type=int, default=4096, help="boundary count (profiling of smaller cases)")
+    args = ap.parse_args()
+    WORKLOAD["boundaries"] = args.boundaries
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

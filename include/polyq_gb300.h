@@ -162,6 +162,17 @@ PQ_API int64_t pq_server_poll(pq_server *s, pq_result *out, int64_t cap, double 
 PQ_API double pq_server_now(const pq_server *s);
 PQ_API pq_status pq_server_drain(pq_server *s, double timeout_s);
 
+/* ---- measurement -------------------------------------------------------------------- */
+/* Device times (ms) of the last completed launch of the simulator's size-n plan (and of a
+ * batch): [0] prepare, [1] enumeration, [2] reductions.  Blocks until that launch is done. */
+PQ_API pq_status pq_sim_kernel_ms(pq_sim *sim, int64_t n, float *ms);
+PQ_API pq_status pq_batch_kernel_ms(pq_batch *b, float *ms);
+/* Work items of the simulator's size-n plan (-1 if it has no such plan yet). */
+PQ_API int64_t pq_sim_launch_items(pq_sim *sim, int64_t n);
+/* Issue rates measured on the current device: [0] lop3.b32 ops/s, [1] popc.b32 ops/s,
+ * [2] add.f32 ops/s, [3] SM count. */
+PQ_API pq_status pq_measure_peaks(double out[4]);
+
 /* ---- checks (bit-exact comparisons against a CPU restatement) ------------------------ */
 /* Canonical dump of branch engine `branch`: normal form, diagonal masks, kernel and
  * boundary columns, RREF; returns the word count (out = NULL to size), < 0 on error. */

@@ -172,9 +172,16 @@ struct Plan {
     std::vector<int> job_engine_d;
     std::vector<JobDev> jobs_host;
     KArgs args{};
+    // ev_in/ev_out order the plan's stream against a caller's stream; tev[0..3] bracket
+    // prepare | enumerate | reductions inside every launch (event-record nodes in the graph)
+    cudaEvent_t ev_in = nullptr, ev_out = nullptr, tev[4] = {nullptr, nullptr, nullptr, nullptr};
     ~Plan() {
         if (gexec) cudaGraphExecDestroy(gexec);
         if (graph) cudaGraphDestroy(graph);
+        if (ev_in) cudaEventDestroy(ev_in);
+        if (ev_out) cudaEventDestroy(ev_out);
+        for (auto &e : tev)
+            if (e) cudaEventDestroy(e);
         if (own_stream && stream) cudaStreamDestroy(stream);
     }
 };
@@ -283,6 +290,9 @@ static pq_status build_plan(const std::vector<Segment> &segs, int nw, cudaStream
     CU(P.out.alloc((size_t)P.nout * 2 * sizeof(double)));
     CU(P.err.alloc((size_t)P.nout * sizeof(double)));
     CU(P.errflag.alloc(sizeof(int)));
+    CU(cudaEventCreateWithFlags(&P.ev_in, cudaEventDisableTiming));
+    CU(cudaEventCreateWithFlags(&P.ev_out, cudaEventDisableTiming));
+    for (auto &e : P.tev) CU(cudaEventCreate(&e));
     CU(P.hx.alloc((size_t)P.nreq * nw * 8));
     CU(P.hy.alloc((size_t)P.nreq * nw * 8));
     CU(P.hout.alloc((size_t)P.nout * 2 * sizeof(double)));
@@ -334,15 +344,23 @@ static pq_status build_plan(const std::vector<Segment> &segs, int nw, cudaStream
 // Enqueue the core launch sequence on P.stream (capturable).
 static cudaError_t enqueue_core(Plan &P, int mode) {
     cudaError_t e;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if ((e = cudaStreamIsCapturing(P.stream, &cs)) != cudaSuccess) return e;
+    // timing events become event-record nodes of the graph while capturing
+    const unsigned evflag = cs == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
     e = cudaMemsetAsync(P.errflag.p, 0, sizeof(int), P.stream);
     if (e != cudaSuccess) return e;
-    prepare_kernel<<<P.grid_prep, 128, (size_t)4 * P.smem_words * 8, P.stream>>>(P.args);
     e = cudaMemsetAsync(P.counter.p, 0, sizeof(unsigned long long), P.stream);
     if (e != cudaSuccess) return e;
+    if ((e = cudaEventRecordWithFlags(P.tev[0], P.stream, evflag)) != cudaSuccess) return e;
+    prepare_kernel<<<P.grid_prep, 128, (size_t)4 * P.smem_words * 8, P.stream>>>(P.args);
+    if ((e = cudaEventRecordWithFlags(P.tev[1], P.stream, evflag)) != cudaSuccess) return e;
     if (mode == 1) enum_kernel<1><<<P.grid_enum, P.block_enum, 0, P.stream>>>(P.args);
     else enum_kernel<0><<<P.grid_enum, P.block_enum, 0, P.stream>>>(P.args);
+    if ((e = cudaEventRecordWithFlags(P.tev[2], P.stream, evflag)) != cudaSuccess) return e;
     job_reduce_kernel<<<(P.njobs + 255) / 256, 256, 0, P.stream>>>(P.args);
     out_reduce_kernel<<<(P.nout + 255) / 256, 256, 0, P.stream>>>(P.args);
+    if ((e = cudaEventRecordWithFlags(P.tev[3], P.stream, evflag)) != cudaSuccess) return e;
     return cudaGetLastError();
 }
 
@@ -407,17 +425,13 @@ static pq_status run_host(Plan &P, const uint64_t *x, const uint64_t *y, double 
     return PQ_OK;
 }
 
-// Device-buffer run on `stream` (no host synchronisation).
+// Device-buffer run ordered after, and waited for by, the caller's `stream` (CUDA convention:
+// NULL is the legacy default stream).  No host synchronisation.
 static pq_status run_device(Plan &P, const uint64_t *x, const uint64_t *y, double *out, double *err,
                             cudaStream_t stream) {
     const size_t bw = (size_t)P.nreq * P.nw * 8;
-    cudaStream_t s = stream ? stream : P.stream;
-    cudaEvent_t ev = nullptr;
-    if (s != P.stream) {  // order the plan's stream after the caller's
-        CU(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-        CU(cudaEventRecord(ev, s));
-        CU(cudaStreamWaitEvent(P.stream, ev, 0));
-    }
+    CU(cudaEventRecord(P.ev_in, stream));
+    CU(cudaStreamWaitEvent(P.stream, P.ev_in, 0));
     if (x != P.x.as<uint64_t>()) CU(cudaMemcpyAsync(P.x.p, x, bw, cudaMemcpyDeviceToDevice, P.stream));
     if (y != P.y.as<uint64_t>()) CU(cudaMemcpyAsync(P.y.p, y, bw, cudaMemcpyDeviceToDevice, P.stream));
     pq_status st = launch_graph(P);
@@ -426,10 +440,16 @@ static pq_status run_device(Plan &P, const uint64_t *x, const uint64_t *y, doubl
         CU(cudaMemcpyAsync(out, P.out.p, (size_t)P.nout * 16, cudaMemcpyDeviceToDevice, P.stream));
     if (err && err != P.err.as<double>())
         CU(cudaMemcpyAsync(err, P.err.p, (size_t)P.nout * 8, cudaMemcpyDeviceToDevice, P.stream));
-    if (ev) {
-        CU(cudaEventRecord(ev, P.stream));
-        CU(cudaStreamWaitEvent(s, ev, 0));
-        cudaEventDestroy(ev);
+    CU(cudaEventRecord(P.ev_out, P.stream));
+    CU(cudaStreamWaitEvent(stream, P.ev_out, 0));
+    return PQ_OK;
+}
+
+// Device times (ms) of the last completed launch: prepare, enumerate, reductions.
+static pq_status last_kernel_ms(Plan &P, float *ms) {
+    for (int i = 0; i < 3; i++) {
+        cudaError_t e = cudaEventElapsedTime(&ms[i], P.tev[i], P.tev[i + 1]);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaEventElapsedTime");
     }
     return PQ_OK;
 }
@@ -825,6 +845,28 @@ PQ_API pq_status pq_batch_run_device(pq_batch *b, const uint64_t *x, const uint6
     if (!b || !x || !y || !out) return fail(PQ_ERR_INVALID_ARG, "null argument");
     std::lock_guard<std::mutex> lk(b->mu);
     return run_device(*b->plan, x, y, out, err, (cudaStream_t)stream);
+}
+
+PQ_API pq_status pq_sim_kernel_ms(pq_sim *s, int64_t n, float *ms) {
+    if (!s || !ms) return fail(PQ_ERR_INVALID_ARG, "null argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->plans.find(n);
+    if (it == s->plans.end() || !it->second->graph_ready) return fail(PQ_ERR_INVALID_ARG, "no launch of that size yet");
+    CU(cudaEventSynchronize(it->second->tev[3]));
+    return last_kernel_ms(*it->second, ms);
+}
+PQ_API pq_status pq_batch_kernel_ms(pq_batch *b, float *ms) {
+    if (!b || !ms) return fail(PQ_ERR_INVALID_ARG, "null argument");
+    std::lock_guard<std::mutex> lk(b->mu);
+    if (!b->plan->graph_ready) return fail(PQ_ERR_INVALID_ARG, "batch has not run yet");
+    CU(cudaEventSynchronize(b->plan->tev[3]));
+    return last_kernel_ms(*b->plan, ms);
+}
+PQ_API int64_t pq_sim_launch_items(pq_sim *s, int64_t n) {
+    if (!s) return -1;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->plans.find(n);
+    return it == s->plans.end() ? -1 : (int64_t)it->second->nitems;
 }
 
 // ---------------------------------------------------------------- checks

@@ -84,6 +84,10 @@ SIGNATURES = {
     "pq_server_poll": (ct.c_int64, [P, ct.POINTER(Result), ct.c_int64, ct.c_double]),
     "pq_server_now": (ct.c_double, [P]),
     "pq_server_drain": (ct.c_int, [P, ct.c_double]),
+    "pq_sim_kernel_ms": (ct.c_int, [P, ct.c_int64, ct.POINTER(ct.c_float)]),
+    "pq_batch_kernel_ms": (ct.c_int, [P, ct.POINTER(ct.c_float)]),
+    "pq_sim_launch_items": (ct.c_int64, [P, ct.c_int64]),
+    "pq_measure_peaks": (ct.c_int, [f64p]),
     "pq_debug_engine_dump": (ct.c_int64, [P, ct.c_int32, u64p, ct.c_int64]),
     "pq_debug_branch_phases": (ct.c_int32, [P, ct.c_int32, u64p, u64p, u8p]),
 }

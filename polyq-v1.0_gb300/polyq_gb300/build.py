@@ -21,7 +21,7 @@ LIB_PATH = os.path.join(LIB_DIR, "libpolyq_gb300.so")
 OBJ_DIR = os.path.join(ROOT, "_build")
 
 GENCODE = "arch=compute_103a,code=sm_103a"
-SOURCES_CU = ["pq_device.cu"]
+SOURCES_CU = ["pq_device.cu", "pq_peak.cu"]
 SOURCES_CPP = ["pq_host.cpp"]
 HEADERS = ["pq_core.cuh", "pq_kernels.cuh", "pq_host.hpp"]
 
