@@ -117,6 +117,18 @@ PQ_API pq_status pq_amplitudes_device(pq_sim *sim, int64_t n, const uint64_t *x,
  * one-boundary-per-launch path, kept as the comparison baseline for batching). */
 PQ_API pq_status pq_amplitudes_plain(pq_sim *sim, int64_t n, const uint64_t *x, const uint64_t *y, double *out);
 
+/* Allocation-free amplitudes (no counterpart in the reference crate).  For callers that may
+ * not allocate device memory when they need results -- code inside CUDA graph capture, hosts
+ * under an externally enforced device-memory budget, callbacks that forbid allocation.
+ * x, y (n bitstrings each) and out (2n doubles) are DEVICE pointers owned by the caller; the
+ * work is enqueued on `stream` (NULL = legacy default stream) and not waited for.  Per-call
+ * state lives in one fixed 1.7 MiB static device array: n x (branch engines) <= 4096, at most
+ * 64 branch engines and 65536 work items, else PQ_ERR_INVALID_ARG.  The first call on a
+ * device looks up that array's address, so make one call before any stream capture.  Calls
+ * share the array: calls that overlap on the GPU race, serialise them. */
+PQ_API pq_status pq_amplitudes_noalloc(pq_sim *sim, int64_t n, const uint64_t *x, const uint64_t *y, double *out,
+                                       void *stream);
+
 /* ---- batched multi-circuit launch (one persistent, graph-captured launch) ------------ */
 /* Amplitudes of counts[i] boundaries on sims[i], all i, in one CUDA-graph launch of a
  * persistent kernel whose warps pull (circuit, boundary, chunk-range) work items. */

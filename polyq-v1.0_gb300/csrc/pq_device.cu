@@ -931,3 +931,193 @@ PQ_API int32_t pq_debug_branch_phases(pq_sim *s, int32_t branch, const uint64_t 
 }
 
 }  // extern "C"
+
+// ========================================================================================
+// Allocation-free evaluation
+//
+// Some callers cannot allocate device memory at the point where they need amplitudes:
+// code running while a CUDA graph is being captured (cudaMalloc is not capturable), hosts
+// that run under a fixed device-memory budget enforced by an outer allocator, or plugin
+// callbacks invoked from a context that forbids allocation.  For them,
+// pq_amplitudes_noalloc evaluates a resident simulator's amplitudes using only the
+// simulator's already-uploaded structures plus one fixed scratch array that lives in this
+// file as a static __device__ variable (it exists on every GPU that loads the library,
+// until the process exits).  The caller passes device pointers for the boundaries and the
+// results.  The scratch holds the per-call job records, work-item layout and partial sums;
+// every call overwrites it, so calls that overlap on the GPU (two streams, or two host
+// threads) race on it and must be serialised by the caller.
+// ========================================================================================
+namespace pq {
+
+static const int kNaMaxEngines = 64;    // branch engines of the simulator (2^pairs <= 64)
+static const int kNaMaxJobs = 4096;     // boundaries x branch engines per call
+static const int kNaMaxItems = 65536;   // work items (chunk ranges) per call
+
+struct NoAllocScratch {
+    EngineDev engines[kNaMaxEngines];
+    IoMapDev map;
+    JobDev jobs[kNaMaxJobs];
+    int perm[kNaMaxJobs], kinv[kNaMaxJobs], jdl[kNaMaxJobs];
+    unsigned jcpi[kNaMaxJobs];
+    unsigned long long jnch[kNaMaxJobs];
+    long long istart[kNaMaxJobs + 1];
+    int out_jobs[kNaMaxJobs + 1];
+    double2 partials[kNaMaxItems];
+    double2 job_vals[kNaMaxJobs];
+    double job_err[kNaMaxJobs];
+    unsigned long long counter;
+    int errflag;
+};
+
+// The scratch array (about 1.7 MiB).  Host code must not take its address directly: the
+// host-side symbol is only a stand-in; the device address comes from cudaGetSymbolAddress.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocScratch)];
+
+static std::mutex g_na_mu;
+static NoAllocScratch *g_na_ptr[64] = {nullptr};  // device address of the scratch, per device
+
+// Same per-job work shape as the regular launch layout, so each job's partial sums come out
+// in the same order (and the results bit-identical to pq_amplitudes).
+__device__ __forceinline__ void na_job_shape(int d, int DI, int cpl, int &dl, unsigned long long &nch,
+                                             unsigned &cpi) {
+    dl = d <= 5 ? 0 : min(d - 5, DI);
+    nch = 1ull << (d - dl);
+    unsigned long long per = 32ull * (unsigned long long)cpl;
+    while ((nch + per - 1) / per > (1ull << 16)) per *= 2;
+    cpi = (unsigned)(nch < per ? nch : per);
+}
+
+// One block: job records, identity item order, per-job shapes and the item prefix sums.
+__global__ void __launch_bounds__(1024) na_layout_kernel(NoAllocScratch *S, int nreq, int nb, int cpl) {
+    __shared__ long long part[1024];
+    const int njobs = nreq * nb;
+    const int per = (njobs + 1023) / 1024;
+    const int j0 = threadIdx.x * per;
+    long long local = 0;
+    for (int j = j0; j < j0 + per && j < njobs; j++) {
+        JobDev &J = S->jobs[j];
+        J.engine = j % nb;
+        J.iomap = 0;
+        J.req = j / nb;
+        J.out = j / nb;
+        S->perm[j] = j;
+        S->kinv[j] = j;
+        const EngineDev &E = S->engines[j % nb];
+        na_job_shape(E.d, E.DI, cpl, S->jdl[j], S->jnch[j], S->jcpi[j]);
+        local += (long long)((S->jnch[j] + S->jcpi[j] - 1) / S->jcpi[j]);
+    }
+    part[threadIdx.x] = local;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long acc = 0;
+        for (int t = 0; t < 1024; t++) {
+            long long v = part[t];
+            part[t] = acc;
+            acc += v;
+        }
+    }
+    __syncthreads();
+    long long acc = part[threadIdx.x];
+    for (int j = j0; j < j0 + per && j < njobs; j++) {
+        S->istart[j] = acc;
+        acc += (long long)((S->jnch[j] + S->jcpi[j] - 1) / S->jcpi[j]);
+    }
+    if (threadIdx.x == 1023) S->istart[njobs] = acc;
+    for (int o = threadIdx.x; o <= nreq; o += 1024) S->out_jobs[o] = o * nb;
+}
+
+}  // namespace pq
+
+extern "C" PQ_API pq_status pq_amplitudes_noalloc(pq_sim *s, int64_t n, const uint64_t *x, const uint64_t *y,
+                                                  double *out, void *stream) {
+    if (!s || !x || !y || !out) return fail(PQ_ERR_INVALID_ARG, "null argument");
+    if (s->host_only) return fail(PQ_ERR_NO_DEVICE, "simulator was created by pq_analyze (host structures only)");
+    const int nb = (int)s->main.dev.size();
+    if (nb > kNaMaxEngines)
+        return fail(PQ_ERR_INVALID_ARG, "pq_amplitudes_noalloc: simulator has " + std::to_string(nb) +
+                                            " branch engines; the fixed scratch holds at most 64");
+    if (n <= 0 || n * nb > kNaMaxJobs)
+        return fail(PQ_ERR_INVALID_ARG, "pq_amplitudes_noalloc: boundaries x branch engines = " +
+                                            std::to_string(n * nb) + " outside 1..4096 (fixed scratch size)");
+    pq_tuning tu;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        tu = g_tuning;
+    }
+    long long nitems = 0;
+    for (int64_t r = 0; r < n; r++)
+        for (int b = 0; b < nb; b++) {
+            const EngineDev &E = s->main.dev[b];
+            if (E.d > kMaxD || E.rank > kMaxPivots) return fail(PQ_ERR_UNSUPPORTED, "branch engine outside kernel limits");
+            if (E.d > tu.max_branch_dim) return fail(PQ_ERR_ADMISSION_REFUSED, "branch dimension above the cap");
+            int dl;
+            unsigned long long nch;
+            unsigned cpi;
+            job_shape(E.d, E.DI, tu.chunks_per_lane, dl, nch, cpi);
+            nitems += (long long)((nch + cpi - 1) / cpi);
+        }
+    if (nitems > kNaMaxItems)
+        return fail(PQ_ERR_INVALID_ARG, "pq_amplitudes_noalloc: " + std::to_string(nitems) +
+                                            " work items exceed the fixed scratch (65536); pass fewer boundaries");
+    std::lock_guard<std::mutex> lk(s->mu);
+    CU(cudaSetDevice(s->device));
+    if (s->device < 0 || s->device >= 64) return fail(PQ_ERR_INVALID_ARG, "device index above 63");
+    NoAllocScratch *S = nullptr;
+    {
+        // First call on this device: look up the scratch's device address (with this
+        // device current).  Make that first call before any stream capture begins.
+        std::lock_guard<std::mutex> lk2(g_na_mu);
+        if (!g_na_ptr[s->device]) {
+            void *p = nullptr;
+            CU(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+            g_na_ptr[s->device] = reinterpret_cast<NoAllocScratch *>(p);
+        }
+        S = g_na_ptr[s->device];
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    CU(cudaMemcpyAsync(S->engines, s->main.dev.data(), sizeof(EngineDev) * (size_t)nb, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(&S->map, &s->main.iom_dev, sizeof(IoMapDev), cudaMemcpyHostToDevice, st));
+    // counter and error flag must start at zero; everything else is fully rewritten below
+    CU(cudaMemsetAsync(&S->counter, 0, sizeof(unsigned long long) + sizeof(int), st));
+    na_layout_kernel<<<1, 1024, 0, st>>>(S, (int)n, nb, tu.chunks_per_lane);
+    KArgs a{};
+    a.engines = S->engines;
+    a.maps = &S->map;
+    a.jobs = S->jobs;
+    a.njobs = (int)(n * nb);
+    a.perm = S->perm;
+    a.kinv = S->kinv;
+    a.istart = S->istart;
+    a.jdl = S->jdl;
+    a.jcpi = S->jcpi;
+    a.jnch = S->jnch;
+    a.nitems = nitems;
+    a.partials = S->partials;
+    a.counter = &S->counter;
+    a.job_vals = S->job_vals;
+    a.job_err = S->job_err;
+    a.out_jobs = S->out_jobs;
+    a.nout = (int)n;
+    a.out = out;
+    a.err = nullptr;
+    a.out_prob = 0;
+    a.xs = x;
+    a.ys = y;
+    a.nw = s->nw;
+    a.smem_words = std::max(8, s->main.max_words);
+    a.dbg = nullptr;
+    a.errflag = &S->errflag;
+    const size_t psmem = (size_t)4 * a.smem_words * 8;
+    if (psmem > 48 * 1024) CU(cudaFuncSetAttribute(prepare_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
+    const int bw = std::max(1, std::min(8, tu.block_warps));
+    int occ = 0;
+    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, enum_kernel<0>, 32 * bw, 0));
+    const long long want = (long long)sm_count() * std::max(occ, 1);
+    const int grid_enum = (int)std::max(1LL, std::min<long long>(want, (nitems + bw - 1) / bw));
+    prepare_kernel<<<std::max(1, std::min(a.njobs / 4 + 1, 65535)), 128, psmem, st>>>(a);
+    enum_kernel<0><<<grid_enum, 32 * bw, 0, st>>>(a);
+    job_reduce_kernel<<<(a.njobs + 255) / 256, 256, 0, st>>>(a);
+    out_reduce_kernel<<<(a.nout + 255) / 256, 256, 0, st>>>(a);
+    CU(cudaGetLastError());
+    return PQ_OK;
+}
