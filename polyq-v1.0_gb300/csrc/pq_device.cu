@@ -59,19 +59,23 @@ static double now_s() {
 struct DevMem {
     void *p = nullptr;
     size_t n = 0;
+    cudaStream_t astream = nullptr;  // set: stream-ordered allocation from the device memory pool
     DevMem() = default;
     DevMem(const DevMem &) = delete;
     DevMem &operator=(const DevMem &) = delete;
     ~DevMem() { reset(); }
     void reset() {
-        if (p) cudaFree(p);
+        if (p) {
+            if (astream) cudaFreeAsync(p, astream);
+            else cudaFree(p);
+        }
         p = nullptr;
         n = 0;
     }
     cudaError_t alloc(size_t bytes) {
         reset();
         n = std::max<size_t>(bytes, 16);
-        return cudaMalloc(&p, n);
+        return astream ? cudaMallocAsync(&p, n, astream) : cudaMalloc(&p, n);
     }
     template <class T> T *as() const { return reinterpret_cast<T *>(p); }
 };
@@ -95,8 +99,10 @@ struct HostPinned {
 template <class T> static cudaError_t upload(DevMem &m, const std::vector<T> &v) {
     cudaError_t e = m.alloc(v.size() * sizeof(T));
     if (e != cudaSuccess) return e;
-    if (!v.empty()) e = cudaMemcpy(m.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
-    return e;
+    if (v.empty()) return e;
+    // pageable source: the call returns once the data is staged, so `v` may go away after it
+    if (m.astream) return cudaMemcpyAsync(m.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, m.astream);
+    return cudaMemcpy(m.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
 }
 
 // ------------------------------------------------------------------------ targets
@@ -207,13 +213,21 @@ static void job_shape(int d, int DI, int cpl, int &dl, unsigned long long &nch, 
     cpi = (unsigned)std::min<unsigned long long>(nch, per);
 }
 
+// `light`: a one-shot plan (serving waves): device buffers come from the stream-ordered pool
+// and are released in stream order; no pinned host staging.
 static pq_status build_plan(const std::vector<Segment> &segs, int nw, cudaStream_t stream, const pq_tuning &tu,
-                            Plan &P) {
+                            Plan &P, bool light = false) {
     P.nw = nw;
     P.stream = stream;
     if (!P.stream) {
         CU(cudaStreamCreateWithFlags(&P.stream, cudaStreamNonBlocking));
         P.own_stream = true;
+    }
+    if (light) {
+        for (DevMem *m : {&P.engines, &P.maps, &P.jobs, &P.perm, &P.kinv, &P.istart, &P.jdl, &P.jcpi, &P.jnch,
+                          &P.partials, &P.counter, &P.job_vals, &P.job_err, &P.out_jobs, &P.x, &P.y, &P.out, &P.err,
+                          &P.errflag})
+            m->astream = P.stream;
     }
     std::vector<EngineDev> eng;
     std::vector<IoMapDev> maps;
@@ -293,11 +307,13 @@ static pq_status build_plan(const std::vector<Segment> &segs, int nw, cudaStream
     CU(cudaEventCreateWithFlags(&P.ev_in, cudaEventDisableTiming));
     CU(cudaEventCreateWithFlags(&P.ev_out, cudaEventDisableTiming));
     for (auto &e : P.tev) CU(cudaEventCreate(&e));
-    CU(P.hx.alloc((size_t)P.nreq * nw * 8));
-    CU(P.hy.alloc((size_t)P.nreq * nw * 8));
-    CU(P.hout.alloc((size_t)P.nout * 2 * sizeof(double)));
-    CU(P.herr.alloc((size_t)P.nout * sizeof(double)));
-    CU(P.herrflag.alloc(sizeof(int)));
+    if (!light) {
+        CU(P.hx.alloc((size_t)P.nreq * nw * 8));
+        CU(P.hy.alloc((size_t)P.nreq * nw * 8));
+        CU(P.hout.alloc((size_t)P.nout * 2 * sizeof(double)));
+        CU(P.herr.alloc((size_t)P.nout * sizeof(double)));
+        CU(P.herrflag.alloc(sizeof(int)));
+    }
     P.jobs_host = jobs;
     KArgs &a = P.args;
     a.engines = P.engines.as<EngineDev>();
@@ -741,6 +757,39 @@ PQ_API pq_status pq_amplitudes_fp64(pq_sim *s, int64_t n, const uint64_t *x, con
     return PQ_OK;
 }
 
+// Sandwich engines of one measured-qubit list, built and uploaded on first use and cached
+// (caller holds s->mu).  Their fixed set is the first-occurrence order of the variables put
+// by Sandwich::assignment: inputs, C^dagger C outputs, measured junctions (src/sim.rs:95-124).
+static pq_status marg_target(pq_sim *s, const int32_t *qubits, int nmeas, pq_sim::Marg **out) {
+    const int nq = s->circ.nq;
+    std::vector<int> key(qubits, qubits + nmeas);
+    auto it = s->marg.find(key);
+    if (it != s->marg.end()) {
+        *out = it->second.get();
+        return PQ_OK;
+    }
+    if (!s->have_sw) {
+        s->sw = PathSum::sandwich(s->circ, s->junction, s->jneg);
+        s->have_sw = true;
+    }
+    std::vector<std::pair<int, int32_t>> puts;
+    for (int q = 0; q < nq; q++) puts.push_back({q, io_src(q, 0, 0)});
+    for (int q = 0; q < nq; q++) puts.push_back({s->sw.outputs[q], io_src(q, 0, s->sw.out_neg[q])});
+    for (int i = 0; i < nmeas; i++) puts.push_back({s->junction[qubits[i]], io_src(qubits[i], 1, s->jneg[qubits[i]])});
+    auto M = std::make_unique<pq_sim::Marg>();
+    M->tg.iom = build_iomap(puts);
+    try {
+        M->tg.rs = build_rank(s->sw, M->tg.iom.fixed, s->strategy, s->pairs);
+    } catch (const std::exception &e) {
+        return fail(PQ_ERR_INTERNAL, std::string("marginal engine build: ") + e.what());
+    }
+    pq_status st = upload_target(M->tg, s->di_max);
+    if (st != PQ_OK) return st;
+    *out = M.get();
+    s->marg.emplace(key, std::move(M));
+    return PQ_OK;
+}
+
 PQ_API pq_status pq_marginal(pq_sim *s, const uint64_t *x, int32_t nmeas, const int32_t *qubits,
                              const uint8_t *outcomes, double *out) {
     if (!s || !x || !out || nmeas < 0 || (nmeas > 0 && (!qubits || !outcomes)))
@@ -751,48 +800,27 @@ PQ_API pq_status pq_marginal(pq_sim *s, const uint64_t *x, int32_t nmeas, const 
         if (qubits[i] < 0 || qubits[i] >= nq) return fail(PQ_ERR_INVALID_ARG, "measured qubit out of range");
     std::lock_guard<std::mutex> lk(s->mu);
     CU(cudaSetDevice(s->device));
-    if (!s->have_sw) {
-        s->sw = PathSum::sandwich(s->circ, s->junction, s->jneg);
-        s->have_sw = true;
-    }
-    // puts of Sandwich::assignment (src/sim.rs:105-124); the engine's fixed set is the
-    // first-occurrence order of these variables (= io_vars + measured junctions, sim.rs:95-103)
-    std::vector<std::pair<int, int32_t>> puts;
-    for (int q = 0; q < nq; q++) puts.push_back({q, io_src(q, 0, 0)});
-    for (int q = 0; q < nq; q++) puts.push_back({s->sw.outputs[q], io_src(q, 0, s->sw.out_neg[q])});
-    std::vector<int> key;
-    for (int i = 0; i < nmeas; i++) {
-        puts.push_back({s->junction[qubits[i]], io_src(qubits[i], 1, s->jneg[qubits[i]])});
-        key.push_back(qubits[i]);
-    }
-    auto it = s->marg.find(key);
-    if (it == s->marg.end()) {
-        auto M = std::make_unique<pq_sim::Marg>();
-        M->tg.iom = build_iomap(puts);
-        try {
-            M->tg.rs = build_rank(s->sw, M->tg.iom.fixed, s->strategy, s->pairs);
-        } catch (const std::exception &e) {
-            return fail(PQ_ERR_INTERNAL, std::string("marginal engine build: ") + e.what());
-        }
-        pq_status st = upload_target(M->tg, s->di_max);
-        if (st != PQ_OK) return st;
+    pq_sim::Marg *M = nullptr;
+    pq_status st = marg_target(s, qubits, nmeas, &M);
+    if (st != PQ_OK) return st;
+    if (!M->plan) {
         pq_tuning tu;
         {
             std::lock_guard<std::mutex> lk2(g_mu);
             tu = g_tuning;
         }
-        M->plan = std::make_unique<Plan>();
+        auto P = std::make_unique<Plan>();
         std::vector<Segment> segs{{&M->tg, 1}};
-        st = build_plan(segs, s->nw, s->stream, tu, *M->plan);
+        st = build_plan(segs, s->nw, s->stream, tu, *P);
         if (st != PQ_OK) return st;
-        it = s->marg.emplace(key, std::move(M)).first;
+        M->plan = std::move(P);
     }
     std::vector<uint64_t> yv((size_t)s->nw, 0ull);
     for (int i = 0; i < nmeas; i++)
         if (outcomes[i]) yv[qubits[i] >> 6] |= 1ull << (qubits[i] & 63);
     // repeated measured qubits with different outcomes contradict: the map's check makes it 0
     double amp[2];
-    pq_status st = run_host(*it->second->plan, x, yv.data(), amp, nullptr, false);
+    st = run_host(*M->plan, x, yv.data(), amp, nullptr, false);
     if (st != PQ_OK) return st;
     *out = amp[0] > 0.0 ? amp[0] : 0.0;
     return PQ_OK;
@@ -1121,3 +1149,359 @@ extern "C" PQ_API pq_status pq_amplitudes_noalloc(pq_sim *s, int64_t n, const ui
     CU(cudaGetLastError());
     return PQ_OK;
 }
+
+// ========================================================================================
+// Serving loop: continuous batching over resident simulators
+//
+// pq_server_submit queues requests (amplitude, probability, single-qubit-set marginal).  A
+// worker thread forms a wave from the queue head -- at most max_slots requests whose launch
+// memory fits what the budget has left -- and launches it on a free stream of a small pool,
+// then keeps admitting: requests that arrive while earlier waves run go into the next wave on
+// another stream, so their work overlaps on the device.  Finished waves are retired in
+// completion order; every result carries its submit and completion time.  A request whose
+// branch engines exceed the dimension cap, or whose own launch would not fit the budget, is
+// completed at once with PQ_ERR_ADMISSION_REFUSED.  Each boundary's result is the same as
+// when evaluated alone: a job's work decomposition does not depend on the rest of the wave.
+// ========================================================================================
+namespace pq {
+static const int kSrvStreams = 4;
+
+struct SrvReq {
+    pq_request r;
+    double t_submit = 0.0;
+    Target *tg = nullptr;
+    int64_t bytes = 0;
+};
+struct SrvWave {
+    std::vector<SrvReq> reqs;
+    std::unique_ptr<Plan> plan;
+    int slot = -1;
+    int64_t bytes = 0;
+    cudaEvent_t done = nullptr;
+};
+
+// Device bytes of one request's launch state (jobs, item partials, outputs).
+static int64_t request_bytes(const Target &T, const pq_tuning &tu) {
+    int64_t b = 64 + 2 * 2 * 8 + 3 * 8;  // boundaries, outputs
+    for (const auto &E : T.dev) {
+        int dl;
+        unsigned long long nch;
+        unsigned cpi;
+        job_shape(E.d, E.DI, tu.chunks_per_lane, dl, nch, cpi);
+        b += (int64_t)sizeof(JobDev) + 64 + 16 * (int64_t)((nch + cpi - 1) / cpi);
+    }
+    return b;
+}
+}  // namespace pq
+
+struct pq_server {
+    std::vector<pq_sim *> sims;
+    int max_slots = 256;
+    int64_t budget = 0;
+    int max_d = 48;
+    int device = 0;
+    double t0 = 0.0;
+    std::vector<cudaStream_t> streams;
+    std::vector<double *> hbuf;  // pinned per stream: max_slots x (re, im, err)
+    std::vector<char> busy;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<pq::SrvReq> pending;
+    std::vector<pq_result> finished;
+    std::vector<std::unique_ptr<pq::SrvWave>> inflight;
+    int64_t inflight_bytes = 0;
+    bool stop = false;
+    std::thread worker;
+    ~pq_server() {
+        for (auto s : streams) cudaStreamDestroy(s);
+        for (auto p : hbuf) cudaFreeHost(p);
+    }
+};
+
+namespace pq {
+static double srv_now(const pq_server *S) { return now_s() - S->t0; }
+
+static pq_result srv_result(const SrvReq &q, int32_t status, double t) {
+    pq_result r;
+    std::memset(&r, 0, sizeof(r));
+    r.tag = q.r.tag;
+    r.status = status;
+    r.kind = q.r.kind;
+    r.submit_s = q.t_submit;
+    r.done_s = t;
+    return r;
+}
+
+// Resolve a request's target (marginal engines are built on first use).
+static pq_status srv_resolve(pq_server *S, SrvReq &q) {
+    pq_sim *s = S->sims[q.r.sim];
+    if (q.r.kind != PQ_REQ_MARGINAL) {
+        q.tg = &s->main;
+        return PQ_OK;
+    }
+    std::lock_guard<std::mutex> lk(s->mu);
+    pq_sim::Marg *M = nullptr;
+    pq_status st = marg_target(s, &q.r.qubit, 1, &M);
+    if (st == PQ_OK) q.tg = &M->tg;
+    return st;
+}
+
+static pq_status srv_launch(pq_server *S, SrvWave &w, const pq_tuning &tu) {
+    // group by target (stable), boundaries in that order
+    std::stable_sort(w.reqs.begin(), w.reqs.end(), [](const SrvReq &a, const SrvReq &b) { return a.tg < b.tg; });
+    std::vector<Segment> segs;
+    for (auto &q : w.reqs) {
+        if (segs.empty() || segs.back().tg != q.tg) segs.push_back({q.tg, 0});
+        segs.back().count++;
+    }
+    const int n = (int)w.reqs.size();
+    std::vector<uint64_t> xs((size_t)2 * n), ys((size_t)2 * n);
+    for (int i = 0; i < n; i++) {
+        const pq_request &r = w.reqs[i].r;
+        xs[2 * i] = r.x[0];
+        xs[2 * i + 1] = r.x[1];
+        if (r.kind == PQ_REQ_MARGINAL) {
+            ys[2 * i] = ys[2 * i + 1] = 0;
+            if (r.outcome) ys[2 * i + (r.qubit >> 6)] |= 1ull << (r.qubit & 63);
+        } else {
+            ys[2 * i] = r.y[0];
+            ys[2 * i + 1] = r.y[1];
+        }
+    }
+    cudaStream_t st = S->streams[w.slot];
+    w.plan = std::make_unique<Plan>();
+    pq_status ps = build_plan(segs, 2, st, tu, *w.plan, true);
+    if (ps != PQ_OK) return ps;
+    Plan &P = *w.plan;
+    CU(cudaMemcpyAsync(P.x.p, xs.data(), xs.size() * 8, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(P.y.p, ys.data(), ys.size() * 8, cudaMemcpyHostToDevice, st));
+    CU(enqueue_core(P, 0));
+    double *hb = S->hbuf[w.slot];
+    CU(cudaMemcpyAsync(hb, P.out.p, (size_t)n * 16, cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(hb + 2 * S->max_slots, P.err.p, (size_t)n * 8, cudaMemcpyDeviceToHost, st));
+    CU(cudaEventCreateWithFlags(&w.done, cudaEventDisableTiming));
+    CU(cudaEventRecord(w.done, st));
+    return PQ_OK;
+}
+
+static void srv_loop(pq_server *S) {
+    cudaSetDevice(S->device);
+    std::unique_lock<std::mutex> lk(S->mu);
+    while (true) {
+        // retire finished waves
+        bool progressed = false;
+        for (size_t i = 0; i < S->inflight.size();) {
+            SrvWave *w = S->inflight[i].get();
+            cudaError_t q = cudaEventQuery(w->done);
+            if (q == cudaErrorNotReady) {
+                i++;
+                continue;
+            }
+            const double t = srv_now(S);
+            const double *hb = S->hbuf[w->slot];
+            for (size_t k = 0; k < w->reqs.size(); k++) {
+                const SrvReq &rq = w->reqs[k];
+                pq_result r = srv_result(rq, q == cudaSuccess ? PQ_OK : PQ_ERR_DEVICE, t);
+                const double re = hb[2 * k], im = hb[2 * k + 1], eb = hb[2 * S->max_slots + k];
+                if (rq.r.kind == PQ_REQ_AMPLITUDE) {
+                    r.re = re;
+                    r.im = im;
+                    r.errbound = eb;
+                } else if (rq.r.kind == PQ_REQ_PROBABILITY) {
+                    r.re = re * re + im * im;
+                    r.errbound = eb * (2.0 * std::sqrt(r.re) + eb);
+                } else {
+                    r.re = re > 0.0 ? re : 0.0;
+                    r.errbound = eb;
+                }
+                S->finished.push_back(r);
+            }
+            S->inflight_bytes -= w->bytes;
+            S->busy[w->slot] = 0;
+            std::unique_ptr<SrvWave> dead = std::move(S->inflight[i]);
+            S->inflight.erase(S->inflight.begin() + (long)i);
+            lk.unlock();
+            if (dead->done) cudaEventDestroy(dead->done);
+            dead.reset();  // stream-ordered frees of the wave's buffers
+            lk.lock();
+            progressed = true;
+        }
+        if (progressed) S->cv_done.notify_all();
+        if (S->stop && S->pending.empty() && S->inflight.empty()) break;
+        int slot = -1;
+        for (int k = 0; k < (int)S->busy.size(); k++)
+            if (!S->busy[k]) {
+                slot = k;
+                break;
+            }
+        if (slot >= 0 && !S->pending.empty()) {
+            // candidates from the head of the queue
+            std::vector<SrvReq> cand;
+            while (!S->pending.empty() && (int)cand.size() < S->max_slots) {
+                cand.push_back(S->pending.front());
+                S->pending.pop_front();
+            }
+            const int64_t room = S->budget - S->inflight_bytes;
+            lk.unlock();
+            pq_tuning tu;
+            {
+                std::lock_guard<std::mutex> g(g_mu);
+                tu = g_tuning;
+            }
+            tu.max_branch_dim = std::min(tu.max_branch_dim, S->max_d);
+            std::vector<pq_result> refused;
+            auto w = std::make_unique<SrvWave>();
+            std::vector<SrvReq> back;
+            for (auto &q : cand) {
+                if (!back.empty()) {
+                    back.push_back(q);
+                    continue;
+                }
+                pq_status st = srv_resolve(S, q);
+                if (st != PQ_OK) {
+                    refused.push_back(srv_result(q, st, srv_now(S)));
+                    continue;
+                }
+                int dmax = 0;
+                for (auto &E : q.tg->dev) dmax = std::max(dmax, E.d);
+                q.bytes = request_bytes(*q.tg, tu);
+                if (dmax > tu.max_branch_dim || q.bytes > S->budget) {
+                    refused.push_back(srv_result(q, PQ_ERR_ADMISSION_REFUSED, srv_now(S)));
+                    continue;
+                }
+                if (w->bytes + q.bytes > room) {  // wait for memory: keep FIFO order
+                    back.push_back(q);
+                    continue;
+                }
+                w->bytes += q.bytes;
+                w->reqs.push_back(q);
+            }
+            pq_status lst = PQ_OK;
+            if (!w->reqs.empty()) {
+                w->slot = slot;
+                lst = srv_launch(S, *w, tu);
+                if (lst != PQ_OK) {
+                    for (auto &q : w->reqs) refused.push_back(srv_result(q, lst, srv_now(S)));
+                    w->reqs.clear();
+                    if (w->done) cudaEventDestroy(w->done);
+                    w->plan.reset();
+                }
+            }
+            lk.lock();
+            for (auto it = back.rbegin(); it != back.rend(); ++it) S->pending.push_front(*it);
+            for (auto &r : refused) S->finished.push_back(r);
+            if (!refused.empty()) S->cv_done.notify_all();
+            if (!w->reqs.empty()) {
+                S->busy[slot] = 1;
+                S->inflight_bytes += w->bytes;
+                S->inflight.push_back(std::move(w));
+                continue;
+            }
+        }
+        // nothing launchable now: wait for a submission or poll in-flight waves again
+        S->cv_work.wait_for(lk, std::chrono::microseconds(S->inflight.empty() ? 2000 : 50));
+    }
+}
+}  // namespace pq
+
+extern "C" {
+
+PQ_API pq_status pq_server_create(int32_t nsims, pq_sim *const *sims, int32_t max_slots, int64_t mem_budget_bytes,
+                                  int32_t max_branch_dim, pq_server **out) {
+    if (nsims <= 0 || !sims || !out || max_slots <= 0 || max_slots > 65536 || mem_budget_bytes <= 0)
+        return fail(PQ_ERR_INVALID_ARG, "bad server arguments");
+    *out = nullptr;
+    auto S = std::make_unique<pq_server>();
+    for (int i = 0; i < nsims; i++) {
+        if (!sims[i] || sims[i]->host_only) return fail(PQ_ERR_INVALID_ARG, "bad simulator");
+        if (sims[i]->circ.nq > 128) return fail(PQ_ERR_INVALID_ARG, "served circuits are limited to 128 qubits");
+        S->sims.push_back(sims[i]);
+    }
+    S->max_slots = max_slots;
+    S->budget = mem_budget_bytes;
+    S->max_d = max_branch_dim > 0 ? std::min(max_branch_dim, kMaxD) : 48;
+    S->device = g_device;
+    S->t0 = now_s();
+    CU(cudaSetDevice(S->device));
+    for (int k = 0; k < kSrvStreams; k++) {
+        cudaStream_t st;
+        CU(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        S->streams.push_back(st);
+        double *hb = nullptr;
+        CU(cudaMallocHost(&hb, (size_t)max_slots * 3 * sizeof(double)));
+        S->hbuf.push_back(hb);
+        S->busy.push_back(0);
+    }
+    pq_server *raw = S.release();
+    raw->worker = std::thread(srv_loop, raw);
+    *out = raw;
+    return PQ_OK;
+}
+
+PQ_API void pq_server_destroy(pq_server *s) {
+    if (!s) return;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop = true;
+    }
+    s->cv_work.notify_all();
+    if (s->worker.joinable()) s->worker.join();
+    delete s;
+}
+
+PQ_API double pq_server_now(const pq_server *s) { return s ? srv_now(s) : 0.0; }
+
+PQ_API pq_status pq_server_submit(pq_server *s, int64_t n, const pq_request *reqs) {
+    if (!s || n < 0 || (n > 0 && !reqs)) return fail(PQ_ERR_INVALID_ARG, "bad submit arguments");
+    std::vector<SrvReq> ok;
+    std::vector<pq_result> bad;
+    const double t = srv_now(s);
+    for (int64_t i = 0; i < n; i++) {
+        SrvReq q;
+        q.r = reqs[i];
+        q.t_submit = t;
+        const pq_request &r = reqs[i];
+        bool valid = r.sim >= 0 && r.sim < (int)s->sims.size() && r.kind >= 0 && r.kind <= 2;
+        if (valid) {
+            const int nq = s->sims[r.sim]->circ.nq;
+            auto fits = [&](const uint64_t *v) {
+                for (int b = nq; b < 128; b++)
+                    if ((v[b >> 6] >> (b & 63)) & 1ull) return false;
+                return true;
+            };
+            valid = fits(r.x) && (r.kind == PQ_REQ_MARGINAL || fits(r.y));
+            if (r.kind == PQ_REQ_MARGINAL) valid = valid && r.qubit >= 0 && r.qubit < nq && (r.outcome == 0 || r.outcome == 1);
+        }
+        if (valid) ok.push_back(q);
+        else bad.push_back(srv_result(q, PQ_ERR_INVALID_ARG, t));
+    }
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        for (auto &q : ok) s->pending.push_back(q);
+        for (auto &r : bad) s->finished.push_back(r);
+    }
+    s->cv_work.notify_all();
+    if (!bad.empty()) s->cv_done.notify_all();
+    return PQ_OK;
+}
+
+PQ_API int64_t pq_server_poll(pq_server *s, pq_result *out, int64_t cap, double timeout_s) {
+    if (!s || !out || cap <= 0) return 0;
+    std::unique_lock<std::mutex> lk(s->mu);
+    if (s->finished.empty() && timeout_s > 0)
+        s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), [&] { return !s->finished.empty(); });
+    const int64_t k = std::min<int64_t>(cap, (int64_t)s->finished.size());
+    for (int64_t i = 0; i < k; i++) out[i] = s->finished[i];
+    s->finished.erase(s->finished.begin(), s->finished.begin() + k);
+    return k;
+}
+
+PQ_API pq_status pq_server_drain(pq_server *s, double timeout_s) {
+    if (!s) return fail(PQ_ERR_INVALID_ARG, "null server");
+    std::unique_lock<std::mutex> lk(s->mu);
+    bool ok = s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s),
+                                  [&] { return s->pending.empty() && s->inflight.empty(); });
+    return ok ? PQ_OK : fail(PQ_ERR_TIMEOUT, "requests still pending after the timeout");
+}
+
+}  // extern "C"

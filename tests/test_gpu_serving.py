@@ -1,0 +1,155 @@
+"""Serving loop on the GPU: mixed request kinds, continuous batching, memory admission.
+
+Each served result must equal the simulator's own answer for that request evaluated alone
+(the same work decomposition: bit-identical), whatever else shares its wave.
+"""
+import time
+
+import numpy as np
+import pytest
+
+import oracle as O
+from polyq_gb300 import Simulator
+from polyq_gb300.rng import random_outputs, workload_batch
+from polyq_gb300.serve import AMPLITUDE, MARGINAL, PROBABILITY, Server
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def pool(gpu):
+    circs = [c for c, _ in workload_batch(6, seed=11, t_max=14)]
+    return circs, [Simulator(c) for c in circs]
+
+
+def _requests(circs, count, seed):
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for i in range(count):
+        k = int(rng.integers(len(circs)))
+        n = circs[k].num_qubits
+        kind = int(rng.integers(3))
+        y = random_outputs(n, 1, int(rng.integers(1 << 30)))[0]
+        reqs.append({"sim": k, "kind": kind, "x": 0, "y": y, "qubit": int(rng.integers(n)),
+                     "outcome": int(rng.integers(2)), "tag": i})
+    return reqs
+
+
+def _expected(sims, r):
+    s = sims[r["sim"]]
+    if r["kind"] == AMPLITUDE:
+        return complex(s.amplitudes([0], [r["y"]])[0])
+    if r["kind"] == PROBABILITY:
+        a = complex(s.amplitudes([0], [r["y"]])[0])
+        return a.real * a.real + a.imag * a.imag
+    return s.marginal(0, [(r["qubit"], r["outcome"])])
+
+
+def _value(res):
+    return complex(res["re"], res["im"]) if res["kind"] == AMPLITUDE else res["re"]
+
+
+def test_mixed_requests_match_direct_evaluation(pool):
+    circs, sims = pool
+    srv = Server(sims, max_slots=32, mem_budget_bytes=1 << 28, max_branch_dim=40)
+    reqs = _requests(circs, 200, 1)
+    srv.submit(reqs)
+    got = {r["tag"]: r for r in srv.collect(len(reqs), 120)}
+    assert len(got) == len(reqs)
+    for r in reqs:
+        res = got[r["tag"]]
+        assert res["status"] == 0, res
+        want = _expected(sims, r)
+        if r["kind"] == MARGINAL:
+            assert abs(_value(res) - want) <= 1e-12
+        elif r["kind"] == PROBABILITY:  # |a|^2 formed on the host (a fused multiply-add may differ by an ulp)
+            assert abs(_value(res) - want) <= 1e-15 * abs(want)
+        else:
+            assert _value(res) == want  # same decomposition -> bit-identical
+        assert res["done_s"] >= res["submit_s"]
+    srv.close()
+
+
+def test_alone_equals_in_the_mix(pool):
+    circs, sims = pool
+    srv = Server(sims, max_slots=64, mem_budget_bytes=1 << 28)
+    probe = {"sim": 2, "kind": AMPLITUDE, "x": 0, "y": random_outputs(circs[2].num_qubits, 1, 99)[0], "tag": -1}
+    srv.submit([probe])
+    alone = srv.collect(1, 60)[0]
+    mix = _requests(circs, 150, 2)
+    srv.submit(mix[:75] + [dict(probe, tag=-2)] + mix[75:])
+    res = {r["tag"]: r for r in srv.collect(151, 120)}
+    assert _value(res[-2]) == _value(alone)
+    srv.close()
+
+
+def test_marginals_match_oracle(pool):
+    circs, sims = pool
+    srv = Server(sims, max_slots=16, mem_budget_bytes=1 << 28)
+    c = circs[0]
+    ref = O.OracleSim(c)
+    reqs = [{"sim": 0, "kind": MARGINAL, "x": 0, "qubit": q, "outcome": b, "tag": 2 * q + b}
+            for q in range(min(4, c.num_qubits)) for b in (0, 1)]
+    srv.submit(reqs)
+    res = {r["tag"]: r for r in srv.collect(len(reqs), 120)}
+    for r in reqs:
+        want = ref.marginal(0, [(r["qubit"], r["outcome"])])
+        assert abs(res[r["tag"]]["re"] - want) <= 1e-9
+    # P(q=0) + P(q=1) = 1
+    for q in range(min(4, c.num_qubits)):
+        assert abs(res[2 * q]["re"] + res[2 * q + 1]["re"] - 1.0) <= 1e-9
+    srv.close()
+
+
+def test_admission_by_dimension_cap_and_memory(pool):
+    circs, sims = pool
+    dims = [s.stats_full()["branch_dim"] for s in sims]
+    k = int(np.argmax(dims))
+    srv = Server(sims, max_slots=8, mem_budget_bytes=1 << 28, max_branch_dim=max(1, dims[k] - 1))
+    srv.submit([{"sim": k, "kind": AMPLITUDE, "x": 0, "y": 0, "tag": 1}])
+    r = srv.collect(1, 30)[0]
+    assert r["status"] == 3  # refused, not run
+    srv.close()
+    # a budget too small for any single request: refused immediately
+    srv = Server(sims, max_slots=8, mem_budget_bytes=64, max_branch_dim=40)
+    srv.submit([{"sim": 0, "kind": AMPLITUDE, "x": 0, "y": 0, "tag": 1}])
+    assert srv.collect(1, 30)[0]["status"] == 3
+    srv.close()
+    # a budget that fits only a few requests at a time: everything completes, in waves
+    one = sims[0]
+    srv = Server(sims, max_slots=64, mem_budget_bytes=20000, max_branch_dim=40)
+    reqs = [{"sim": 0, "kind": AMPLITUDE, "x": 0, "y": y, "tag": i}
+            for i, y in enumerate(random_outputs(circs[0].num_qubits, 40, 5))]
+    srv.submit(reqs)
+    res = {r["tag"]: r for r in srv.collect(40, 120)}
+    assert all(res[i]["status"] == 0 for i in range(40))
+    want = one.amplitudes([0] * 40, [r["y"] for r in reqs])
+    assert np.array_equal(np.array([_value(res[i]) for i in range(40)]), want)
+    srv.close()
+
+
+def test_invalid_requests_complete_with_status(pool):
+    circs, sims = pool
+    srv = Server(sims, max_slots=8, mem_budget_bytes=1 << 24)
+    srv.submit([{"sim": 99, "kind": 0, "tag": 1}, {"sim": 0, "kind": MARGINAL, "qubit": 999, "tag": 2},
+                {"sim": 0, "kind": AMPLITUDE, "y": 1 << 127, "tag": 3}])
+    res = {r["tag"]: r for r in srv.collect(3, 10)}
+    assert res[1]["status"] == 1 and res[2]["status"] == 1 and res[3]["status"] == 1
+    srv.drain(10)
+    srv.close()
+
+
+def test_overlapping_arrivals_are_admitted_while_waves_run(pool):
+    circs, sims = pool
+    srv = Server(sims, max_slots=4, mem_budget_bytes=1 << 28)
+    t0 = time.monotonic()
+    tags = 0
+    for burst in range(10):
+        srv.submit(_requests(circs, 8, 100 + burst))
+        tags += 8
+        time.sleep(0.001)
+    res = srv.collect(tags, 120)
+    assert len(res) == tags and all(r["status"] == 0 for r in res)
+    lat = sorted(r["done_s"] - r["submit_s"] for r in res)
+    assert lat[len(lat) // 2] < 10.0
+    srv.close()
