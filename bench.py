@@ -332,6 +332,279 @@ def run_gb300(args):
     return 0
 
 
+def _pct(xs, q):
+    xs = sorted(xs)
+    if not xs:
+        return None
+    return xs[min(len(xs) - 1, int(q * (len(xs) - 1) + 0.5))]
+
+
+def _gpu_setup():
+    import polyq_gb300 as pq
+    from polyq_gb300 import _native as N
+    N.check(N.lib().pq_init(0))
+    return pq, N
+
+
+def run_batched(args):
+    """Uneven batch: 256 circuits (n ~ U[16,64], 40n gates, T ~ U[8,36]), 64 uniform y each,
+    one persistent graph launch per step vs the plain per-circuit and per-boundary paths."""
+    import ctypes as ct
+
+    import numpy as np
+    import torch
+
+    pq, N = _gpu_setup()
+    from polyq_gb300.rng import random_outputs, workload_batch
+    t0 = time.perf_counter()
+    circs = workload_batch(256, seed=3)
+    sims = [pq.Simulator(c) for c, _ in circs]
+    build_s = time.perf_counter() - t0
+    outs = [random_outputs(c.num_qubits, 64, 1000 + i) for i, (c, _) in enumerate(circs)]
+    b = pq.Batch(sims, [64] * len(sims))
+    xs, ys = b.pack([[0] * 64] * len(sims), outs)
+    n = 64 * len(sims)
+    dx = torch.from_numpy(xs.view(np.int64)).cuda()
+    dy = torch.from_numpy(ys.view(np.int64)).cuda()
+    dout = torch.zeros(2 * n, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.Stream()
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            b.run_device(ct.c_void_p(dx.data_ptr()), ct.c_void_p(dy.data_ptr()), ct.c_void_p(dout.data_ptr()),
+                         None, ct.c_void_p(stream.cuda_stream))
+        ms = []
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            b.run_device(ct.c_void_p(dx.data_ptr()), ct.c_void_p(dy.data_ptr()), ct.c_void_p(dout.data_ptr()),
+                         None, ct.c_void_p(stream.cuda_stream))
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+    batched_ms = sum(ms) / len(ms)
+    got = dout.cpu().numpy().view(np.complex128)
+    # plain path 1: one launch per circuit (its 64 boundaries), host buffers, sequential
+    for s, o in zip(sims, outs):
+        s.amplitudes([0] * 64, o)  # plans and graphs built outside the timing
+    per_circ = []
+    same = True
+    t0 = time.perf_counter()
+    for i, (s, o) in enumerate(zip(sims, outs)):
+        t1 = time.perf_counter()
+        a = s.amplitudes([0] * 64, o)
+        per_circ.append(time.perf_counter() - t1)
+        same = same and np.array_equal(a, got[64 * i:64 * i + 64])
+    plain_circ_s = time.perf_counter() - t0
+    # plain path 2: one launch per (circuit, boundary)
+    for s, o in zip(sims, outs):
+        s.amplitudes_plain([0], o[:1])
+    t0 = time.perf_counter()
+    for s, o in zip(sims, outs):
+        s.amplitudes_plain([0] * 64, o)
+    plain_bnd_s = time.perf_counter() - t0
+    buckets = {}
+    for s, t in zip(sims, per_circ):
+        d = s.stats_full()["branch_dim"]
+        key = "d<=12" if d <= 12 else ("d13-18" if d <= 18 else "d>=19")
+        bk = buckets.setdefault(key, [0, 0.0])
+        bk[0] += 64
+        bk[1] += t
+    line = {"metric": METRIC, "workload": "batched", "value": n / (batched_ms * 1e-3), "unit": "amplitudes/s",
+            "branches_per_s": b.branches / (batched_ms * 1e-3), "ms_per_step": batched_ms, "steps": args.steps,
+            "warmup": args.warmup, "n_gpus": 1, "higher_is_better": True, "data": "synthetic",
+            "plain_per_circuit_amps_per_s": n / plain_circ_s, "plain_per_boundary_amps_per_s": n / plain_bnd_s,
+            "speedup_vs_plain_per_circuit": plain_circ_s / (batched_ms * 1e-3),
+            "speedup_vs_plain_per_boundary": plain_bnd_s / (batched_ms * 1e-3),
+            "batched_equals_per_circuit_bitwise": bool(same),
+            "per_d_bucket_amps_per_s_plain": {k: v[0] / v[1] for k, v in buckets.items()},
+            "config": {"workload": "256 circuits, n~U[16,64], 40n gates, T~U[8,36] (seed 3), 64 uniform y each, "
+                                   "strategy auto", "branches_per_step": b.branches, "host_build_s": build_s,
+                       "l2": "flushed between steps"}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_serve(args):
+    """Poisson stream of amplitude / probability / single-qubit-marginal requests against 64
+    resident circuits (n~U[16,64], 40n gates, T~U[8,40]); throughput and p50/p99 latency at the
+    offered load and below saturation, beside plain per-request launches."""
+    import random
+
+    import numpy as np
+
+    pq, N = _gpu_setup()
+    from polyq_gb300.rng import random_outputs, workload_batch
+    from polyq_gb300.serve import AMPLITUDE, MARGINAL, Server
+    circs = [c for c, _ in workload_batch(64, seed=5, t_max=40)]
+    sims = [pq.Simulator(c) for c in circs]
+    srv = Server(sims, max_slots=args.slots, mem_budget_bytes=8 << 30, max_branch_dim=args.max_d)
+    rng = random.Random(7)
+    marg_qubits = 4  # marginal requests measure one of the first 4 qubits (engines built in warm-up)
+    warm = [{"sim": k, "kind": MARGINAL, "x": 0, "qubit": q, "outcome": 0, "tag": -1}
+            for k in range(len(sims)) for q in range(min(marg_qubits, circs[k].num_qubits))]
+    srv.submit(warm)
+    srv.collect(len(warm), 600)
+
+    def make(i):
+        k = rng.randrange(len(sims))
+        kind = rng.randrange(3)
+        n = circs[k].num_qubits
+        return {"sim": k, "kind": kind, "x": 0, "y": random_outputs(n, 1, rng.randrange(1 << 30))[0],
+                "qubit": rng.randrange(min(marg_qubits, n)), "outcome": rng.randrange(2), "tag": i}
+
+    def load(rate, duration):
+        nreq = int(rate * duration)
+        arrivals = []
+        t = 0.0
+        for _ in range(nreq):
+            t += rng.expovariate(rate)
+            arrivals.append(t)
+        reqs = [make(i) for i in range(nreq)]
+        start = time.monotonic()
+        i = 0
+        while i < nreq:
+            now = time.monotonic() - start
+            j = i
+            while j < nreq and arrivals[j] <= now:
+                j += 1
+            if j > i:
+                srv.submit(reqs[i:j])
+                i = j
+            else:
+                time.sleep(max(0.0, min(0.0005, arrivals[i] - now)))
+        res = srv.collect(nreq, 600)
+        ok = [r for r in res if r["status"] == 0]
+        lat = [r["done_s"] - r["submit_s"] for r in ok]
+        span = (max(r["done_s"] for r in ok) - min(r["submit_s"] for r in ok)) if ok else 0.0
+        return {"offered_per_s": rate, "requests": nreq, "completed": len(ok),
+                "refused": sum(1 for r in res if r["status"] == 3), "other_errors": sum(1 for r in res if r["status"] not in (0, 3)),
+                "throughput_per_s": len(ok) / span if span > 0 else None,
+                "p50_ms": 1e3 * _pct(lat, 0.5) if lat else None, "p99_ms": 1e3 * _pct(lat, 0.99) if lat else None}
+
+    full = load(args.rate, args.duration)
+    cap = full["throughput_per_s"] or args.rate
+    sub = load(0.3 * min(cap, args.rate), args.duration)
+    # plain per-request launches (one synchronous call per request, no batching)
+    reqs = [make(10 ** 6 + i) for i in range(300)]
+    for r in reqs[:20]:
+        s = sims[r["sim"]]
+        if r["kind"] == MARGINAL:
+            s.marginal(0, [(r["qubit"], r["outcome"])])
+        else:
+            s.amplitudes([0], [r["y"]])
+    lat = []
+    t0 = time.perf_counter()
+    for r in reqs:
+        t1 = time.perf_counter()
+        s = sims[r["sim"]]
+        try:
+            if r["kind"] == MARGINAL:
+                s.marginal(0, [(r["qubit"], r["outcome"])])
+            else:
+                s.amplitudes([0], [r["y"]])
+        except N.PqError:
+            continue
+        lat.append(time.perf_counter() - t1)
+    plain = {"requests": len(reqs), "completed": len(lat), "throughput_per_s": len(lat) / (time.perf_counter() - t0),
+             "p50_ms": 1e3 * _pct(lat, 0.5), "p99_ms": 1e3 * _pct(lat, 0.99)}
+    srv.close()
+    line = {"metric": METRIC, "workload": "serve", "value": full["throughput_per_s"], "unit": "requests/s",
+            "at_offered_load": full, "sub_saturation": sub, "plain_per_request": plain, "n_gpus": 1,
+            "data": "synthetic",
+            "config": {"workload": "64 resident circuits n~U[16,64], 40n gates, T~U[8,40] (seed 5); Poisson arrivals; "
+                                   "amplitude/probability/marginal 1:1:1; marginals on one of the first 4 qubits",
+                       "max_slots": args.slots, "max_branch_dim": args.max_d, "duration_s": args.duration}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_small(args):
+    """One amplitude <0|C|0> and its probability: n=20, 200 gates, 16 T (seed 1)."""
+    import numpy as np
+
+    pq, N = _gpu_setup()
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    from polyq_gb300.rng import workload_small
+    c = workload_small(1)
+    t0 = time.perf_counter()
+    sim = pq.Simulator(c)
+    build = time.perf_counter() - t0
+    for _ in range(20):
+        sim.amplitudes([0], [0])
+    lat, plat = [], []
+    for _ in range(200):
+        t1 = time.perf_counter()
+        a = sim.amplitudes([0], [0])[0]
+        lat.append(time.perf_counter() - t1)
+        t1 = time.perf_counter()
+        p = sim.probability(0, 0)
+        plat.append(time.perf_counter() - t1)
+    ref = oracle.OracleSim(c).amplitude(0, 0)
+    dense = oracle.dense_statevector(c, 0)[0]
+    line = {"metric": METRIC, "workload": "small", "value": 1.0 / _pct(lat, 0.5), "unit": "amplitudes/s (serial)",
+            "amplitude": [a.real, a.imag], "probability": p, "p50_ms": 1e3 * _pct(lat, 0.5),
+            "p99_ms": 1e3 * _pct(lat, 0.99), "probability_p50_ms": 1e3 * _pct(plat, 0.5),
+            "abs_err_vs_fp64_oracle": abs(a - ref), "abs_err_vs_dense": abs(a - dense),
+            "prob_abs_err_vs_dense": abs(p - abs(dense) ** 2), "build_s": build, "stats": sim.stats_full(),
+            "config": {"workload": "n=20, 200 gates, 16 T (seed 1), <0|C|0>"}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_rotations(args):
+    """Arbitrary angles: rz(theta) slots plus CCZ layers, FP32-compensated vs device FP64 per
+    amplitude; a 20-qubit variant also against the dense statevector."""
+    import numpy as np
+
+    pq, N = _gpu_setup()
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    from polyq_gb300.rng import random_outputs, workload_rotations
+    res = {}
+    # scaled variant: n=40, 1500 gates, 24 rz; CCZ per layer reduced until the branch sum fits 2^30
+    chosen = None
+    for per_layer in (8, 4, 3, 2, 1):
+        c = workload_rotations(n=40, ngates=1500, n_rz=24, ccz_layers=4, ccz_per_layer=per_layer, seed=4)
+        st = pq.Simulator(c, host_only=True).stats_full()
+        res["n40_ccz_per_layer_%d_branches_per_amp" % per_layer] = st["branches_per_amplitude"]
+        if st["branches_per_amplitude"] <= (1 << 30) and chosen is None:
+            chosen = (per_layer, c)
+    per_layer, c = chosen
+    sim = pq.Simulator(c)
+    nb = args.boundaries if args.boundaries != 4096 else 256  # 3.9e10 branches per amplitude at this size
+    ys = random_outputs(40, nb, 4)
+    sim.amplitudes([0] * 2, ys[:2])
+    t0 = time.perf_counter()
+    got, err = sim.amplitudes([0] * nb, ys, with_error=True)
+    t32 = time.perf_counter() - t0
+    ref = sim.amplitudes_fp64([0] * nb, ys)
+    rel = np.abs(got - ref) / np.abs(ref)
+    res["n40"] = {"ccz_per_layer": per_layer, "stats": sim.stats_full(), "seconds_fp32_path": t32,
+                  "max_rel_err_vs_fp64": float(np.max(rel)), "median_rel_err": float(np.median(rel)),
+                  "within_1e-6": float(np.mean(rel <= 1e-6)), "max_bound_over_abs": float(np.max(err / np.abs(ref)))}
+    # dense-checkable variant
+    c20 = workload_rotations(n=20, ngates=600, n_rz=12, ccz_layers=2, ccz_per_layer=2, seed=4)
+    s20 = pq.Simulator(c20)
+    sv = oracle.dense_statevector(c20, 0)
+    idx = [int(i) for i in np.argsort(-np.abs(sv))[:1024]]
+    g20 = s20.amplitudes([0] * len(idx), idx)
+    rel20 = np.abs(g20 - sv[idx]) / np.abs(sv[idx])
+    res["n20_dense"] = {"stats": s20.stats_full(), "max_rel_err_vs_dense": float(np.max(rel20)),
+                        "median_rel_err_vs_dense": float(np.median(rel20)),
+                        "prob_max_abs_err": float(np.max(np.abs(s20.probabilities([0] * len(idx), idx) -
+                                                                np.abs(sv[idx]) ** 2)))}
+    line = {"metric": METRIC, "workload": "rotations", "value": nb / t32, "unit": "amplitudes/s", "data": "synthetic",
+            "branches_per_s": nb * res["n40"]["stats"]["branches_per_amplitude"] / t32,
+            "results": res, "config": {"workload": "n=40, 1500 gates, 24 rz(theta) theta~U[0,2pi) + 4 CCZ layers "
+                                                   "(per-layer count reduced until <= 2^30 branches per amplitude); "
+                                                   "%d uniform y; n=20 variant vs dense" % nb}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -342,12 +615,26 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=24)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--boundaries", type=int, default=4096, help="boundary count (profiling of smaller cases)")
+    ap.add_argument("--workload", default="many_boundaries",
+                    choices=["many_boundaries", "batched", "serve", "small", "rotations"])
+    ap.add_argument("--rate", type=float, default=5000.0, help="serve: offered requests/s")
+    ap.add_argument("--duration", type=float, default=2.0, help="serve: seconds of arrivals")
+    ap.add_argument("--slots", type=int, default=256, help="serve: requests per wave")
+    ap.add_argument("--max-d", type=int, default=32, help="serve: branch-dimension cap")
     args = ap.parse_args()
     WORKLOAD["boundaries"] = args.boundaries
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batched":
+        return run_batched(args)
+    if args.workload == "serve":
+        return run_serve(args)
+    if args.workload == "small":
+        return run_small(args)
+    if args.workload == "rotations":
+        return run_rotations(args)
     return run_gb300(args)
 
 

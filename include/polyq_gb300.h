@@ -65,7 +65,7 @@ typedef struct pq_stats {
     int64_t free_vars, planes, lines, radical, terms, branch_dim;
     int64_t pairs;          /* decomposed T-pairs p */
     int64_t num_branches;   /* 2^p branch engines */
-    int64_t branches_per_amplitude; /* sum over branch engines of 2^d */
+    double branches_per_amplitude;  /* sum over branch engines of 2^d */
     int64_t device_bytes;   /* HBM held by the simulator's resident structures */
     double build_seconds;   /* host compile + elimination + upload time */
 } pq_stats;
@@ -108,9 +108,9 @@ PQ_API pq_status pq_probabilities(pq_sim *sim, int64_t n, const uint64_t *x, con
  * pairs.  The sandwich engine of each distinct measured-qubit set is built once and cached. */
 PQ_API pq_status pq_marginal(pq_sim *sim, const uint64_t *x, int32_t nmeas, const int32_t *qubits,
                              const uint8_t *outcomes, double *out);
-/* Device-resident variant of pq_amplitudes: x, y, out, errbound are device pointers and the
- * work is enqueued on `stream` (cudaStream_t, NULL = the simulator's stream) without a host
- * synchronisation. */
+/* Device-resident variant of pq_amplitudes: x, y, out, errbound are device pointers; the work
+ * is ordered after, and waited for by, `stream` (cudaStream_t; NULL = the legacy default
+ * stream) without a host synchronisation. */
 PQ_API pq_status pq_amplitudes_device(pq_sim *sim, int64_t n, const uint64_t *x, const uint64_t *y, double *out,
                                       double *errbound, void *stream);
 /* Same evaluation split into one launch sequence per boundary (the plain one-circuit,

@@ -648,7 +648,7 @@ PQ_API pq_status pq_sim_stats(const pq_sim *s, pq_stats *o) {
     o->branch_dim = e.d;
     o->pairs = s->main.rs.pairs;
     o->num_branches = (int64_t)s->main.rs.branches.size();
-    o->branches_per_amplitude = (int64_t)s->main.branches_per_amp;
+    o->branches_per_amplitude = s->main.branches_per_amp;
     o->device_bytes = s->main.bytes;
     o->build_seconds = s->build_s;
     return PQ_OK;

@@ -34,7 +34,7 @@ class CircuitDesc(ct.Structure):
 class Stats(ct.Structure):
     _fields_ = [("free_vars", ct.c_int64), ("planes", ct.c_int64), ("lines", ct.c_int64), ("radical", ct.c_int64),
                 ("terms", ct.c_int64), ("branch_dim", ct.c_int64), ("pairs", ct.c_int64),
-                ("num_branches", ct.c_int64), ("branches_per_amplitude", ct.c_int64),
+                ("num_branches", ct.c_int64), ("branches_per_amplitude", ct.c_double),
                 ("device_bytes", ct.c_int64), ("build_seconds", ct.c_double)]
 
 
