@@ -164,6 +164,9 @@ typedef struct pq_result {
     double errbound;
     double submit_s, done_s;  /* seconds on the server's monotonic clock */
 } pq_result;
+/* max_slots: requests per launched wave; mem_budget_bytes: device memory the in-flight waves
+ * may hold; max_branch_dim: a request whose work -- branches summed over its branch engines --
+ * exceeds 2^max_branch_dim is refused (PQ_ERR_ADMISSION_REFUSED) rather than run. */
 PQ_API pq_status pq_server_create(int32_t nsims, pq_sim *const *sims, int32_t max_slots, int64_t mem_budget_bytes,
                                   int32_t max_branch_dim, pq_server **out);
 PQ_API void pq_server_destroy(pq_server *s);

@@ -48,6 +48,8 @@ struct EngineDev {
     int DI, nsl_tp, nsl_th;
     int joint;               // 1: weights from the joint hi/lo table; 0: FP64 product path
     double sum_abs_bound;
+    double grid;             // hi parts of wtab are integer multiples of this power of two
+    double errfac;           // bound on a job's FP32 lo-sum error (before the 2^{(mag2-h)/2} scale)
     const uint64_t *o1, *o3, *wa, *wb, *wem;  // diagonal masks
     const uint64_t *ucols;   // nf x W   boundary columns  [a|b|o|e]
     const uint64_t *mcols;   // t  x W   term columns      [a|b|o|e]

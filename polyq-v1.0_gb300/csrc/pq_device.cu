@@ -268,12 +268,16 @@ static pq_status build_plan(const std::vector<Segment> &segs, int nw, cudaStream
     P.nout = (int)req;
     P.smem_words = maxw;
     if (P.njobs == 0) return fail(PQ_ERR_INVALID_ARG, "empty launch");
-    // item layout: jobs in decreasing branch dimension (longest work first)
+    // item layout: jobs in decreasing branch dimension (longest work first); equal dimensions
+    // grouped by engine, so warps running at the same time share that engine's tables in L1
     std::vector<int> perm((size_t)P.njobs), kinv((size_t)P.njobs), jdl((size_t)P.njobs);
     std::vector<unsigned> jcpi((size_t)P.njobs);
     std::vector<unsigned long long> jnch((size_t)P.njobs);
     for (int j = 0; j < P.njobs; j++) perm[j] = j;
-    std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) { return jd[a] > jd[b]; });
+    std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) {
+        if (jd[a] != jd[b]) return jd[a] > jd[b];
+        return jobs[a].engine < jobs[b].engine;
+    });
     std::vector<long long> istart((size_t)P.njobs + 1, 0);
     P.branches = 0.0;
     for (int k = 0; k < P.njobs; k++) {
@@ -1159,8 +1163,8 @@ extern "C" PQ_API pq_status pq_amplitudes_noalloc(pq_sim *s, int64_t n, const ui
 // then keeps admitting: requests that arrive while earlier waves run go into the next wave on
 // another stream, so their work overlaps on the device.  Finished waves are retired in
 // completion order; every result carries its submit and completion time.  A request whose
-// branch engines exceed the dimension cap, or whose own launch would not fit the budget, is
-// completed at once with PQ_ERR_ADMISSION_REFUSED.  Each boundary's result is the same as
+// work (branches over its branch engines) exceeds 2^cap, or whose own launch would not fit the
+// budget, is completed at once with PQ_ERR_ADMISSION_REFUSED.  Each boundary's result is the same as
 // when evaluated alone: a job's work decomposition does not depend on the rest of the wave.
 // ========================================================================================
 namespace pq {
@@ -1362,10 +1366,9 @@ static void srv_loop(pq_server *S) {
                     refused.push_back(srv_result(q, st, srv_now(S)));
                     continue;
                 }
-                int dmax = 0;
-                for (auto &E : q.tg->dev) dmax = std::max(dmax, E.d);
+                // work of the request: branches over all of its branch engines
                 q.bytes = request_bytes(*q.tg, tu);
-                if (dmax > tu.max_branch_dim || q.bytes > S->budget) {
+                if (q.tg->branches_per_amp > std::ldexp(1.0, S->max_d) || q.bytes > S->budget) {
                     refused.push_back(srv_result(q, PQ_ERR_ADMISSION_REFUSED, srv_now(S)));
                     continue;
                 }

@@ -692,13 +692,37 @@ PackedEngine pack_engine(const HostEngine& e, const EngineTables& T) {
     d.tlo64 = as_off<double2>(k.vec(T.tlo));
     d.tp64 = as_off<double2>(k.vec(T.tp));
     d.joint = T.joint ? 1 : 0;
-    std::vector<float> w32;  // hi.re, hi.im, lo.re, lo.im with hi + lo = the FP64 weight
+    // hi.re, hi.im, lo.re, lo.im with hi + lo = the FP64 weight.  hi lies on the grid g, a power
+    // of two with 2^DI * max|w| <= 2^23 g: any sum of at most 2^DI hi parts (a chunk) is then an
+    // integer multiple of g below 2^24 g, i.e. exact in FP32; lo = w - hi (|lo| <= g/2) carries
+    // the rest and is summed in plain FP32.
+    double wmax = 0.0;
+    for (const auto& c : T.w) wmax = std::max(wmax, std::max(std::fabs(c.re), std::fabs(c.im)));
+    double grid = 0.0;
+    if (wmax > 0.0) grid = std::ldexp(1.0, (int)std::ceil(std::log2(std::ldexp(wmax, T.DI) / 8388608.0)));
+    d.grid = grid;
+    // Error of one job's chunk sums from the lo parts: per chunk of N <= 2^DI branches the four
+    // lo accumulators err by <= N (g/2)(gamma_N + u) each (summation and the FP32 rounding of lo);
+    // chunks are scaled by the FP64 weight of the coordinates >= DI, whose absolute sum over
+    // chunks is prod_{j >= DI} (|a_j0| + |a_j1|).
+    {
+        const double u = 5.9604644775390625e-08, n = std::ldexp(1.0, T.DI);
+        const double gam = n * u / (1.0 - n * u);
+        double hi_abs = 1.0;
+        for (int j = T.DI; j < e.d; j++) {
+            int kk = e.free_col[j];
+            hi_abs *= std::hypot(e.alpha[kk].re, e.alpha[kk].im) + std::hypot(e.beta[kk].re, e.beta[kk].im);
+        }
+        d.errfac = 4.0 * n * (grid / 2.0) * (gam + u) * hi_abs;
+    }
+    std::vector<float> w32;
     for (const auto& c : T.w) {
-        float hr = (float)c.re, hi = (float)c.im;
-        w32.push_back(hr);
-        w32.push_back(hi);
-        w32.push_back((float)(c.re - (double)hr));
-        w32.push_back((float)(c.im - (double)hi));
+        const double hr = grid > 0.0 ? std::nearbyint(c.re / grid) * grid : 0.0;
+        const double hi = grid > 0.0 ? std::nearbyint(c.im / grid) * grid : 0.0;
+        w32.push_back((float)hr);
+        w32.push_back((float)hi);
+        w32.push_back((float)(c.re - hr));
+        w32.push_back((float)(c.im - hi));
     }
     d.wtab = as_off<float4>(k.vec(w32));
     P.blob.swap(k.blob);

@@ -136,6 +136,71 @@ __global__ void __launch_bounds__(128) prepare_kernel(KArgs a) {
 }
 
 // ------------------------------------------------------------------------------ enumerate
+// Gray walk over the 2^dl inner coordinates of one chunk (dl >= 3), unrolled by 8: inside a
+// group of 8 steps coordinates 0 and 1 flip at fixed positions with fixed directions
+// (0+, 1+, 0-, 0+, 1-, 0-), coordinate 2 flips once with the group's direction and the group
+// boundary flips coordinate 3 + ctz(g+1).
+//   m     Z4 index (k8 - k0)/2 of the current branch, kept modulo 4 by masking at use
+//   sidx  (pivot bits << DI) | low DI coordinates: the weight-table index
+//   P     bit j = parity(G_j & s) for the inner coordinates j < dl
+// A step on coordinate j adds +-Lp_j + 2 P_j to m, xors the inner part of G_j into P and
+// T_j = (1 << j) | (R_j << DI) into sidx.  The branch value i^m * w accumulates as
+// S = A + iB with A += cos(m pi/2) w, B += sin(m pi/2) w (coefficients 0/+-1: the hi sums are
+// exact multiples of the table grid; lo sums in plain FP32).
+template <int MODE>
+__device__ __forceinline__ void gray_chunk8(const float4 *__restrict__ W, const float2 *cs, uint32_t &m,
+                                            uint32_t &sidx, uint32_t &P, const uint32_t *Gi, const uint32_t *Tg,
+                                            const uint8_t *Lp, const uint8_t *Lm, int dl, float (&acc)[8],
+                                            uint8_t *dbg, uint64_t sbase, uint32_t k0) {
+    const uint32_t G0 = Gi[0], G1 = Gi[1], G2 = Gi[2];
+    const uint32_t T0 = Tg[0], T1 = Tg[1], T2 = Tg[2];
+    const uint32_t L0p = Lp[0], L0m = Lm[0], L1p = Lp[1], L1m = Lm[1], L2p = Lp[2], L2m = Lm[2];
+    const uint32_t inner = (1u << dl) - 1u;
+    const uint32_t ngroups = 1u << (dl - 3);
+#define PQ_EVAL()                                                                   \
+    {                                                                               \
+        if (MODE == 2) dbg[sbase | (sidx & inner)] = (uint8_t)((k0 + 2u * m) & 7u); \
+        const float2 c = cs[m & 3u];                                                \
+        const float4 w = __ldg(&W[sidx]);                                           \
+        acc[0] = fmaf(c.x, w.x, acc[0]);                                            \
+        acc[1] = fmaf(c.x, w.y, acc[1]);                                            \
+        acc[2] = fmaf(c.y, w.x, acc[2]);                                            \
+        acc[3] = fmaf(c.y, w.y, acc[3]);                                            \
+        acc[4] = fmaf(c.x, w.z, acc[4]);                                            \
+        acc[5] = fmaf(c.x, w.w, acc[5]);                                            \
+        acc[6] = fmaf(c.y, w.z, acc[6]);                                            \
+        acc[7] = fmaf(c.y, w.w, acc[7]);                                            \
+    }
+#define PQ_STEP(j, L, Gj, Tj)                \
+    {                                        \
+        m += (L) + (((P >> (j)) & 1u) << 1); \
+        P ^= (Gj);                           \
+        sidx ^= (Tj);                        \
+    }
+    for (uint32_t g = 0;; ++g) {
+        PQ_EVAL();
+        PQ_STEP(0, L0p, G0, T0);
+        PQ_EVAL();
+        PQ_STEP(1, L1p, G1, T1);
+        PQ_EVAL();
+        PQ_STEP(0, L0m, G0, T0);
+        PQ_EVAL();
+        PQ_STEP(2, ((sidx >> 2) & 1u) ? L2m : L2p, G2, T2);
+        PQ_EVAL();
+        PQ_STEP(0, L0p, G0, T0);
+        PQ_EVAL();
+        PQ_STEP(1, L1m, G1, T1);
+        PQ_EVAL();
+        PQ_STEP(0, L0m, G0, T0);
+        PQ_EVAL();
+        if (g + 1 == ngroups) break;
+        const int j = 3 + ctz32(g + 1);
+        PQ_STEP(j, ((sidx >> j) & 1u) ? (uint32_t)Lm[j] : (uint32_t)Lp[j], Gi[j], Tg[j]);
+    }
+#undef PQ_EVAL
+#undef PQ_STEP
+}
+
 // MODE 0: FP32 weights, compensated accumulation.  MODE 1: FP64 weights and accumulation.
 // MODE 2: record the Z8 index of every branch into dbg (single-job debug launches).
 template <int MODE>
@@ -144,11 +209,21 @@ __global__ void __launch_bounds__(256) enum_kernel(KArgs a) {
     __shared__ uint64_t sR[8][64];
     __shared__ uint8_t sLp[8][64];
     __shared__ uint8_t sLm[8][64];
+    __shared__ uint32_t sGi[8][32];  // G_j restricted to the inner coordinates (< dl)
+    __shared__ uint32_t sTg[8][32];  // (1 << j) | (R_j << DI)
+    __shared__ float2 sCS[4];        // (cos, sin)(m pi/2)
+    if (threadIdx.x < 4) {
+        const float cv[4] = {1.f, 0.f, -1.f, 0.f}, sv[4] = {0.f, 1.f, 0.f, -1.f};
+        sCS[threadIdx.x] = make_float2(cv[threadIdx.x], sv[threadIdx.x]);
+    }
+    __syncthreads();
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     uint64_t *G = sG[wib];
     uint64_t *R = sR[wib];
     uint8_t *Lp = sLp[wib];
     uint8_t *Lm = sLm[wib];
+    uint32_t *Gi = sGi[wib];
+    uint32_t *Tg = sTg[wib];
     int cur_k = -1;  // position (item order) of the job whose data is staged
     long long kbeg = 0, kend = 0;
     while (true) {
@@ -169,11 +244,16 @@ __global__ void __launch_bounds__(256) enum_kernel(KArgs a) {
             const JobDev &J = a.jobs[jb];
             const EngineDev &E = a.engines[J.engine];
             __syncwarp();
+            const int dlj = a.jdl[jb];
             for (int j = lane; j < E.d; j += 32) {
                 G[j] = E.G[j];
                 R[j] = E.R[j];
                 Lp[j] = J.Lp[j];
                 Lm[j] = (uint8_t)((4u - J.Lp[j]) & 3u);
+                if (j < dlj) {
+                    Gi[j] = (uint32_t)(E.G[j] & ((1ull << dlj) - 1ull));
+                    Tg[j] = (1u << j) | ((uint32_t)E.R[j] << E.DI);
+                }
             }
             __syncwarp();
         }
@@ -217,8 +297,19 @@ __global__ void __launch_bounds__(256) enum_kernel(KArgs a) {
                     }
                     accx += sx * chi.x - sy * chi.y;
                     accy += sx * chi.y + sy * chi.x;
+                } else if (dl >= 3) {
+                    // FP32, unrolled Gray walk with exact hi sums (gray_chunk8)
+                    float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+                    uint32_t sidx = (uint32_t)((yy << E.DI) | (s & lomask));
+                    uint32_t P = 0;
+                    for (int j = 0; j < dl; j++) P |= (uint32_t)(popc64(G[j] & s) & 1) << j;
+                    gray_chunk8<MODE>(E.wtab, sCS, m, sidx, P, Gi, Tg, Lp, Lm, dl, acc, a.dbg, s, J.k0);
+                    const double vx = ((double)acc[0] + (double)acc[4]) - ((double)acc[3] + (double)acc[7]);
+                    const double vy = ((double)acc[1] + (double)acc[5]) + ((double)acc[2] + (double)acc[6]);
+                    accx += vx * chi.x - vy * chi.y;
+                    accy += vx * chi.y + vy * chi.x;
                 } else {
-                    // FP32: hi parts with TwoSum, lo parts plain (their error is u * u|c|)
+                    // FP32 for chunks of fewer than 8 steps: hi parts with TwoSum, lo parts plain
                     float ax = 0.f, ay = 0.f, cx = 0.f, cy = 0.f, lx = 0.f, ly = 0.f;
                     const float4 *__restrict__ W = E.wtab;
                     const int DI = E.DI;
@@ -295,6 +386,7 @@ __global__ void job_reduce_kernel(KArgs a) {
             rel = (n + 2.0 * E.nsl_tp + 8.0 + (double)E.nsl_th) * 2.0 * u64;
         }
         eb = rel * E.sum_abs_bound * mag;
+        if (E.joint) eb += E.errfac * mag;  // lo-part sums of the unrolled walk (exact hi sums)
     }
     a.job_vals[j] = v;
     a.job_err[j] = eb;

@@ -194,7 +194,7 @@ def test_many_boundaries_full_fp32_vs_device_fp64(gpu):
     assert np.all(diff <= err + 1e-300)
     rel = diff / np.abs(ref)
     assert np.max(rel) <= REL
-    assert np.median(rel) < 1e-10
+    assert np.median(rel) < 1e-8
 
 
 def test_batch_equals_individual_and_plain(gpu):
