@@ -125,35 +125,31 @@ def cpu_threads():
 
 
 def cpu_rate(circ, ys, sample, threads):
-    """CPU restatement of the reference engine on `sample` boundaries (branches/s)."""
+    """CPU restatement of the reference engine on `sample` boundaries: (branches enumerated,
+    seconds).  Branches of (boundary, branch engine) pairs whose sum vanishes are not counted:
+    neither implementation enumerates them."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle
     sim = oracle.OracleSim(circ, "auto")
-    st = sim.stats()
-    per_amp = None
     sub = ys[:sample]
     sim.amplitudes([0], sub[:1], nthreads=threads)  # warm caches
     t0 = time.perf_counter()
     sim.amplitudes([0] * len(sub), sub, nthreads=threads)
     dt = time.perf_counter() - t0
-    return sim, st, dt
+    return sim.last_branches(), dt
 
 
-def branches_per_amp_and_ops(sim):
-    """Sum over branch engines of 2^d and of 2^d * (5 W_o + 6 W_g) reference-form int64 ops,
-    plus the popc64 / logic64 split (src/normal_form.rs:479-493, src/engine.rs:700-718)."""
-    st = sim.stats_full()
-    br = ops = popc = logic = 0.0
-    for b in range(st["num_branches"]):
-        h = sim.engine_dump(b)[:8]
-        g, nodd, d = int(h[1]), int(h[2]), int(h[5])
-        wo, wg = (nodd + 63) // 64, (g + 63) // 64
-        n = float(1 << d)
-        br += n
-        ops += n * (5 * wo + 6 * wg)
-        popc += n * (2 * wo + wg)
-        logic += n * (3 * wo + 5 * wg)
-    return br, ops, popc, logic
+def enumerated(L, N, sim, n):
+    """Work of the last size-n launch: branches enumerated, reference-form int64 ops
+    (5 W_o + 6 W_g per branch: src/normal_form.rs:479-493, src/engine.rs:700-718) and their
+    popcount / logic split, plus the branches of each boundary."""
+    import ctypes as ct
+
+    import numpy as np
+    out = (ct.c_double * 4)()
+    per = np.zeros(n, dtype=np.float64)
+    N.check(L.pq_sim_enumerated(sim.handle, n, out, per.ctypes.data_as(ct.POINTER(ct.c_double))))
+    return out[0], out[1], out[2], out[3], per
 
 
 def run_reference(args):
@@ -166,23 +162,17 @@ def run_reference(args):
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle
     sim = oracle.OracleSim(circ, "auto")
-    st = sim.stats()
-    bpa = None
-    # branches per amplitude from the oracle's own engines
-    bpa = 0
-    for b in range(st["branches"]):
-        h = sim.engine_dump(b)[:8]
-        bpa += 1 << int(h[5])
     for w in range(args.warmup):
         sim.amplitudes([0] * 2, ys[:2], nthreads=threads)
-    times = []
+    times, branches = [], 0.0
     for k in range(args.steps):
         sub = ys[(k * sample) % len(ys):][:sample]
         t0 = time.perf_counter()
         sim.amplitudes([0] * len(sub), sub, nthreads=threads)
         times.append(time.perf_counter() - t0)
+        branches += sim.last_branches()  # enumerated: vanishing (boundary, engine) pairs excluded
     ms = 1e3 * sum(times) / len(times)
-    value = sample * bpa / (ms * 1e-3)
+    value = branches / sum(times)
     line = {"metric": METRIC, "impl": "reference", "value": value, "unit": "branches/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u64+f64", "data": "synthetic",
@@ -212,8 +202,13 @@ def run_gb300(args):
     n = len(ys)
     sim = pq.Simulator(circ, "auto")
     stats = sim.stats_full()
-    bpa, ops_amp, popc_amp, logic_amp = branches_per_amp_and_ops(sim)
-    branches_step = bpa * n
+    tune_s = time.perf_counter()
+    if args.no_autotune:
+        tuning = sim.tuning()
+    else:
+        # launch shape chosen by the library's autotuner on this workload (outside the timed region)
+        tuning, _ = sim.autotune([0] * n, ys, reps=2)
+    tune_s = time.perf_counter() - tune_s
     xs_h = pack_bits([0] * n, circ.num_qubits)
     ys_h = pack_bits(ys, circ.num_qubits)
     dx = torch.from_numpy(xs_h.view(np.int64)).cuda()
@@ -233,6 +228,8 @@ def run_gb300(args):
         for _ in range(max(3, args.warmup)):
             step_device()
         torch.cuda.synchronize()
+        # work of one step: branches enumerated (vanishing pairs excluded) and reference-form ops
+        branches_step, ops_step, popc_step, logic_step, per_boundary = enumerated(L, N, sim, n)
         peaks = (ct.c_double * 4)()
         N.check(L.pq_measure_peaks(peaks))
         if dist:
@@ -290,16 +287,18 @@ def run_gb300(args):
     # roofline of the enumeration kernel (reference-form integer work)
     enum_avg = sum(enum_ms) / len(enum_ms)
     lop3, popcr = peaks[0], peaks[1]
-    t_branch_at_peak = max(2.0 * popc_amp / popcr, 2.0 * logic_amp / lop3) / bpa  # s per branch
-    ops_branch = ops_amp / bpa
-    peak_ops = ops_branch / t_branch_at_peak
-    achieved = ops_amp * n / (enum_avg * 1e-3)
+    # the reference form needs 2 popc.b32 per 64-bit popcount and 2 lop3.b32 per 64-bit logic op:
+    # at the measured pipe rates one launch's work takes at least t_peak seconds
+    t_peak = max(2.0 * popc_step / popcr, 2.0 * logic_step / lop3)
+    ops_branch = ops_step / branches_step
+    peak_ops = ops_step / t_peak
+    achieved = ops_step / (enum_avg * 1e-3)
     cpu = None
     if rank == 0 and not args.no_cpu:
         threads = cpu_threads()
         sample = max(4, int(args.cpu_sample))
-        _, _, dt = cpu_rate(circ, ys, sample, threads)
-        cpu = {"value": sample * bpa / dt, "unit": "branches/s", "cores": threads, "kind": "port",
+        cbr, dt = cpu_rate(circ, ys, sample, threads)
+        cpu = {"value": cbr / dt, "unit": "branches/s", "cores": threads, "kind": "port",
                "sample": "%d of the 4096 boundaries, same circuit and strategy (auto), CPU restatement of the "
                          "reference engine" % sample}
     line = {
@@ -308,7 +307,10 @@ def run_gb300(args):
         "vs_baseline": None, "dtype": "u64+f32", "data": "synthetic",
         "amplitudes_per_s": ws * n / (ms * 1e-3),
         "config": config({"branch_engines": stats["num_branches"], "pairs": stats["pairs"],
-                          "branches_per_step": branches_step, "wall_s_timed_region": t_wall}),
+                          "branches_per_step": branches_step, "branches_counted": "enumerated (boundary, branch "
+                          "engine) pairs only; pairs whose sum vanishes are zeros, not enumerated",
+                          "wall_s_timed_region": t_wall, "tuning": tuning,
+                          "tuning_source": "fixed" if args.no_autotune else "pq_sim_autotune (%.1f s)" % tune_s}),
         "precision": {"max_rel_err_vs_fp64": float(np.max(rel)), "median_rel_err_vs_fp64": float(np.median(rel)),
                       "max_errbound_rel": float(np.max(errb / np.abs(ref)))},
         "e2e": {"value": e2e_value, "unit": "branches/s", "ms_per_step": e2e_ms,
@@ -387,6 +389,8 @@ def run_batched(args):
     import ctypes as _ct
     kms = (_ct.c_float * 3)()
     N.check(N.lib().pq_batch_kernel_ms(b._h, kms))
+    benum = (_ct.c_double * 4)()
+    N.check(N.lib().pq_batch_enumerated(b._h, benum))
     got = dout.cpu().numpy().view(np.complex128)
     # plain path 1: one launch per circuit (its 64 boundaries), host buffers, sequential
     for s, o in zip(sims, outs):
@@ -415,7 +419,7 @@ def run_batched(args):
         bk[0] += 64
         bk[1] += t
     line = {"metric": METRIC, "workload": "batched", "value": n / (batched_ms * 1e-3), "unit": "amplitudes/s",
-            "branches_per_s": b.branches / (batched_ms * 1e-3), "ms_per_step": batched_ms, "steps": args.steps,
+            "branches_per_s": benum[0] / (batched_ms * 1e-3), "ms_per_step": batched_ms, "steps": args.steps,
             "warmup": args.warmup, "n_gpus": 1, "higher_is_better": True, "data": "synthetic",
             "plain_per_circuit_amps_per_s": n / plain_circ_s, "plain_per_boundary_amps_per_s": n / plain_bnd_s,
             "speedup_vs_plain_per_circuit": plain_circ_s / (batched_ms * 1e-3),
@@ -424,7 +428,8 @@ def run_batched(args):
             "kernel_ms_last_step": {"prepare": kms[0], "enumerate": kms[1], "reduce": kms[2]},
             "per_d_bucket_amps_per_s_plain": {k: v[0] / v[1] for k, v in buckets.items()},
             "config": {"workload": "256 circuits, n~U[16,64], 40n gates, T~U[8,36] (seed 3), 64 uniform y each, "
-                                   "strategy auto", "branches_per_step": b.branches, "host_build_s": build_s,
+                                   "strategy auto", "branches_enumerated_per_step": benum[0],
+                       "branches_all_engines_per_step": b.branches, "host_build_s": build_s,
                        "l2": "flushed between steps"}}
     print(json.dumps(line), flush=True)
     return 0
@@ -605,7 +610,7 @@ def run_rotations(args):
                         "prob_max_abs_err": float(np.max(np.abs(s20.probabilities([0] * len(idx), idx) -
                                                                 np.abs(sv[idx]) ** 2)))}
     line = {"metric": METRIC, "workload": "rotations", "value": nb / t32, "unit": "amplitudes/s", "data": "synthetic",
-            "branches_per_s": nb * res["n40"]["stats"]["branches_per_amplitude"] / t32,
+            "branches_per_s": enumerated(N.lib(), N, sim, nb)[0] / t32,
             "results": res, "config": {"workload": "n=40, 1500 gates, 24 rz(theta) theta~U[0,2pi) + 4 CCZ layers "
                                                    "(per-layer count reduced until <= 2^36 branches per amplitude); "
                                                    "%d uniform y; n=20 variant vs dense" % nb}}
@@ -622,6 +627,7 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=48)
     ap.add_argument("--ref-sample", type=int, default=24)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the library's default launch shape")
     ap.add_argument("--boundaries", type=int, default=4096, help="boundary count (profiling of smaller cases)")
     ap.add_argument("--workload", default="many_boundaries",
                     choices=["many_boundaries", "batched", "serve", "small", "rotations"])

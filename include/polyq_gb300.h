@@ -74,8 +74,9 @@ typedef struct pq_stats {
 typedef struct pq_tuning {
     int32_t inner_dims;      /* Gray steps per lane chunk = 2^inner_dims (4..14) */
     int32_t chunks_per_lane; /* chunks a lane walks per work item (1..64) */
-    int32_t block_warps;     /* warps per CTA of the enumeration kernel (1..16) */
+    int32_t block_warps;     /* warps per CTA of the enumeration kernel (1..8) */
     int32_t max_branch_dim;  /* admission cap on d per branch engine (<= 62) */
+    int32_t blocks_per_sm;   /* enumeration kernel register budget: 3 (80 regs) or 4 (64 regs) blocks */
 } pq_tuning;
 
 /* ---- library ------------------------------------------------------------------------ */
@@ -177,11 +178,31 @@ PQ_API int64_t pq_server_poll(pq_server *s, pq_result *out, int64_t cap, double 
 PQ_API double pq_server_now(const pq_server *s);
 PQ_API pq_status pq_server_drain(pq_server *s, double timeout_s);
 
+/* ---- autotuner (no counterpart in the reference crate, whose enumeration is a CPU loop) -- */
+/* Times the evaluation of n representative boundaries (host bitstrings) under candidate launch
+ * shapes -- lane chunk length 2^inner_dims (8..10), chunks_per_lane, block_warps, blocks_per_sm --
+ * by coordinate descent from the simulator's current tuning (best of `reps` device timings
+ * per candidate after a warm-up; reps 0 = 3), and leaves the simulator on the fastest.
+ * Amplitudes do not depend on the choice beyond FP64 summation order.  best (optional)
+ * receives the tuning, best_ms (optional) its device time. */
+PQ_API pq_status pq_sim_autotune(pq_sim *sim, int64_t n, const uint64_t *x, const uint64_t *y, int32_t reps,
+                                 pq_tuning *best, double *best_ms);
+/* The launch shape the simulator's plans use. */
+PQ_API pq_status pq_sim_get_tuning(const pq_sim *sim, pq_tuning *out);
+
 /* ---- measurement -------------------------------------------------------------------- */
 /* Device times (ms) of the last completed launch of the simulator's size-n plan (and of a
  * batch): [0] prepare, [1] enumeration, [2] reductions.  Blocks until that launch is done. */
 PQ_API pq_status pq_sim_kernel_ms(pq_sim *sim, int64_t n, float *ms);
 PQ_API pq_status pq_batch_kernel_ms(pq_batch *b, float *ms);
+/* Work of the last launch of the simulator's size-n plan (and of a batch), over the
+ * (boundary, branch engine) pairs whose sum did not vanish: out[0] branches enumerated (2^d
+ * each), out[1] the reference engine's integer ops for them (5 W_o + 6 W_g 64-bit ops per
+ * branch, W_o / W_g = words of odd lines / planes), out[2] the popcounts among them, out[3] the
+ * logic ops.  per_boundary (optional, n doubles) splits out[0] by boundary.  Blocks until that
+ * launch is done. */
+PQ_API pq_status pq_sim_enumerated(pq_sim *sim, int64_t n, double *out, double *per_boundary);
+PQ_API pq_status pq_batch_enumerated(pq_batch *b, double *out);
 /* Work items of the simulator's size-n plan (-1 if it has no such plan yet). */
 PQ_API int64_t pq_sim_launch_items(pq_sim *sim, int64_t n);
 /* Issue rates measured on the current device: [0] lop3.b32 ops/s, [1] popc.b32 ops/s,

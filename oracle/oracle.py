@@ -53,6 +53,8 @@ def lib():
             L.pqo_sim_free.argtypes = [P]
             L.pqo_stats.argtypes = [P, i64p]
             L.pqo_amplitudes.argtypes = [P, ct.c_int, u64p, u64p, f64p, ct.c_int]
+            L.pqo_last_branches.restype = ct.c_double
+            L.pqo_last_branches.argtypes = [P]
             L.pqo_marginal.restype = ct.c_double
             L.pqo_marginal.argtypes = [P, u64p, ct.c_int, i32p, u8p]
             L.pqo_brute_force.restype = ct.c_int
@@ -138,6 +140,10 @@ class OracleSim:
 
     def amplitude(self, x, y):
         return complex(self.amplitudes([x], [y])[0])
+
+    def last_branches(self):
+        """Branches enumerated by the last amplitudes() call (vanishing jobs excluded)."""
+        return float(self.L.pqo_last_branches(self.h))
 
     def probability(self, x, y):
         return abs(self.amplitude(x, y)) ** 2

@@ -1057,6 +1057,7 @@ struct pqo_sim {
     rank_engine eng;
     int strategy, pairs;
     int have_sw;
+    double last_branches; /* branches enumerated by the last pqo_amplitudes call */
     pathsum sw;
     int *junction;
     uint8_t *jneg;
@@ -1097,8 +1098,10 @@ static int default_threads(int n) {
     return c > 0 ? (int)c : 1;
 }
 /* Evaluate the rank engine `r` on `na` assignments; out[i] = sum over branches. */
-static void eval_many(const rank_engine *r, int na, asg_t **asg, int *asg_n, cx *out, int nthreads) {
+/* Returns the number of branches enumerated (2^d of every job whose prepare succeeded). */
+static double eval_many(const rank_engine *r, int na, asg_t **asg, int *asg_n, cx *out, int nthreads) {
     int njobs = na * r->nbr;
+    double enumerated = 0.0;
     job_t *jobs = (job_t *)calloc((size_t)(njobs ? njobs : 1), sizeof(job_t));
     for (int i = 0; i < na; i++) {
         for (int b = 0; b < r->nbr; b++) {
@@ -1112,7 +1115,10 @@ static void eval_many(const rank_engine *r, int na, asg_t **asg, int *asg_n, cx 
             values_from_asg(E, asg[i], asg_n[i], vals);
             engine_prepare(E, vals, &J->prep);
             free(vals);
-            if (J->prep.ok) J->chunk_out = (cx *)calloc((size_t)1 << J->nchunk_log2, sizeof(cx));
+            if (J->prep.ok) {
+                J->chunk_out = (cx *)calloc((size_t)1 << J->nchunk_log2, sizeof(cx));
+                enumerated += ldexp(1.0, E->el.d);
+            }
         }
     }
     run_pool(jobs, njobs, nthreads);
@@ -1133,6 +1139,7 @@ static void eval_many(const rank_engine *r, int na, asg_t **asg, int *asg_n, cx 
         out[i] = tot;
     }
     free(jobs);
+    return enumerated;
 }
 void pqo_amplitudes(pqo_sim *s, int n, const uint64_t *xs, const uint64_t *ys, double *out, int nthreads) {
     int nw = (s->ps.nq + 63) / 64;
@@ -1144,7 +1151,7 @@ void pqo_amplitudes(pqo_sim *s, int n, const uint64_t *xs, const uint64_t *ys, d
         an[i] = ps_boundary(&s->ps, xs + (size_t)i * nw, ys + (size_t)i * nw, asg[i]);
     }
     cx *res = (cx *)calloc((size_t)(n ? n : 1), sizeof(cx));
-    eval_many(&s->eng, n, asg, an, res, default_threads(nthreads));
+    s->last_branches = eval_many(&s->eng, n, asg, an, res, default_threads(nthreads));
     for (int i = 0; i < n; i++) { out[2 * i] = res[i].re; out[2 * i + 1] = res[i].im; free(asg[i]); }
     free(asg); free(an); free(res);
 }
@@ -1188,6 +1195,8 @@ int pqo_brute_force(pqo_sim *s, const uint64_t *x, const uint64_t *y, double out
     out[0] = v.re; out[1] = v.im;
     return rc;
 }
+
+double pqo_last_branches(const pqo_sim *s) { return s->last_branches; }
 
 /* ------------------------------------------------------------------ dense reference (src/dense.rs) */
 static void diag1(cx *sv, uint64_t dim, int q, cx ph) {

@@ -36,6 +36,9 @@ void pqo_stats(const pqo_sim *s, int64_t out[8]);
 /* <y|C|x> for n boundaries, evaluated on `nthreads` host threads (<=0: all cores). */
 void pqo_amplitudes(pqo_sim *s, int n, const uint64_t *xs, const uint64_t *ys, double *out, int nthreads);
 
+/* Branches enumerated by the last pqo_amplitudes call (2^d of each non-vanishing job). */
+double pqo_last_branches(const pqo_sim *s);
+
 /* Marginal probability of measuring (qubits[i] -> outcomes[i]) on input x (src/sim.rs:225-231). */
 double pqo_marginal(pqo_sim *s, const uint64_t *x, int nmeas, const int32_t *qubits, const uint8_t *outcomes);
 

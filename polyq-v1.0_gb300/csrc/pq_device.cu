@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
@@ -34,7 +35,7 @@ namespace pq {
 thread_local std::string g_err;
 static std::mutex g_mu;
 static int g_device = 0;
-static pq_tuning g_tuning = {10, 4, 8, 48};
+static pq_tuning g_tuning = {10, 4, 8, 48, 3};
 
 static pq_status fail(pq_status s, const std::string &m) {
     g_err = m;
@@ -167,6 +168,7 @@ struct Plan {
     double branches = 0.0;  // branches enumerated per run (vanishing boundaries included)
     int smem_words = 8;
     int grid_prep = 1, grid_enum = 1, block_enum = 256;
+    int minb = 3;  // enum_kernel<0, minb> instantiation (blocks per SM its registers allow)
     bool graph_ready = false;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
@@ -348,8 +350,10 @@ static pq_status build_plan(const std::vector<Segment> &segs, int nw, cudaStream
     a.errflag = P.errflag.as<int>();
     const int bw = std::max(1, std::min(8, tu.block_warps));
     P.block_enum = 32 * bw;
+    P.minb = tu.blocks_per_sm == 4 ? 4 : 3;
     int occ = 0;
-    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, enum_kernel<0>, P.block_enum, 0));
+    if (P.minb == 4) CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, enum_kernel<0, 4>, P.block_enum, 0));
+    else CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, enum_kernel<0, 3>, P.block_enum, 0));
     occ = std::max(occ, 1);
     long long want = (long long)sm_count() * occ;
     P.grid_enum = (int)std::max(1LL, std::min<long long>(want, (P.nitems + bw - 1) / bw));
@@ -376,7 +380,8 @@ static cudaError_t enqueue_core(Plan &P, int mode) {
     prepare_kernel<<<P.grid_prep, 128, (size_t)4 * P.smem_words * 8, P.stream>>>(P.args);
     if ((e = cudaEventRecordWithFlags(P.tev[1], P.stream, evflag)) != cudaSuccess) return e;
     if (mode == 1) enum_kernel<1><<<P.grid_enum, P.block_enum, 0, P.stream>>>(P.args);
-    else enum_kernel<0><<<P.grid_enum, P.block_enum, 0, P.stream>>>(P.args);
+    else if (P.minb == 4) enum_kernel<0, 4><<<P.grid_enum, P.block_enum, 0, P.stream>>>(P.args);
+    else enum_kernel<0, 3><<<P.grid_enum, P.block_enum, 0, P.stream>>>(P.args);
     if ((e = cudaEventRecordWithFlags(P.tev[2], P.stream, evflag)) != cudaSuccess) return e;
     job_reduce_kernel<<<(P.njobs + 255) / 256, 256, 0, P.stream>>>(P.args);
     out_reduce_kernel<<<(P.nout + 255) / 256, 256, 0, P.stream>>>(P.args);
@@ -485,6 +490,7 @@ struct pq_sim {
     PathSum ps;
     int strategy = 0, pairs = 0;
     int di_max = 10;
+    pq_tuning tu{};  // launch shape of this simulator's plans (library default at creation, or autotuned)
     int nw = 1;
     bool host_only = false;
     Target main;
@@ -559,6 +565,10 @@ PQ_API pq_status pq_set_default_tuning(const pq_tuning *t) {
         if (t->max_branch_dim < 1 || t->max_branch_dim > kMaxD) return fail(PQ_ERR_INVALID_ARG, "max_branch_dim in 1..62");
         n.max_branch_dim = t->max_branch_dim;
     }
+    if (t->blocks_per_sm) {
+        if (t->blocks_per_sm != 3 && t->blocks_per_sm != 4) return fail(PQ_ERR_INVALID_ARG, "blocks_per_sm is 3 or 4");
+        n.blocks_per_sm = t->blocks_per_sm;
+    }
     g_tuning = n;
     return PQ_OK;
 }
@@ -585,6 +595,7 @@ static pq_status sim_build_host(const pq_circuit_desc *c, int32_t strategy, int3
     S->nw = words_for(c->num_qubits);
     {
         std::lock_guard<std::mutex> lk(g_mu);
+        S->tu = g_tuning;
         S->di_max = g_tuning.inner_dims;
     }
     try {
@@ -665,14 +676,9 @@ static pq_status sim_plan(pq_sim *s, int64_t n, Plan **out) {
         *out = it->second.get();
         return PQ_OK;
     }
-    pq_tuning tu;
-    {
-        std::lock_guard<std::mutex> lk(g_mu);
-        tu = g_tuning;
-    }
     auto P = std::make_unique<Plan>();
     std::vector<Segment> segs{{&s->main, n}};
-    pq_status st = build_plan(segs, s->nw, s->stream, tu, *P);
+    pq_status st = build_plan(segs, s->nw, s->stream, s->tu, *P);
     if (st != PQ_OK) return st;
     *out = P.get();
     s->plans[n] = std::move(P);
@@ -808,14 +814,9 @@ PQ_API pq_status pq_marginal(pq_sim *s, const uint64_t *x, int32_t nmeas, const 
     pq_status st = marg_target(s, qubits, nmeas, &M);
     if (st != PQ_OK) return st;
     if (!M->plan) {
-        pq_tuning tu;
-        {
-            std::lock_guard<std::mutex> lk2(g_mu);
-            tu = g_tuning;
-        }
         auto P = std::make_unique<Plan>();
         std::vector<Segment> segs{{&M->tg, 1}};
-        st = build_plan(segs, s->nw, s->stream, tu, *P);
+        st = build_plan(segs, s->nw, s->stream, s->tu, *P);
         if (st != PQ_OK) return st;
         M->plan = std::move(P);
     }
@@ -894,11 +895,164 @@ PQ_API pq_status pq_batch_kernel_ms(pq_batch *b, float *ms) {
     CU(cudaEventSynchronize(b->plan->tev[3]));
     return last_kernel_ms(*b->plan, ms);
 }
+// Branches actually enumerated by the last launch of the simulator's size-n plan: 2^d of every
+// (boundary, branch engine) job whose boundary did not make the sum vanish (a vanishing job --
+// contradictory boundary or inconsistent radical system -- is a zero, not enumerated).
+// out[0] branches, out[1] reference-form int64 ops (5 W_o + 6 W_g per branch), out[2] of which
+// 64-bit popcounts (2 W_o + W_g), out[3] of which 64-bit logic ops (3 W_o + 5 W_g).
+static pq_status plan_enumerated(Plan &P, double *out, double *per_out) {
+    CU(cudaStreamSynchronize(P.stream));
+    std::vector<JobDev> jobs((size_t)P.njobs);
+    CU(cudaMemcpy(jobs.data(), P.jobs.p, sizeof(JobDev) * jobs.size(), cudaMemcpyDeviceToHost));
+    std::vector<EngineDev> eng(P.engines.n / sizeof(EngineDev));
+    CU(cudaMemcpy(eng.data(), P.engines.p, sizeof(EngineDev) * eng.size(), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < 4; i++) out[i] = 0.0;
+    if (per_out)
+        for (int o = 0; o < P.nout; o++) per_out[o] = 0.0;
+    for (const auto &J : jobs) {
+        if (J.vanish) continue;
+        const EngineDev &E = eng[J.engine];
+        const double b = std::ldexp(1.0, E.d);
+        out[0] += b;
+        out[1] += b * (5.0 * E.wo + 6.0 * E.wg);
+        out[2] += b * (2.0 * E.wo + E.wg);
+        out[3] += b * (3.0 * E.wo + 5.0 * E.wg);
+        if (per_out) per_out[J.out] += b;
+    }
+    return PQ_OK;
+}
+PQ_API pq_status pq_sim_enumerated(pq_sim *s, int64_t n, double *out, double *per_boundary) {
+    if (!s || !out) return fail(PQ_ERR_INVALID_ARG, "null argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->plans.find(n);
+    if (it == s->plans.end() || !it->second->graph_ready) return fail(PQ_ERR_INVALID_ARG, "no launch of that size yet");
+    return plan_enumerated(*it->second, out, per_boundary);
+}
+PQ_API pq_status pq_batch_enumerated(pq_batch *b, double *out) {
+    if (!b || !out) return fail(PQ_ERR_INVALID_ARG, "null argument");
+    std::lock_guard<std::mutex> lk(b->mu);
+    if (!b->plan->graph_ready) return fail(PQ_ERR_INVALID_ARG, "batch has not run yet");
+    return plan_enumerated(*b->plan, out, nullptr);
+}
 PQ_API int64_t pq_sim_launch_items(pq_sim *s, int64_t n) {
     if (!s) return -1;
     std::lock_guard<std::mutex> lk(s->mu);
     auto it = s->plans.find(n);
     return it == s->plans.end() ? -1 : (int64_t)it->second->nitems;
+}
+
+// ---------------------------------------------------------------- autotuner
+// Rebuilds a simulator's resident weight tables for a new low-coordinate count (the tables'
+// layout depends on it); cached plans point into the old tables and are dropped first.
+static pq_status retable_sim(pq_sim *s, int di) {
+    CU(cudaStreamSynchronize(s->stream));
+    s->plans.clear();
+    s->main.dev.clear();
+    s->main.mem.clear();
+    s->main.max_d = s->main.max_rank = s->main.max_words = 0;
+    pq_status st = upload_target(s->main, di);
+    if (st != PQ_OK) return st;
+    s->di_max = di;
+    return PQ_OK;
+}
+
+// Device time (ms, best of `reps` after one warm-up) of one launch of the simulator's
+// evaluation of n boundaries under tuning `tu`.
+static pq_status time_tuning(pq_sim *s, int64_t n, const uint64_t *x, const uint64_t *y, int reps,
+                             const pq_tuning &tu, std::vector<double> &scratch, double *ms_out) {
+    if (tu.inner_dims != s->di_max) {
+        pq_status st = retable_sim(s, tu.inner_dims);
+        if (st != PQ_OK) return st;
+    }
+    Plan P;
+    std::vector<Segment> segs{{&s->main, n}};
+    pq_status st = build_plan(segs, s->nw, s->stream, tu, P);
+    if (st != PQ_OK) return st;
+    scratch.resize((size_t)2 * n);
+    double best = 1e300;
+    for (int r = 0; r <= reps; r++) {
+        st = run_host(P, x, y, scratch.data(), nullptr, false);
+        if (st != PQ_OK) return st;
+        float ms[3];
+        st = last_kernel_ms(P, ms);
+        if (st != PQ_OK) return st;
+        if (r > 0) best = std::min(best, (double)ms[0] + ms[1] + ms[2]);
+    }
+    *ms_out = best;
+    return PQ_OK;
+}
+
+PQ_API pq_status pq_sim_autotune(pq_sim *s, int64_t n, const uint64_t *x, const uint64_t *y, int32_t reps,
+                                 pq_tuning *best_out, double *best_ms) {
+    if (!s || !x || !y) return fail(PQ_ERR_INVALID_ARG, "null argument");
+    pq_status st = check_n(n);
+    if (st != PQ_OK) return st;
+    if (reps < 0 || reps > 1000) return fail(PQ_ERR_INVALID_ARG, "reps in 0..1000");
+    if (reps == 0) reps = 3;
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->host_only) return fail(PQ_ERR_NO_DEVICE, "simulator was created by pq_analyze (host structures only)");
+    CU(cudaSetDevice(s->device));
+    // candidate values per field; the search starts from the simulator's current tuning.  Lane
+    // chunks stop at 2^10 steps: the plain-FP32 low-part sums lose accuracy as 4^inner_dims
+    // (more terms on a coarser exact grid), and 2^12 already costs an order of magnitude.
+    const std::vector<int> axes[4] = {{8, 9, 10}, {1, 2, 4, 8, 16}, {2, 4, 8}, {3, 4}};
+    auto field = [](pq_tuning &t, int k) -> int32_t & {
+        return k == 0 ? t.inner_dims : k == 1 ? t.chunks_per_lane : k == 2 ? t.block_warps : t.blocks_per_sm;
+    };
+    std::map<std::array<int, 4>, double> seen;
+    std::vector<double> scratch;
+    auto eval = [&](pq_tuning t, double *ms) -> pq_status {
+        std::array<int, 4> key{t.inner_dims, t.chunks_per_lane, t.block_warps, t.blocks_per_sm};
+        auto it = seen.find(key);
+        if (it != seen.end()) {
+            *ms = it->second;
+            return PQ_OK;
+        }
+        pq_status e = time_tuning(s, n, x, y, reps, t, scratch, ms);
+        if (e == PQ_OK) seen[key] = *ms;
+        return e;
+    };
+    pq_tuning best = s->tu;
+    best.inner_dims = s->di_max;
+    double best_t = 0.0;
+    st = eval(best, &best_t);
+    // coordinate descent: sweep one field at a time, keep the fastest, until a full pass
+    // changes nothing (at most three passes)
+    for (int pass = 0; st == PQ_OK && pass < 3; pass++) {
+        bool changed = false;
+        for (int k = 0; k < 4 && st == PQ_OK; k++) {
+            for (int v : axes[k]) {
+                pq_tuning t = best;
+                field(t, k) = v;
+                double ms = 0.0;
+                st = eval(t, &ms);
+                if (st != PQ_OK) break;
+                if (ms < best_t * 0.98) {  // a 2% margin keeps timing noise from flipping choices
+                    best = t;
+                    best_t = ms;
+                    changed = true;
+                }
+            }
+        }
+        if (!changed) break;
+    }
+    // whatever happened, leave the simulator on its best known tuning
+    pq_status st2 = PQ_OK;
+    if (best.inner_dims != s->di_max) st2 = retable_sim(s, best.inner_dims);
+    s->tu = best;
+    s->plans.clear();
+    if (st != PQ_OK) return st;
+    if (st2 != PQ_OK) return st2;
+    if (best_out) *best_out = best;
+    if (best_ms) *best_ms = best_t;
+    return PQ_OK;
+}
+
+PQ_API pq_status pq_sim_get_tuning(const pq_sim *s, pq_tuning *out) {
+    if (!s || !out) return fail(PQ_ERR_INVALID_ARG, "null argument");
+    *out = s->tu;
+    out->inner_dims = s->di_max;
+    return PQ_OK;
 }
 
 // ---------------------------------------------------------------- checks

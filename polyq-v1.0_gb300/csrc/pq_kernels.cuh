@@ -147,6 +147,14 @@ __global__ void __launch_bounds__(128) prepare_kernel(KArgs a) {
 // T_j = (1 << j) | (R_j << DI) into sidx.  The branch value i^m * w accumulates as
 // S = A + iB with A += cos(m pi/2) w, B += sin(m pi/2) w (coefficients 0/+-1: the hi sums are
 // exact multiples of the table grid; lo sums in plain FP32).
+// (cos, sin)(m pi/2) from the bits of m: +-1.0f carries the sign in bit 31 ((m & 2) << 30), and
+// exactly one of the two is non-zero (chosen by m & 1).
+__device__ __forceinline__ float2 quarter_turn(uint32_t m) {
+    const uint32_t one = 0x3F800000u | ((m & 2u) << 30);
+    const uint32_t odd = m & 1u;
+    return make_float2(__uint_as_float(odd ? 0u : one), __uint_as_float(odd ? one : 0u));
+}
+
 template <int MODE>
 __device__ __forceinline__ void gray_chunk8(const float4 *__restrict__ W, const float2 *cs, uint32_t &m,
                                             uint32_t &sidx, uint32_t &P, const uint32_t *Gi, const uint32_t *Tg,
@@ -160,7 +168,7 @@ __device__ __forceinline__ void gray_chunk8(const float4 *__restrict__ W, const 
 #define PQ_EVAL()                                                                   \
     {                                                                               \
         if (MODE == 2) dbg[sbase | (sidx & inner)] = (uint8_t)((k0 + 2u * m) & 7u); \
-        const float2 c = cs[m & 3u];                                                \
+        const float2 c = quarter_turn(m);                                           \
         const float4 w = __ldg(&W[sidx]);                                           \
         acc[0] = fmaf(c.x, w.x, acc[0]);                                            \
         acc[1] = fmaf(c.x, w.y, acc[1]);                                            \
@@ -203,8 +211,10 @@ __device__ __forceinline__ void gray_chunk8(const float4 *__restrict__ W, const 
 
 // MODE 0: FP32 weights, compensated accumulation.  MODE 1: FP64 weights and accumulation.
 // MODE 2: record the Z8 index of every branch into dbg (single-job debug launches).
-template <int MODE>
-__global__ void __launch_bounds__(256) enum_kernel(KArgs a) {
+// MINB: resident blocks per SM the register allocation is sized for (3: 80 registers, no
+// spills; 4: 64 registers) -- chosen per launch by measurement.
+template <int MODE, int MINB = 3>
+__global__ void __launch_bounds__(256, MINB) enum_kernel(KArgs a) {
     __shared__ uint64_t sG[8][64];
     __shared__ uint64_t sR[8][64];
     __shared__ uint8_t sLp[8][64];
@@ -276,8 +286,8 @@ __global__ void __launch_bounds__(256) enum_kernel(KArgs a) {
                 uint32_t m;
                 uint64_t yy;
                 chunk_start(Lp, G, R, J.y0, s, m, yy);
-                const double2 chi = chunk_high_weight(E, s);
                 uint64_t ss = s;
+                double vx, vy;  // the chunk's sum before the weight of the coordinates >= DI
                 if (MODE == 1 || !E.joint) {
                     // FP64 weights and accumulation (verification mode, and engines with more
                     // pivots than the joint table holds)
@@ -295,8 +305,8 @@ __global__ void __launch_bounds__(256) enum_kernel(KArgs a) {
                         ss ^= 1ull << j;
                         yy ^= R[j];
                     }
-                    accx += sx * chi.x - sy * chi.y;
-                    accy += sx * chi.y + sy * chi.x;
+                    vx = sx;
+                    vy = sy;
                 } else if (dl >= 3) {
                     // FP32, unrolled Gray walk with exact hi sums (gray_chunk8)
                     float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
@@ -304,10 +314,8 @@ __global__ void __launch_bounds__(256) enum_kernel(KArgs a) {
                     uint32_t P = 0;
                     for (int j = 0; j < dl; j++) P |= (uint32_t)(popc64(G[j] & s) & 1) << j;
                     gray_chunk8<MODE>(E.wtab, sCS, m, sidx, P, Gi, Tg, Lp, Lm, dl, acc, a.dbg, s, J.k0);
-                    const double vx = ((double)acc[0] + (double)acc[4]) - ((double)acc[3] + (double)acc[7]);
-                    const double vy = ((double)acc[1] + (double)acc[5]) + ((double)acc[2] + (double)acc[6]);
-                    accx += vx * chi.x - vy * chi.y;
-                    accy += vx * chi.y + vy * chi.x;
+                    vx = ((double)acc[0] + (double)acc[4]) - ((double)acc[3] + (double)acc[7]);
+                    vy = ((double)acc[1] + (double)acc[5]) + ((double)acc[2] + (double)acc[6]);
                 } else {
                     // FP32 for chunks of fewer than 8 steps: hi parts with TwoSum, lo parts plain
                     float ax = 0.f, ay = 0.f, cx = 0.f, cy = 0.f, lx = 0.f, ly = 0.f;
@@ -326,11 +334,12 @@ __global__ void __launch_bounds__(256) enum_kernel(KArgs a) {
                         ss ^= 1ull << j;
                         yy ^= R[j];
                     }
-                    const double vx = (double)ax + (double)cx + (double)lx;
-                    const double vy = (double)ay + (double)cy + (double)ly;
-                    accx += vx * chi.x - vy * chi.y;
-                    accy += vx * chi.y + vy * chi.x;
+                    vx = (double)ax + (double)cx + (double)lx;
+                    vy = (double)ay + (double)cy + (double)ly;
                 }
+                const double2 chi = chunk_high_weight(E, s);
+                accx += vx * chi.x - vy * chi.y;
+                accy += vx * chi.y + vy * chi.x;
             }
         }
         for (int o = 16; o; o >>= 1) {

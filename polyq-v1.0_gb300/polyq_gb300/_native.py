@@ -40,7 +40,7 @@ class Stats(ct.Structure):
 
 class Tuning(ct.Structure):
     _fields_ = [("inner_dims", ct.c_int32), ("chunks_per_lane", ct.c_int32), ("block_warps", ct.c_int32),
-                ("max_branch_dim", ct.c_int32)]
+                ("max_branch_dim", ct.c_int32), ("blocks_per_sm", ct.c_int32)]
 
 
 class Request(ct.Structure):
@@ -88,7 +88,11 @@ SIGNATURES = {
     "pq_sim_kernel_ms": (ct.c_int, [P, ct.c_int64, ct.POINTER(ct.c_float)]),
     "pq_batch_kernel_ms": (ct.c_int, [P, ct.POINTER(ct.c_float)]),
     "pq_sim_launch_items": (ct.c_int64, [P, ct.c_int64]),
+    "pq_sim_enumerated": (ct.c_int, [P, ct.c_int64, f64p, f64p]),
+    "pq_batch_enumerated": (ct.c_int, [P, f64p]),
     "pq_measure_peaks": (ct.c_int, [f64p]),
+    "pq_sim_autotune": (ct.c_int, [P, ct.c_int64, u64p, u64p, ct.c_int32, ct.POINTER(Tuning), f64p]),
+    "pq_sim_get_tuning": (ct.c_int, [P, ct.POINTER(Tuning)]),
     "pq_debug_engine_dump": (ct.c_int64, [P, ct.c_int32, u64p, ct.c_int64]),
     "pq_debug_branch_phases": (ct.c_int32, [P, ct.c_int32, u64p, u64p, u8p]),
 }

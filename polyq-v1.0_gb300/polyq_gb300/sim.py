@@ -136,6 +136,22 @@ class Simulator:
                                             _p(out, ct.c_double)))
         return out.view(np.complex128)
 
+    def autotune(self, inputs, outputs, reps: int = 3):
+        """Pick the fastest launch shape for boundaries like these (pq_sim_autotune); returns
+        (tuning dict, device ms of one launch)."""
+        xs = pack_bits(inputs, self.num_qubits)
+        ys = pack_bits(outputs, self.num_qubits)
+        t = N.Tuning()
+        ms = ct.c_double(0.0)
+        N.check(self._L.pq_sim_autotune(self._h, xs.shape[0], _p(xs, ct.c_uint64), _p(ys, ct.c_uint64), reps,
+                                        ct.byref(t), ct.byref(ms)))
+        return {k: getattr(t, k) for k, _ in N.Tuning._fields_}, ms.value
+
+    def tuning(self) -> dict:
+        t = N.Tuning()
+        N.check(self._L.pq_sim_get_tuning(self._h, ct.byref(t)))
+        return {k: getattr(t, k) for k, _ in N.Tuning._fields_}
+
     def amplitudes_fp64(self, inputs, outputs):
         xs = pack_bits(inputs, self.num_qubits)
         ys = pack_bits(outputs, self.num_qubits)
@@ -233,8 +249,9 @@ class Batch:
             pass
 
 
-def set_tuning(inner_dims=0, chunks_per_lane=0, block_warps=0, max_branch_dim=0):
-    t = N.Tuning(inner_dims, chunks_per_lane, block_warps, max_branch_dim)
+def set_tuning(inner_dims=0, chunks_per_lane=0, block_warps=0, max_branch_dim=0, blocks_per_sm=0):
+    """Defaults for simulators and batches created afterwards (0 keeps a field unchanged)."""
+    t = N.Tuning(inner_dims, chunks_per_lane, block_warps, max_branch_dim, blocks_per_sm)
     N.check(N.lib().pq_set_default_tuning(ct.byref(t)))
 
 

@@ -46,4 +46,6 @@ def test_tuning_validation(native):
         set_tuning(inner_dims=20)
     with pytest.raises(N.PqError):
         set_tuning(block_warps=9)
+    with pytest.raises(N.PqError):
+        set_tuning(blocks_per_sm=5)
     assert get_tuning() == old

@@ -249,3 +249,30 @@ def test_device_resident_path_matches_host_path(gpu):
     torch.cuda.synchronize()
     dev = out.cpu().numpy().view(np.complex128)
     assert np.array_equal(dev, host)
+
+
+def test_autotune_keeps_results(gpu):
+    # the autotuner may change every launch-shape field; amplitudes move at most by FP64
+    # summation order and stay within their bounds of the FP64 oracle
+    c = workload_many_boundaries(0)
+    s = Simulator(c)
+    ys = random_outputs(50, 128, 5)
+    before = s.amplitudes([0] * 128, ys)
+    tuning, ms = s.autotune([0] * 128, ys, reps=1)
+    assert ms > 0.0
+    assert s.tuning() == tuning
+    assert tuning["blocks_per_sm"] in (3, 4) and 8 <= tuning["inner_dims"] <= 10
+    after, err = s.amplitudes([0] * 128, ys, with_error=True)
+    scale = float(np.max(np.abs(before)))
+    assert np.all(np.abs(after - before) <= err + 1e-12 * scale)
+    want = O.OracleSim(c).amplitudes([0] * 24, ys[:24])
+    assert_amps(after[:24], want, err[:24])
+    for bps in (3, 4):
+        set_old = get_tuning()
+        try:
+            set_tuning(blocks_per_sm=bps)
+            s2 = Simulator(c)
+            assert s2.tuning()["blocks_per_sm"] == bps
+            np.testing.assert_allclose(s2.amplitudes([0] * 128, ys), before, rtol=0, atol=1e-13 * scale)
+        finally:
+            set_tuning(blocks_per_sm=set_old["blocks_per_sm"])
