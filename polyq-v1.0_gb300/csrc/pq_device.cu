@@ -206,15 +206,6 @@ static int sm_count() {
 
 // Work decomposition of one job (fixed per job, so a boundary's result does not depend on
 // what else shares the launch): chunks of 2^dl Gray steps, 32 * cpl chunks per item.
-static void job_shape(int d, int DI, int cpl, int &dl, unsigned long long &nch, unsigned &cpi) {
-    dl = d <= 5 ? 0 : std::min(d - 5, DI);
-    nch = 1ull << (d - dl);
-    unsigned long long per = 32ull * (unsigned long long)cpl;
-    // at most 2^16 items per job so partial buffers stay bounded
-    while ((nch + per - 1) / per > (1ull << 16)) per *= 2;
-    cpi = (unsigned)std::min<unsigned long long>(nch, per);
-}
-
 // `light`: a one-shot plan (serving waves): device buffers come from the stream-ordered pool
 // and are released in stream order; no pinned host staging.
 static pq_status build_plan(const std::vector<Segment> &segs, int nw, cudaStream_t stream, const pq_tuning &tu,
@@ -286,7 +277,7 @@ static pq_status build_plan(const std::vector<Segment> &segs, int nw, cudaStream
         int j = perm[k];
         kinv[j] = k;
         const EngineDev &E = eng[jobs[j].engine];
-        job_shape(E.d, E.DI, tu.chunks_per_lane, jdl[j], jnch[j], jcpi[j]);
+        job_shape(E, tu.chunks_per_lane, jdl[j], jnch[j], jcpi[j]);
         istart[k + 1] = istart[k] + (long long)((jnch[j] + jcpi[j] - 1) / jcpi[j]);
         P.branches += std::ldexp(1.0, E.d);
     }
@@ -1164,15 +1155,6 @@ static NoAllocScratch *g_na_ptr[64] = {nullptr};  // device address of the scrat
 
 // Same per-job work shape as the regular launch layout, so each job's partial sums come out
 // in the same order (and the results bit-identical to pq_amplitudes).
-__device__ __forceinline__ void na_job_shape(int d, int DI, int cpl, int &dl, unsigned long long &nch,
-                                             unsigned &cpi) {
-    dl = d <= 5 ? 0 : min(d - 5, DI);
-    nch = 1ull << (d - dl);
-    unsigned long long per = 32ull * (unsigned long long)cpl;
-    while ((nch + per - 1) / per > (1ull << 16)) per *= 2;
-    cpi = (unsigned)(nch < per ? nch : per);
-}
-
 // One block: job records, identity item order, per-job shapes and the item prefix sums.
 __global__ void __launch_bounds__(1024) na_layout_kernel(NoAllocScratch *S, int nreq, int nb, int cpl) {
     __shared__ long long part[1024];
@@ -1189,7 +1171,7 @@ __global__ void __launch_bounds__(1024) na_layout_kernel(NoAllocScratch *S, int 
         S->perm[j] = j;
         S->kinv[j] = j;
         const EngineDev &E = S->engines[j % nb];
-        na_job_shape(E.d, E.DI, cpl, S->jdl[j], S->jnch[j], S->jcpi[j]);
+        job_shape(E, cpl, S->jdl[j], S->jnch[j], S->jcpi[j]);
         local += (long long)((S->jnch[j] + S->jcpi[j] - 1) / S->jcpi[j]);
     }
     part[threadIdx.x] = local;
@@ -1239,7 +1221,7 @@ extern "C" PQ_API pq_status pq_amplitudes_noalloc(pq_sim *s, int64_t n, const ui
             int dl;
             unsigned long long nch;
             unsigned cpi;
-            job_shape(E.d, E.DI, tu.chunks_per_lane, dl, nch, cpi);
+            job_shape(E, tu.chunks_per_lane, dl, nch, cpi);
             nitems += (long long)((nch + cpi - 1) / cpi);
         }
     if (nitems > kNaMaxItems)
@@ -1345,7 +1327,7 @@ static int64_t request_bytes(const Target &T, const pq_tuning &tu) {
         int dl;
         unsigned long long nch;
         unsigned cpi;
-        job_shape(E.d, E.DI, tu.chunks_per_lane, dl, nch, cpi);
+        job_shape(E, tu.chunks_per_lane, dl, nch, cpi);
         b += (int64_t)sizeof(JobDev) + 64 + 16 * (int64_t)((nch + cpi - 1) / cpi);
     }
     return b;

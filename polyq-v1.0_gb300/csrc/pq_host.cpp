@@ -692,6 +692,13 @@ PackedEngine pack_engine(const HostEngine& e, const EngineTables& T) {
     d.tlo64 = as_off<double2>(k.vec(T.tlo));
     d.tp64 = as_off<double2>(k.vec(T.tp));
     d.joint = T.joint ? 1 : 0;
+    d.pairc = -1;
+    if (T.joint)
+        for (int j = T.DI; j < e.d; j++)
+            if (e.R[(size_t)j] == 0) {
+                d.pairc = j;
+                break;
+            }
     // hi.re, hi.im, lo.re, lo.im with hi + lo = the FP64 weight.  hi lies on the grid g, a power
     // of two with 2^DI * max|w| <= 2^23 g: any sum of at most 2^DI hi parts (a chunk) is then an
     // integer multiple of g below 2^24 g, i.e. exact in FP32; lo = w - hi (|lo| <= g/2) carries
@@ -715,8 +722,20 @@ PackedEngine pack_engine(const HostEngine& e, const EngineTables& T) {
         }
         d.errfac = 4.0 * n * (grid / 2.0) * (gam + u) * hi_abs;
     }
+    // The table entry of low coordinates s carries the sign (-1)^{q(s)} of the quadratic phase
+    // among them, q(s) = sum_{i<j<DI} G_ij s_i s_j, so that the enumeration sees a Z4 index that
+    // is linear in the coordinates it walks.
+    std::vector<uint8_t> qsign((size_t)1 << T.DI, 0);
+    for (size_t s = 1; s < qsign.size(); s++) {
+        const int j = __builtin_ctzll((unsigned long long)s);
+        const uint64_t rest = (uint64_t)s & ~(1ull << j);
+        qsign[s] = (uint8_t)(qsign[rest] ^ (__builtin_popcountll(e.G[(size_t)j] & rest) & 1));
+    }
     std::vector<float> w32;
-    for (const auto& c : T.w) {
+    const size_t lomask = ((size_t)1 << T.DI) - 1;
+    for (size_t idx = 0; idx < T.w.size(); idx++) {
+        Cplx c = T.w[idx];
+        if (qsign[idx & lomask]) c = Cplx{-c.re, -c.im};
         const double hr = grid > 0.0 ? std::nearbyint(c.re / grid) * grid : 0.0;
         const double hi = grid > 0.0 ? std::nearbyint(c.im / grid) * grid : 0.0;
         w32.push_back((float)hr);

@@ -136,17 +136,6 @@ __global__ void __launch_bounds__(128) prepare_kernel(KArgs a) {
 }
 
 // ------------------------------------------------------------------------------ enumerate
-// Gray walk over the 2^dl inner coordinates of one chunk (dl >= 3), unrolled by 8: inside a
-// group of 8 steps coordinates 0 and 1 flip at fixed positions with fixed directions
-// (0+, 1+, 0-, 0+, 1-, 0-), coordinate 2 flips once with the group's direction and the group
-// boundary flips coordinate 3 + ctz(g+1).
-//   m     Z4 index (k8 - k0)/2 of the current branch, kept modulo 4 by masking at use
-//   sidx  (pivot bits << DI) | low DI coordinates: the weight-table index
-//   P     bit j = parity(G_j & s) for the inner coordinates j < dl
-// A step on coordinate j adds +-Lp_j + 2 P_j to m, xors the inner part of G_j into P and
-// T_j = (1 << j) | (R_j << DI) into sidx.  The branch value i^m * w accumulates as
-// S = A + iB with A += cos(m pi/2) w, B += sin(m pi/2) w (coefficients 0/+-1: the hi sums are
-// exact multiples of the table grid; lo sums in plain FP32).
 // (cos, sin)(m pi/2) from the bits of m: +-1.0f carries the sign in bit 31 ((m & 2) << 30), and
 // exactly one of the two is non-zero (chosen by m & 1).
 __device__ __forceinline__ float2 quarter_turn(uint32_t m) {
@@ -155,58 +144,110 @@ __device__ __forceinline__ float2 quarter_turn(uint32_t m) {
     return make_float2(__uint_as_float(odd ? 0u : one), __uint_as_float(odd ? one : 0u));
 }
 
-template <int MODE>
-__device__ __forceinline__ void gray_chunk8(const float4 *__restrict__ W, const float2 *cs, uint32_t &m,
-                                            uint32_t &sidx, uint32_t &P, const uint32_t *Gi, const uint32_t *Tg,
-                                            const uint8_t *Lp, const uint8_t *Lm, int dl, float (&acc)[8],
-                                            uint8_t *dbg, uint64_t sbase, uint32_t k0) {
-    const uint32_t G0 = Gi[0], G1 = Gi[1], G2 = Gi[2];
+// Parity of the quadratic part sum_{i<j} G_ij x_i x_j restricted to the bits of x (G symmetric,
+// zero diagonal): every pair is counted twice by sum_{j in x} popc(G_j & x).
+__device__ __forceinline__ uint32_t quad_parity(const uint64_t *G, uint64_t x) {
+    uint32_t t = 0;
+    for (uint64_t r = x; r; r &= r - 1) t += (uint32_t)popc64(G[ctz64(r)] & x);
+    return (t >> 1) & 1u;
+}
+
+// Gray walk over the 2^dl inner coordinates of K chunks (dl >= 3) in a rotating frame.
+//
+// The weight table W holds w(y, s_lo) * (-1)^{q(s_lo)}, q = sum_{i<j<DI} G_ij s_i s_j: the
+// quadratic phase among the low coordinates is folded into the table.  What remains of the Z4
+// index over the walked coordinates is linear: flipping coordinate j up adds L'_j = Lp_j + 2 c_j
+// (c_j = parity(G_j & s_hi), constant inside a chunk), flipping it down subtracts L'_j.
+//
+// With m_k the (folded) index of the k-th branch, the walk keeps A_k = i^{-m_k} sum_{l<=k}
+// i^{m_l} w_l, so that A_{k+1} = i^{-Delta_k} A_k + w_{k+1}: each step is a quarter-turn of the
+// accumulator by a per-chunk constant plus the table entry, with no per-branch phase arithmetic.
+// A quarter-turn has coefficients 0/+-1: hi sums stay exact multiples of the table grid, lo sums
+// are plain FP32.  The K chunks of a unit differ only in coordinates that touch no pivot, so
+// they read the same table entry at every step (one load feeds K accumulators); they differ in
+// their c_j.  Unrolled by 8: coordinates 0 and 1 flip at fixed positions with fixed directions
+// (0+, 1+, 0-, 0+, 1-, 0-), coordinate 2 once per group with the group's direction, and the
+// group boundary flips coordinate 3 + ctz(g+1).
+//   sidx   (pivot bits << DI) | low DI coordinates: the table index
+//   Pc[k]  bit j = c_j of chunk k for the walked coordinates
+//   T_j    (1 << j) | (R_j << DI): the change of sidx when coordinate j flips
+// On return acc[k] = (hi.re, hi.im, lo.re, lo.im) of chunk k's A at the last branch, whose
+// folded index is m[k] + L'_{dl-1} (the walk ends on the unit vector of coordinate dl-1).
+template <int MODE, int K>
+__device__ __forceinline__ void gray_chunk_rot(const float4 *__restrict__ W, uint32_t sidx, const uint32_t (&Pc)[K],
+                                               const uint32_t *Tg, const uint8_t *Lp, int dl, float (&acc)[K][4],
+                                               uint8_t *dbg, const uint64_t (&sbase)[K], uint32_t k0,
+                                               uint32_t (&m)[K], const uint64_t *G, uint32_t lomask) {
     const uint32_t T0 = Tg[0], T1 = Tg[1], T2 = Tg[2];
-    const uint32_t L0p = Lp[0], L0m = Lm[0], L1p = Lp[1], L1m = Lm[1], L2p = Lp[2], L2m = Lm[2];
+    const uint32_t Lp0 = Lp[0], Lp1 = Lp[1], Lp2 = Lp[2];
+    float2 r0[K], r1[K], r2[K];
+    float hr[K], hi[K], lr[K], li[K];
+    const float4 w0 = __ldg(&W[sidx]);
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        r0[k] = quarter_turn(Lp0 + ((Pc[k] & 1u) << 1));
+        r1[k] = quarter_turn(Lp1 + (Pc[k] & 2u));
+        r2[k] = quarter_turn(Lp2 + ((Pc[k] >> 1) & 2u));
+        hr[k] = w0.x; hi[k] = w0.y; lr[k] = w0.z; li[k] = w0.w;
+    }
     const uint32_t inner = (1u << dl) - 1u;
     const uint32_t ngroups = 1u << (dl - 3);
-#define PQ_EVAL()                                                                   \
-    {                                                                               \
-        if (MODE == 2) dbg[sbase | (sidx & inner)] = (uint8_t)((k0 + 2u * m) & 7u); \
-        const float2 c = quarter_turn(m);                                           \
-        const float4 w = __ldg(&W[sidx]);                                           \
-        acc[0] = fmaf(c.x, w.x, acc[0]);                                            \
-        acc[1] = fmaf(c.x, w.y, acc[1]);                                            \
-        acc[2] = fmaf(c.y, w.x, acc[2]);                                            \
-        acc[3] = fmaf(c.y, w.y, acc[3]);                                            \
-        acc[4] = fmaf(c.x, w.z, acc[4]);                                            \
-        acc[5] = fmaf(c.x, w.w, acc[5]);                                            \
-        acc[6] = fmaf(c.y, w.z, acc[6]);                                            \
-        acc[7] = fmaf(c.y, w.w, acc[7]);                                            \
+    // MODE 2 records the true Z8 index: folded index + 2 q(s_lo) (the sign held by the table)
+#define PQ_REC(k)                                                                                        \
+    if (MODE == 2)                                                                                       \
+        dbg[sbase[k] | (sidx & inner)] = (uint8_t)((k0 + 2u * (m[k] + 2u * quad_parity(G, sidx & lomask))) & 7u);
+    // A <- i^{-D} A + w with (cos, sin)(D pi/2) = (c, sg):
+    // (c - i sg)(re + i im) = (c re + sg im) + i (c im - sg re)
+#define PQ_ROT(T, CS, SG, DM)                                            \
+    {                                                                    \
+        sidx ^= (T);                                                     \
+        const float4 w = __ldg(&W[sidx]);                                \
+        _Pragma("unroll") for (int k = 0; k < K; k++) {                  \
+            const float c = (CS), sg = (SG);                             \
+            const float nhr = fmaf(sg, hi[k], fmaf(c, hr[k], w.x));      \
+            const float nhi = fmaf(-sg, hr[k], fmaf(c, hi[k], w.y));     \
+            const float nlr = fmaf(sg, li[k], fmaf(c, lr[k], w.z));      \
+            const float nli = fmaf(-sg, lr[k], fmaf(c, li[k], w.w));     \
+            hr[k] = nhr; hi[k] = nhi; lr[k] = nlr; li[k] = nli;          \
+            if (MODE == 2) m[k] += (DM);                                 \
+            PQ_REC(k)                                                    \
+        }                                                                \
     }
-#define PQ_STEP(j, L, Gj, Tj)                \
-    {                                        \
-        m += (L) + (((P >> (j)) & 1u) << 1); \
-        P ^= (Gj);                           \
-        sidx ^= (Tj);                        \
+    if (MODE == 2) {
+#pragma unroll
+        for (int k = 0; k < K; k++) PQ_REC(k)
     }
     for (uint32_t g = 0;; ++g) {
-        PQ_EVAL();
-        PQ_STEP(0, L0p, G0, T0);
-        PQ_EVAL();
-        PQ_STEP(1, L1p, G1, T1);
-        PQ_EVAL();
-        PQ_STEP(0, L0m, G0, T0);
-        PQ_EVAL();
-        PQ_STEP(2, ((sidx >> 2) & 1u) ? L2m : L2p, G2, T2);
-        PQ_EVAL();
-        PQ_STEP(0, L0p, G0, T0);
-        PQ_EVAL();
-        PQ_STEP(1, L1m, G1, T1);
-        PQ_EVAL();
-        PQ_STEP(0, L0m, G0, T0);
-        PQ_EVAL();
+        PQ_ROT(T0, r0[k].x, r0[k].y, Lp0 + ((Pc[k] & 1u) << 1));
+        PQ_ROT(T1, r1[k].x, r1[k].y, Lp1 + (Pc[k] & 2u));
+        PQ_ROT(T0, r0[k].x, -r0[k].y, 0u - (Lp0 + ((Pc[k] & 1u) << 1)));
+        {
+            const bool up = (sidx ^ T2) & 4u;
+            PQ_ROT(T2, r2[k].x, up ? r2[k].y : -r2[k].y,
+                   up ? Lp2 + ((Pc[k] >> 1) & 2u) : 0u - (Lp2 + ((Pc[k] >> 1) & 2u)));
+        }
+        PQ_ROT(T0, r0[k].x, r0[k].y, Lp0 + ((Pc[k] & 1u) << 1));
+        PQ_ROT(T1, r1[k].x, -r1[k].y, 0u - (Lp1 + (Pc[k] & 2u)));
+        PQ_ROT(T0, r0[k].x, -r0[k].y, 0u - (Lp0 + ((Pc[k] & 1u) << 1)));
         if (g + 1 == ngroups) break;
         const int j = 3 + ctz32(g + 1);
-        PQ_STEP(j, ((sidx >> j) & 1u) ? (uint32_t)Lm[j] : (uint32_t)Lp[j], Gi[j], Tg[j]);
+        const uint32_t down = (sidx >> j) & 1u;  // bit j is set before a down flip
+        float2 rj[K];
+        uint32_t Dj[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const uint32_t Lj = (uint32_t)Lp[j] + (((Pc[k] >> j) & 1u) << 1);
+            Dj[k] = down ? 0u - Lj : Lj;
+            rj[k] = quarter_turn(Dj[k]);
+        }
+        PQ_ROT(Tg[j], rj[k].x, rj[k].y, Dj[k]);
     }
-#undef PQ_EVAL
-#undef PQ_STEP
+#undef PQ_ROT
+#undef PQ_REC
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        acc[k][0] = hr[k]; acc[k][1] = hi[k]; acc[k][2] = lr[k]; acc[k][3] = li[k];
+    }
 }
 
 // MODE 0: FP32 weights, compensated accumulation.  MODE 1: FP64 weights and accumulation.
@@ -219,20 +260,12 @@ __global__ void __launch_bounds__(256, MINB) enum_kernel(KArgs a) {
     __shared__ uint64_t sR[8][64];
     __shared__ uint8_t sLp[8][64];
     __shared__ uint8_t sLm[8][64];
-    __shared__ uint32_t sGi[8][32];  // G_j restricted to the inner coordinates (< dl)
     __shared__ uint32_t sTg[8][32];  // (1 << j) | (R_j << DI)
-    __shared__ float2 sCS[4];        // (cos, sin)(m pi/2)
-    if (threadIdx.x < 4) {
-        const float cv[4] = {1.f, 0.f, -1.f, 0.f}, sv[4] = {0.f, 1.f, 0.f, -1.f};
-        sCS[threadIdx.x] = make_float2(cv[threadIdx.x], sv[threadIdx.x]);
-    }
-    __syncthreads();
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     uint64_t *G = sG[wib];
     uint64_t *R = sR[wib];
     uint8_t *Lp = sLp[wib];
     uint8_t *Lm = sLm[wib];
-    uint32_t *Gi = sGi[wib];
     uint32_t *Tg = sTg[wib];
     int cur_k = -1;  // position (item order) of the job whose data is staged
     long long kbeg = 0, kend = 0;
@@ -254,16 +287,13 @@ __global__ void __launch_bounds__(256, MINB) enum_kernel(KArgs a) {
             const JobDev &J = a.jobs[jb];
             const EngineDev &E = a.engines[J.engine];
             __syncwarp();
-            const int dlj = a.jdl[jb];
+            const int dlj = a.jdl[jb] & 255;
             for (int j = lane; j < E.d; j += 32) {
                 G[j] = E.G[j];
                 R[j] = E.R[j];
                 Lp[j] = J.Lp[j];
                 Lm[j] = (uint8_t)((4u - J.Lp[j]) & 3u);
-                if (j < dlj) {
-                    Gi[j] = (uint32_t)(E.G[j] & ((1ull << dlj) - 1ull));
-                    Tg[j] = (1u << j) | ((uint32_t)E.R[j] << E.DI);
-                }
+                if (j < dlj) Tg[j] = (1u << j) | ((uint32_t)E.R[j] << E.DI);
             }
             __syncwarp();
         }
@@ -273,73 +303,129 @@ __global__ void __launch_bounds__(256, MINB) enum_kernel(KArgs a) {
         const long long iin = it - kbeg;
         double accx = 0.0, accy = 0.0;
         if (!J.vanish) {
-            const int dl = a.jdl[job];
+            const int dl = a.jdl[job] & 255;
+            const int pb = (a.jdl[job] >> 8) - 1;  // bit of the pair coordinate in the chunk index
             const unsigned cpi = a.jcpi[job];
-            const unsigned long long nch = a.jnch[job];
+            const unsigned long long nun = a.jnch[job];
             const unsigned long long c0 = (unsigned long long)iin * cpi;
             unsigned long long cend = c0 + cpi;
-            if (cend > nch) cend = nch;
+            if (cend > nun) cend = nun;
             const uint64_t lomask = (E.DI >= 64) ? ~0ull : ((1ull << E.DI) - 1ull);
+            const uint64_t himask = ~lomask;
             const uint32_t steps = 1u << dl;
-            for (unsigned long long ch = c0 + lane; ch < cend; ch += 32) {
-                const uint64_t s = (uint64_t)ch << dl;
-                uint32_t m;
-                uint64_t yy;
-                chunk_start(Lp, G, R, J.y0, s, m, yy);
-                uint64_t ss = s;
-                double vx, vy;  // the chunk's sum before the weight of the coordinates >= DI
-                if (MODE == 1 || !E.joint) {
-                    // FP64 weights and accumulation (verification mode, and engines with more
-                    // pivots than the joint table holds)
-                    double sx = 0.0, sy = 0.0;
-                    for (uint32_t i = 1;; ++i) {
-                        if (MODE == 2) a.dbg[ss] = (uint8_t)((J.k0 + 2u * m) & 7u);
-                        double2 w = E.tlo64[ss & lomask];
-                        for (int sl = 0; sl < E.nsl_tp; sl++) w = cmul_d(w, E.tp64[sl * 256 + (int)((yy >> (8 * sl)) & 255ull)]);
-                        w = rot4d(w, m & 3u);
-                        sx += w.x;
-                        sy += w.y;
-                        if (i == steps) break;
-                        const int j = ctz32(i);
-                        m += (((ss >> j) & 1ull) ? Lm[j] : Lp[j]) + 2u * (uint32_t)(popc64(G[j] & ss) & 1);
-                        ss ^= 1ull << j;
-                        yy ^= R[j];
+            for (unsigned long long un = c0 + lane; un < cend; un += 32) {
+                // unit -> first chunk (a zero inserted at the pair bit) and the pair offset
+                const unsigned long long ch =
+                    pb < 0 ? un : (((un >> pb) << (pb + 1)) | (un & ((1ull << pb) - 1ull)));
+                const uint64_t s1 = (uint64_t)ch << dl;
+                const uint64_t sp = pb < 0 ? 0ull : (1ull << (pb + dl));
+                if (MODE != 1 && E.joint && dl >= 3) {
+                    // FP32 rotating-frame walk over the sign-folded joint table: the folded start
+                    // index and c_j of the walked coordinates (high coordinates only)
+                    uint32_t m1;
+                    uint64_t yy;
+                    chunk_start(Lp, G, R, J.y0, s1, m1, yy);
+                    m1 -= 2u * quad_parity(G, s1 & lomask);
+                    uint32_t P1 = 0;
+                    for (int j = 0; j < dl; j++) P1 |= (uint32_t)(popc64(G[j] & s1 & himask) & 1) << j;
+                    const uint32_t sidx = (uint32_t)((yy << E.DI) | (s1 & lomask));
+                    const int jl = dl - 1;
+                    if (pb >= 0) {
+                        const int pc = E.pairc;
+                        const uint32_t m2 = m1 + (uint32_t)Lp[pc] + 2u * (uint32_t)(popc64(G[pc] & s1) & 1);
+                        const uint32_t P2 = P1 ^ (uint32_t)(G[pc] & (uint64_t)(steps - 1u));
+                        uint32_t Pc[2] = {P1, P2};
+                        uint32_t mm[2] = {m1, m2};
+                        const uint64_t sb[2] = {s1, s1 | sp};
+                        float acc[2][4];
+                        gray_chunk_rot<MODE, 2>(E.wtab, sidx, Pc, Tg, Lp, dl, acc, a.dbg, sb, J.k0, mm, G,
+                                                (uint32_t)lomask);
+                        const uint32_t me[2] = {m1, m2};
+#pragma unroll
+                        for (int k = 0; k < 2; k++) {
+                            // S = i^{m_end} A
+                            const float2 r = quarter_turn(me[k] + (uint32_t)Lp[jl] + (((Pc[k] >> jl) & 1u) << 1));
+                            const double ax = (double)acc[k][0] + (double)acc[k][2];
+                            const double ay = (double)acc[k][1] + (double)acc[k][3];
+                            const double vx = (double)r.x * ax - (double)r.y * ay;
+                            const double vy = (double)r.y * ax + (double)r.x * ay;
+                            const double2 chi = chunk_high_weight(E, sb[k]);
+                            accx += vx * chi.x - vy * chi.y;
+                            accy += vx * chi.y + vy * chi.x;
+                        }
+                    } else {
+                        uint32_t Pc[1] = {P1};
+                        uint32_t mm[1] = {m1};
+                        const uint64_t sb[1] = {s1};
+                        float acc[1][4];
+                        gray_chunk_rot<MODE, 1>(E.wtab, sidx, Pc, Tg, Lp, dl, acc, a.dbg, sb, J.k0, mm, G,
+                                                (uint32_t)lomask);
+                        const float2 r = quarter_turn(m1 + (uint32_t)Lp[jl] + (((P1 >> jl) & 1u) << 1));
+                        const double ax = (double)acc[0][0] + (double)acc[0][2];
+                        const double ay = (double)acc[0][1] + (double)acc[0][3];
+                        const double vx = (double)r.x * ax - (double)r.y * ay;
+                        const double vy = (double)r.y * ax + (double)r.x * ay;
+                        const double2 chi = chunk_high_weight(E, s1);
+                        accx += vx * chi.x - vy * chi.y;
+                        accy += vx * chi.y + vy * chi.x;
                     }
-                    vx = sx;
-                    vy = sy;
-                } else if (dl >= 3) {
-                    // FP32, unrolled Gray walk with exact hi sums (gray_chunk8)
-                    float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-                    uint32_t sidx = (uint32_t)((yy << E.DI) | (s & lomask));
-                    uint32_t P = 0;
-                    for (int j = 0; j < dl; j++) P |= (uint32_t)(popc64(G[j] & s) & 1) << j;
-                    gray_chunk8<MODE>(E.wtab, sCS, m, sidx, P, Gi, Tg, Lp, Lm, dl, acc, a.dbg, s, J.k0);
-                    vx = ((double)acc[0] + (double)acc[4]) - ((double)acc[3] + (double)acc[7]);
-                    vy = ((double)acc[1] + (double)acc[5]) + ((double)acc[2] + (double)acc[6]);
-                } else {
-                    // FP32 for chunks of fewer than 8 steps: hi parts with TwoSum, lo parts plain
-                    float ax = 0.f, ay = 0.f, cx = 0.f, cy = 0.f, lx = 0.f, ly = 0.f;
-                    const float4 *__restrict__ W = E.wtab;
-                    const int DI = E.DI;
-                    for (uint32_t i = 1;; ++i) {
-                        if (MODE == 2) a.dbg[ss] = (uint8_t)((J.k0 + 2u * m) & 7u);
-                        const float4 w = rot4q(__ldg(&W[(yy << DI) | (ss & lomask)]), m & 3u);
-                        two_sum_acc(ax, cx, w.x);
-                        two_sum_acc(ay, cy, w.y);
-                        lx += w.z;
-                        ly += w.w;
-                        if (i == steps) break;
-                        const int j = ctz32(i);
-                        m += (((ss >> j) & 1ull) ? Lm[j] : Lp[j]) + 2u * (uint32_t)(popc64(G[j] & ss) & 1);
-                        ss ^= 1ull << j;
-                        yy ^= R[j];
-                    }
-                    vx = (double)ax + (double)cx + (double)lx;
-                    vy = (double)ay + (double)cy + (double)ly;
+                    continue;
                 }
-                const double2 chi = chunk_high_weight(E, s);
-                accx += vx * chi.x - vy * chi.y;
-                accy += vx * chi.y + vy * chi.x;
+                for (int kc = 0; kc < (pb < 0 ? 1 : 2); kc++) {
+                    const uint64_t s = s1 | (kc ? sp : 0ull);
+                    uint32_t m;
+                    uint64_t yy;
+                    chunk_start(Lp, G, R, J.y0, s, m, yy);
+                    uint64_t ss = s;
+                    double vx, vy;  // the chunk's sum before the weight of the coordinates >= DI
+                    if (MODE == 1 || !E.joint) {
+                        // FP64 weights and accumulation (verification mode, and engines with more
+                        // pivots than the joint table holds)
+                        double sx = 0.0, sy = 0.0;
+                        for (uint32_t i = 1;; ++i) {
+                            if (MODE == 2) a.dbg[ss] = (uint8_t)((J.k0 + 2u * m) & 7u);
+                            double2 w = E.tlo64[ss & lomask];
+                            for (int sl = 0; sl < E.nsl_tp; sl++)
+                                w = cmul_d(w, E.tp64[sl * 256 + (int)((yy >> (8 * sl)) & 255ull)]);
+                            w = rot4d(w, m & 3u);
+                            sx += w.x;
+                            sy += w.y;
+                            if (i == steps) break;
+                            const int j = ctz32(i);
+                            m += (((ss >> j) & 1ull) ? Lm[j] : Lp[j]) + 2u * (uint32_t)(popc64(G[j] & ss) & 1);
+                            ss ^= 1ull << j;
+                            yy ^= R[j];
+                        }
+                        vx = sx;
+                        vy = sy;
+                    } else {
+                        // FP32, chunks of fewer than 8 steps: per-branch folded index over the
+                        // sign-folded table, plain sums
+                        m -= 2u * quad_parity(G, s & lomask);
+                        float hx = 0.f, hy = 0.f, lx = 0.f, ly = 0.f;
+                        const float4 *__restrict__ W = E.wtab;
+                        const int DI = E.DI;
+                        for (uint32_t i = 1;; ++i) {
+                            if (MODE == 2)
+                                a.dbg[ss] = (uint8_t)((J.k0 + 2u * (m + 2u * quad_parity(G, ss & lomask))) & 7u);
+                            const float4 w = rot4q(__ldg(&W[(yy << DI) | (ss & lomask)]), m & 3u);
+                            hx += w.x;
+                            hy += w.y;
+                            lx += w.z;
+                            ly += w.w;
+                            if (i == steps) break;
+                            const int j = ctz32(i);
+                            m += (((ss >> j) & 1ull) ? Lm[j] : Lp[j]) + 2u * (uint32_t)(popc64(G[j] & ss & himask) & 1);
+                            ss ^= 1ull << j;
+                            yy ^= R[j];
+                        }
+                        vx = (double)hx + (double)lx;
+                        vy = (double)hy + (double)ly;
+                    }
+                    const double2 chi = chunk_high_weight(E, s);
+                    accx += vx * chi.x - vy * chi.y;
+                    accy += vx * chi.y + vy * chi.x;
+                }
             }
         }
         for (int o = 16; o; o >>= 1) {
@@ -386,7 +472,7 @@ __global__ void job_reduce_kernel(KArgs a) {
         //  by <= n u * (u sum|c|); FP64 chunk scaling and reductions by a few 2^-52.
         //  FP64 path: (n + 2 * nsl_tp + 8) 2^-53.
         const double u32 = 5.9604644775390625e-08, u64 = 1.1102230246251565e-16;
-        const double n = (double)(1ull << a.jdl[j]);
+        const double n = (double)(1ull << (a.jdl[j] & 255));
         double rel;
         if (E.joint) {
             const double g = n * u32 / (1.0 - n * u32);
