@@ -213,6 +213,10 @@ PQ_API pq_status pq_measure_peaks(double out[4]);
 /* Canonical dump of branch engine `branch`: normal form, diagonal masks, kernel and
  * boundary columns, RREF; returns the word count (out = NULL to size), < 0 on error. */
 PQ_API int64_t pq_debug_engine_dump(const pq_sim *sim, int32_t branch, uint64_t *out, int64_t cap);
+/* Shape of branch engine `branch`: out[0] d, [1] pivots, [2] low coordinates of the weight
+ * table, [3] joint table (1/0), [4] pair coordinate (-1 none), [5] coordinates touching no
+ * pivot, [6] of which high (>= out[2]), [7] terms. */
+PQ_API pq_status pq_debug_engine_shape(const pq_sim *sim, int32_t branch, int64_t out[8]);
 /* Z8 index of every branch s < 2^d of branch engine `branch` for boundary (x, y), as the
  * enumeration kernel computes it on the device.  Returns d, or -1 (vanishing boundary),
  * or -2 (error). */

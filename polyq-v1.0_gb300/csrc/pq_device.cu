@@ -1057,6 +1057,23 @@ PQ_API int64_t pq_debug_engine_dump(const pq_sim *s, int32_t branch, uint64_t *o
     return (int64_t)v.size();
 }
 
+PQ_API pq_status pq_debug_engine_shape(const pq_sim *s, int32_t branch, int64_t *out) {
+    if (!s || !out || branch < 0 || branch >= (int)s->main.rs.branches.size())
+        return fail(PQ_ERR_INVALID_ARG, "bad simulator or branch");
+    const HostEngine &e = *s->main.rs.branches[branch];
+    EngineTables tb = build_tables(e, s->di_max);
+    PackedEngine pk = pack_engine(e, tb);
+    int64_t r0 = 0, r0hi = 0;
+    for (int j = 0; j < e.d; j++)
+        if (e.R[(size_t)j] == 0) {
+            r0++;
+            if (j >= tb.DI) r0hi++;
+        }
+    const int64_t v[8] = {e.d, e.rank, tb.DI, tb.joint ? 1 : 0, pk.off.pairc, r0, r0hi, e.t};
+    for (int i = 0; i < 8; i++) out[i] = v[i];
+    return PQ_OK;
+}
+
 PQ_API int32_t pq_debug_branch_phases(pq_sim *s, int32_t branch, const uint64_t *x, const uint64_t *y, uint8_t *out) {
     if (!s || !x || !y || !out || branch < 0 || branch >= (int)s->main.rs.branches.size()) {
         g_err = "bad argument";

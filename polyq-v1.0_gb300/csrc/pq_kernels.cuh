@@ -162,32 +162,54 @@ __device__ __forceinline__ uint32_t quad_parity(const uint64_t *G, uint64_t x) {
 // With m_k the (folded) index of the k-th branch, the walk keeps A_k = i^{-m_k} sum_{l<=k}
 // i^{m_l} w_l, so that A_{k+1} = i^{-Delta_k} A_k + w_{k+1}: each step is a quarter-turn of the
 // accumulator by a per-chunk constant plus the table entry, with no per-branch phase arithmetic.
-// A quarter-turn has coefficients 0/+-1: hi sums stay exact multiples of the table grid, lo sums
-// are plain FP32.  The K chunks of a unit differ only in coordinates that touch no pivot, so
-// they read the same table entry at every step (one load feeds K accumulators); they differ in
-// their c_j.  Unrolled by 8: coordinates 0 and 1 flip at fixed positions with fixed directions
-// (0+, 1+, 0-, 0+, 1-, 0-), coordinate 2 once per group with the group's direction, and the
-// group boundary flips coordinate 3 + ctz(g+1).
+// The parity of Delta on coordinate j is that of Lp_j, the same for every boundary of an engine,
+// so it is a compile-time case (PAR, bit j for j < 3): an even step is A <- rho A + w, an odd one
+// (re, im) <- rho (im, -re) + w, with rho = +-1 from bit 1 of L'_j (negated on an odd down-flip).
+// Either is two FFMA per complex number, exact on the hi parts (multiples of the table grid).
+// The K chunks of a unit differ only in coordinates that touch no pivot, so they read the same
+// table entry at every step (one load feeds K accumulators); they differ in their c_j.
+// Unrolled by 8: coordinates 0 and 1 flip at fixed positions with fixed directions (0+, 1+, 0-,
+// 0+, 1-, 0-), coordinate 2 once per group with the group's direction, and the group boundary
+// flips coordinate 3 + ctz(g+1) (its parity is warp-uniform: a uniform branch).
 //   sidx   (pivot bits << DI) | low DI coordinates: the table index
 //   Pc[k]  bit j = c_j of chunk k for the walked coordinates
 //   T_j    (1 << j) | (R_j << DI): the change of sidx when coordinate j flips
 // On return acc[k] = (hi.re, hi.im, lo.re, lo.im) of chunk k's A at the last branch, whose
 // folded index is m[k] + L'_{dl-1} (the walk ends on the unit vector of coordinate dl-1).
-template <int MODE, int K>
+template <int ODD>
+__device__ __forceinline__ void qturn_add(float &hr, float &hi, float &lr, float &li, float rho, const float4 &w) {
+    if (ODD) {
+        const float t = hr, u = lr;
+        hr = fmaf(rho, hi, w.x);
+        hi = fmaf(-rho, t, w.y);
+        lr = fmaf(rho, li, w.z);
+        li = fmaf(-rho, u, w.w);
+    } else {
+        hr = fmaf(rho, hr, w.x);
+        hi = fmaf(rho, hi, w.y);
+        lr = fmaf(rho, lr, w.z);
+        li = fmaf(rho, li, w.w);
+    }
+}
+
+__device__ __forceinline__ float rho_of(uint32_t L) { return (L & 2u) ? -1.0f : 1.0f; }
+
+template <int MODE, int K, int PAR>
 __device__ __forceinline__ void gray_chunk_rot(const float4 *__restrict__ W, uint32_t sidx, const uint32_t (&Pc)[K],
                                                const uint32_t *Tg, const uint8_t *Lp, int dl, float (&acc)[K][4],
                                                uint8_t *dbg, const uint64_t (&sbase)[K], uint32_t k0,
                                                uint32_t (&m)[K], const uint64_t *G, uint32_t lomask) {
+    constexpr int O0 = PAR & 1, O1 = (PAR >> 1) & 1, O2 = (PAR >> 2) & 1;
     const uint32_t T0 = Tg[0], T1 = Tg[1], T2 = Tg[2];
     const uint32_t Lp0 = Lp[0], Lp1 = Lp[1], Lp2 = Lp[2];
-    float2 r0[K], r1[K], r2[K];
+    float p0[K], p1[K], p2[K];
     float hr[K], hi[K], lr[K], li[K];
     const float4 w0 = __ldg(&W[sidx]);
 #pragma unroll
     for (int k = 0; k < K; k++) {
-        r0[k] = quarter_turn(Lp0 + ((Pc[k] & 1u) << 1));
-        r1[k] = quarter_turn(Lp1 + (Pc[k] & 2u));
-        r2[k] = quarter_turn(Lp2 + ((Pc[k] >> 1) & 2u));
+        p0[k] = rho_of(Lp0 + ((Pc[k] & 1u) << 1));
+        p1[k] = rho_of(Lp1 + (Pc[k] & 2u));
+        p2[k] = rho_of(Lp2 + ((Pc[k] >> 1) & 2u));
         hr[k] = w0.x; hi[k] = w0.y; lr[k] = w0.z; li[k] = w0.w;
     }
     const uint32_t inner = (1u << dl) - 1u;
@@ -196,57 +218,70 @@ __device__ __forceinline__ void gray_chunk_rot(const float4 *__restrict__ W, uin
 #define PQ_REC(k)                                                                                        \
     if (MODE == 2)                                                                                       \
         dbg[sbase[k] | (sidx & inner)] = (uint8_t)((k0 + 2u * (m[k] + 2u * quad_parity(G, sidx & lomask))) & 7u);
-    // A <- i^{-D} A + w with (cos, sin)(D pi/2) = (c, sg):
-    // (c - i sg)(re + i im) = (c re + sg im) + i (c im - sg re)
-#define PQ_ROT(T, CS, SG, DM)                                            \
-    {                                                                    \
-        sidx ^= (T);                                                     \
-        const float4 w = __ldg(&W[sidx]);                                \
-        _Pragma("unroll") for (int k = 0; k < K; k++) {                  \
-            const float c = (CS), sg = (SG);                             \
-            const float nhr = fmaf(sg, hi[k], fmaf(c, hr[k], w.x));      \
-            const float nhi = fmaf(-sg, hr[k], fmaf(c, hi[k], w.y));     \
-            const float nlr = fmaf(sg, li[k], fmaf(c, lr[k], w.z));      \
-            const float nli = fmaf(-sg, lr[k], fmaf(c, li[k], w.w));     \
-            hr[k] = nhr; hi[k] = nhi; lr[k] = nlr; li[k] = nli;          \
-            if (MODE == 2) m[k] += (DM);                                 \
-            PQ_REC(k)                                                    \
-        }                                                                \
+    // flip by T, then A <- quarter-turn(A) + w for every chunk of the unit
+#define PQ_Q(ODD, T, RHO, DM)                                                     \
+    {                                                                             \
+        sidx ^= (T);                                                              \
+        const float4 w = __ldg(&W[sidx]);                                         \
+        _Pragma("unroll") for (int k = 0; k < K; k++) {                           \
+            qturn_add<ODD>(hr[k], hi[k], lr[k], li[k], (RHO), w);                 \
+            if (MODE == 2) m[k] += (DM);                                          \
+            PQ_REC(k)                                                             \
+        }                                                                         \
     }
     if (MODE == 2) {
 #pragma unroll
         for (int k = 0; k < K; k++) PQ_REC(k)
     }
+#define PQ_L0 (Lp0 + ((Pc[k] & 1u) << 1))
+#define PQ_L1 (Lp1 + (Pc[k] & 2u))
+#define PQ_L2 (Lp2 + ((Pc[k] >> 1) & 2u))
     for (uint32_t g = 0;; ++g) {
-        PQ_ROT(T0, r0[k].x, r0[k].y, Lp0 + ((Pc[k] & 1u) << 1));
-        PQ_ROT(T1, r1[k].x, r1[k].y, Lp1 + (Pc[k] & 2u));
-        PQ_ROT(T0, r0[k].x, -r0[k].y, 0u - (Lp0 + ((Pc[k] & 1u) << 1)));
+        PQ_Q(O0, T0, p0[k], PQ_L0);
+        PQ_Q(O1, T1, p1[k], PQ_L1);
+        PQ_Q(O0, T0, O0 ? -p0[k] : p0[k], 0u - PQ_L0);
         {
             const bool up = (sidx ^ T2) & 4u;
-            PQ_ROT(T2, r2[k].x, up ? r2[k].y : -r2[k].y,
-                   up ? Lp2 + ((Pc[k] >> 1) & 2u) : 0u - (Lp2 + ((Pc[k] >> 1) & 2u)));
+            PQ_Q(O2, T2, (O2 && !up) ? -p2[k] : p2[k], up ? PQ_L2 : 0u - PQ_L2);
         }
-        PQ_ROT(T0, r0[k].x, r0[k].y, Lp0 + ((Pc[k] & 1u) << 1));
-        PQ_ROT(T1, r1[k].x, -r1[k].y, 0u - (Lp1 + (Pc[k] & 2u)));
-        PQ_ROT(T0, r0[k].x, -r0[k].y, 0u - (Lp0 + ((Pc[k] & 1u) << 1)));
+        PQ_Q(O0, T0, p0[k], PQ_L0);
+        PQ_Q(O1, T1, O1 ? -p1[k] : p1[k], 0u - PQ_L1);
+        PQ_Q(O0, T0, O0 ? -p0[k] : p0[k], 0u - PQ_L0);
         if (g + 1 == ngroups) break;
         const int j = 3 + ctz32(g + 1);
         const uint32_t down = (sidx >> j) & 1u;  // bit j is set before a down flip
-        float2 rj[K];
-        uint32_t Dj[K];
-#pragma unroll
-        for (int k = 0; k < K; k++) {
-            const uint32_t Lj = (uint32_t)Lp[j] + (((Pc[k] >> j) & 1u) << 1);
-            Dj[k] = down ? 0u - Lj : Lj;
-            rj[k] = quarter_turn(Dj[k]);
+        const uint32_t Lpj = Lp[j];
+        if (Lpj & 1u) {
+            PQ_Q(1, Tg[j], down ? -rho_of(Lpj + (((Pc[k] >> j) & 1u) << 1)) : rho_of(Lpj + (((Pc[k] >> j) & 1u) << 1)),
+                 down ? 0u - (Lpj + (((Pc[k] >> j) & 1u) << 1)) : Lpj + (((Pc[k] >> j) & 1u) << 1));
+        } else {
+            PQ_Q(0, Tg[j], rho_of(Lpj + (((Pc[k] >> j) & 1u) << 1)),
+                 down ? 0u - (Lpj + (((Pc[k] >> j) & 1u) << 1)) : Lpj + (((Pc[k] >> j) & 1u) << 1));
         }
-        PQ_ROT(Tg[j], rj[k].x, rj[k].y, Dj[k]);
     }
-#undef PQ_ROT
+#undef PQ_L0
+#undef PQ_L1
+#undef PQ_L2
+#undef PQ_Q
 #undef PQ_REC
 #pragma unroll
     for (int k = 0; k < K; k++) {
         acc[k][0] = hr[k]; acc[k][1] = hi[k]; acc[k][2] = lr[k]; acc[k][3] = li[k];
+    }
+}
+
+// Dispatch on the parities of Lp_0..2 (an engine constant, warp-uniform).
+template <int MODE, int K>
+__device__ __forceinline__ void gray_chunk_rot_any(const float4 *__restrict__ W, uint32_t sidx, const uint32_t (&Pc)[K],
+                                                   const uint32_t *Tg, const uint8_t *Lp, int dl, float (&acc)[K][4],
+                                                   uint8_t *dbg, const uint64_t (&sbase)[K], uint32_t k0,
+                                                   uint32_t (&m)[K], const uint64_t *G, uint32_t lomask) {
+    const int par = (Lp[0] & 1) | ((Lp[1] & 1) << 1) | ((Lp[2] & 1) << 2);
+    switch (par) {
+#define PQ_CASE(P) \
+    case P: gray_chunk_rot<MODE, K, P>(W, sidx, Pc, Tg, Lp, dl, acc, dbg, sbase, k0, m, G, lomask); break;
+        PQ_CASE(0) PQ_CASE(1) PQ_CASE(2) PQ_CASE(3) PQ_CASE(4) PQ_CASE(5) PQ_CASE(6) PQ_CASE(7)
+#undef PQ_CASE
     }
 }
 
@@ -338,7 +373,7 @@ __global__ void __launch_bounds__(256, MINB) enum_kernel(KArgs a) {
                         uint32_t mm[2] = {m1, m2};
                         const uint64_t sb[2] = {s1, s1 | sp};
                         float acc[2][4];
-                        gray_chunk_rot<MODE, 2>(E.wtab, sidx, Pc, Tg, Lp, dl, acc, a.dbg, sb, J.k0, mm, G,
+                        gray_chunk_rot_any<MODE, 2>(E.wtab, sidx, Pc, Tg, Lp, dl, acc, a.dbg, sb, J.k0, mm, G,
                                                 (uint32_t)lomask);
                         const uint32_t me[2] = {m1, m2};
 #pragma unroll
@@ -358,7 +393,7 @@ __global__ void __launch_bounds__(256, MINB) enum_kernel(KArgs a) {
                         uint32_t mm[1] = {m1};
                         const uint64_t sb[1] = {s1};
                         float acc[1][4];
-                        gray_chunk_rot<MODE, 1>(E.wtab, sidx, Pc, Tg, Lp, dl, acc, a.dbg, sb, J.k0, mm, G,
+                        gray_chunk_rot_any<MODE, 1>(E.wtab, sidx, Pc, Tg, Lp, dl, acc, a.dbg, sb, J.k0, mm, G,
                                                 (uint32_t)lomask);
                         const float2 r = quarter_turn(m1 + (uint32_t)Lp[jl] + (((P1 >> jl) & 1u) << 1));
                         const double ax = (double)acc[0][0] + (double)acc[0][2];

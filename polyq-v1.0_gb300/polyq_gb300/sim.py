@@ -152,6 +152,13 @@ class Simulator:
         N.check(self._L.pq_sim_get_tuning(self._h, ct.byref(t)))
         return {k: getattr(t, k) for k, _ in N.Tuning._fields_}
 
+    def engine_shape(self, branch: int) -> dict:
+        """d, pivots, table low coordinates, joint table, pair coordinate, pivot-free coordinates."""
+        out = np.zeros(8, dtype=np.int64)
+        N.check(self._L.pq_debug_engine_shape(self._h, branch, _p(out, ct.c_int64)))
+        keys = ("d", "rank", "DI", "joint", "pairc", "free_of_pivots", "free_of_pivots_high", "terms")
+        return dict(zip(keys, (int(v) for v in out)))
+
     def amplitudes_fp64(self, inputs, outputs):
         xs = pack_bits(inputs, self.num_qubits)
         ys = pack_bits(outputs, self.num_qubits)
