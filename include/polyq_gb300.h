@@ -76,7 +76,7 @@ typedef struct pq_tuning {
     int32_t chunks_per_lane; /* chunks a lane walks per work item (1..64) */
     int32_t block_warps;     /* warps per CTA of the enumeration kernel (1..8) */
     int32_t max_branch_dim;  /* admission cap on d per branch engine (<= 62) */
-    int32_t blocks_per_sm;   /* enumeration kernel register budget: 3 (80 regs) or 4 (64 regs) blocks */
+    int32_t blocks_per_sm;   /* enumeration kernel register budget: 2, 3 or 4 blocks of 256 per SM */
 } pq_tuning;
 
 /* ---- library ------------------------------------------------------------------------ */

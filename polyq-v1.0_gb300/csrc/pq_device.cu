@@ -341,9 +341,10 @@ static pq_status build_plan(const std::vector<Segment> &segs, int nw, cudaStream
     a.errflag = P.errflag.as<int>();
     const int bw = std::max(1, std::min(8, tu.block_warps));
     P.block_enum = 32 * bw;
-    P.minb = tu.blocks_per_sm == 4 ? 4 : 3;
+    P.minb = (tu.blocks_per_sm >= 2 && tu.blocks_per_sm <= 4) ? tu.blocks_per_sm : 3;
     int occ = 0;
     if (P.minb == 4) CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, enum_kernel<0, 4>, P.block_enum, 0));
+    else if (P.minb == 2) CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, enum_kernel<0, 2>, P.block_enum, 0));
     else CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, enum_kernel<0, 3>, P.block_enum, 0));
     occ = std::max(occ, 1);
     long long want = (long long)sm_count() * occ;
@@ -372,6 +373,7 @@ static cudaError_t enqueue_core(Plan &P, int mode) {
     if ((e = cudaEventRecordWithFlags(P.tev[1], P.stream, evflag)) != cudaSuccess) return e;
     if (mode == 1) enum_kernel<1><<<P.grid_enum, P.block_enum, 0, P.stream>>>(P.args);
     else if (P.minb == 4) enum_kernel<0, 4><<<P.grid_enum, P.block_enum, 0, P.stream>>>(P.args);
+    else if (P.minb == 2) enum_kernel<0, 2><<<P.grid_enum, P.block_enum, 0, P.stream>>>(P.args);
     else enum_kernel<0, 3><<<P.grid_enum, P.block_enum, 0, P.stream>>>(P.args);
     if ((e = cudaEventRecordWithFlags(P.tev[2], P.stream, evflag)) != cudaSuccess) return e;
     job_reduce_kernel<<<(P.njobs + 255) / 256, 256, 0, P.stream>>>(P.args);
@@ -557,7 +559,7 @@ PQ_API pq_status pq_set_default_tuning(const pq_tuning *t) {
         n.max_branch_dim = t->max_branch_dim;
     }
     if (t->blocks_per_sm) {
-        if (t->blocks_per_sm != 3 && t->blocks_per_sm != 4) return fail(PQ_ERR_INVALID_ARG, "blocks_per_sm is 3 or 4");
+        if (t->blocks_per_sm < 2 || t->blocks_per_sm > 4) return fail(PQ_ERR_INVALID_ARG, "blocks_per_sm is 2, 3 or 4");
         n.blocks_per_sm = t->blocks_per_sm;
     }
     g_tuning = n;
@@ -986,7 +988,7 @@ PQ_API pq_status pq_sim_autotune(pq_sim *s, int64_t n, const uint64_t *x, const 
     // candidate values per field; the search starts from the simulator's current tuning.  Lane
     // chunks stop at 2^10 steps: the plain-FP32 low-part sums lose accuracy as 4^inner_dims
     // (more terms on a coarser exact grid), and 2^12 already costs an order of magnitude.
-    const std::vector<int> axes[4] = {{8, 9, 10}, {1, 2, 4, 8, 16}, {2, 4, 8}, {3, 4}};
+    const std::vector<int> axes[4] = {{8, 9, 10}, {1, 2, 4, 8, 16}, {2, 4, 8}, {2, 3, 4}};
     auto field = [](pq_tuning &t, int k) -> int32_t & {
         return k == 0 ? t.inner_dims : k == 1 ? t.chunks_per_lane : k == 2 ? t.block_warps : t.blocks_per_sm;
     };

@@ -287,8 +287,8 @@ __device__ __forceinline__ void gray_chunk_rot_any(const float4 *__restrict__ W,
 
 // MODE 0: FP32 weights, compensated accumulation.  MODE 1: FP64 weights and accumulation.
 // MODE 2: record the Z8 index of every branch into dbg (single-job debug launches).
-// MINB: resident blocks per SM the register allocation is sized for (3: 80 registers, no
-// spills; 4: 64 registers) -- chosen per launch by measurement.
+// MINB: resident blocks of 256 threads per SM the register allocation is sized for (2: 128,
+// 3: 80, 4: 64 registers per thread) -- chosen per launch by measurement.
 template <int MODE, int MINB = 3>
 __global__ void __launch_bounds__(256, MINB) enum_kernel(KArgs a) {
     __shared__ uint64_t sG[8][64];
@@ -339,7 +339,9 @@ __global__ void __launch_bounds__(256, MINB) enum_kernel(KArgs a) {
         double accx = 0.0, accy = 0.0;
         if (!J.vanish) {
             const int dl = a.jdl[job] & 255;
-            const int pb = (a.jdl[job] >> 8) - 1;  // bit of the pair coordinate in the chunk index
+            const int pb1 = ((a.jdl[job] >> 8) & 255) - 1;  // bits of the pair coordinates in the
+            const int pb2 = ((a.jdl[job] >> 16) & 255) - 1;  // chunk index (-1: none)
+            const int nk = pb1 < 0 ? 1 : (pb2 < 0 ? 2 : 4);
             const unsigned cpi = a.jcpi[job];
             const unsigned long long nun = a.jnch[job];
             const unsigned long long c0 = (unsigned long long)iin * cpi;
@@ -348,12 +350,14 @@ __global__ void __launch_bounds__(256, MINB) enum_kernel(KArgs a) {
             const uint64_t lomask = (E.DI >= 64) ? ~0ull : ((1ull << E.DI) - 1ull);
             const uint64_t himask = ~lomask;
             const uint32_t steps = 1u << dl;
+            const uint64_t e1 = pb1 < 0 ? 0ull : (1ull << (pb1 + dl));  // = 1 << pairc
+            const uint64_t e2 = pb2 < 0 ? 0ull : (1ull << (pb2 + dl));  // = 1 << pairc2
             for (unsigned long long un = c0 + lane; un < cend; un += 32) {
-                // unit -> first chunk (a zero inserted at the pair bit) and the pair offset
-                const unsigned long long ch =
-                    pb < 0 ? un : (((un >> pb) << (pb + 1)) | (un & ((1ull << pb) - 1ull)));
+                // unit -> its first chunk (zeros inserted at the pair bits)
+                unsigned long long ch = un;
+                if (pb1 >= 0) ch = insert_zero(ch, pb1);
+                if (pb2 >= 0) ch = insert_zero(ch, pb2);
                 const uint64_t s1 = (uint64_t)ch << dl;
-                const uint64_t sp = pb < 0 ? 0ull : (1ull << (pb + dl));
                 if (MODE != 1 && E.joint && dl >= 3) {
                     // FP32 rotating-frame walk over the sign-folded joint table: the folded start
                     // index and c_j of the walked coordinates (high coordinates only)
@@ -364,50 +368,60 @@ __global__ void __launch_bounds__(256, MINB) enum_kernel(KArgs a) {
                     uint32_t P1 = 0;
                     for (int j = 0; j < dl; j++) P1 |= (uint32_t)(popc64(G[j] & s1 & himask) & 1) << j;
                     const uint32_t sidx = (uint32_t)((yy << E.DI) | (s1 & lomask));
-                    const int jl = dl - 1;
-                    if (pb >= 0) {
-                        const int pc = E.pairc;
-                        const uint32_t m2 = m1 + (uint32_t)Lp[pc] + 2u * (uint32_t)(popc64(G[pc] & s1) & 1);
-                        const uint32_t P2 = P1 ^ (uint32_t)(G[pc] & (uint64_t)(steps - 1u));
-                        uint32_t Pc[2] = {P1, P2};
-                        uint32_t mm[2] = {m1, m2};
-                        const uint64_t sb[2] = {s1, s1 | sp};
+                    const uint32_t wmask = steps - 1u;
+#define PQ_FINISH(K)                                                                                      \
+    _Pragma("unroll") for (int k = 0; k < K; k++) {                                                       \
+        /* S = i^{m_end} A, m_end = m + L'_{dl-1} */                                                      \
+        const int jl = dl - 1;                                                                            \
+        const float2 r = quarter_turn(me[k] + (uint32_t)Lp[jl] + (((Pc[k] >> jl) & 1u) << 1));            \
+        const double ax = (double)acc[k][0] + (double)acc[k][2];                                          \
+        const double ay = (double)acc[k][1] + (double)acc[k][3];                                          \
+        const double vx = (double)r.x * ax - (double)r.y * ay;                                            \
+        const double vy = (double)r.y * ax + (double)r.x * ay;                                            \
+        const double2 chi = chunk_high_weight(E, sb[k]);                                                  \
+        accx += vx * chi.x - vy * chi.y;                                                                  \
+        accy += vx * chi.y + vy * chi.x;                                                                  \
+    }
+                    if (nk == 4) {
+                        const int p1 = E.pairc, p2 = E.pairc2;
+                        const uint32_t d1 = (uint32_t)Lp[p1] + 2u * (uint32_t)(popc64(G[p1] & s1) & 1);
+                        const uint32_t d2 = (uint32_t)Lp[p2] + 2u * (uint32_t)(popc64(G[p2] & s1) & 1);
+                        const uint32_t d12 = 2u * (uint32_t)((G[p2] >> p1) & 1ull);
+                        const uint32_t g1 = (uint32_t)G[p1] & wmask, g2 = (uint32_t)G[p2] & wmask;
+                        const uint32_t me[4] = {m1, m1 + d1, m1 + d2, m1 + d1 + d2 + d12};
+                        uint32_t Pc[4] = {P1, P1 ^ g1, P1 ^ g2, P1 ^ g1 ^ g2};
+                        uint32_t mm[4] = {me[0], me[1], me[2], me[3]};
+                        const uint64_t sb[4] = {s1, s1 | e1, s1 | e2, s1 | e1 | e2};
+                        float acc[4][4];
+                        gray_chunk_rot_any<MODE, 4>(E.wtab, sidx, Pc, Tg, Lp, dl, acc, a.dbg, sb, J.k0, mm, G,
+                                                    (uint32_t)lomask);
+                        PQ_FINISH(4)
+                    } else if (nk == 2) {
+                        const int p1 = E.pairc;
+                        const uint32_t d1 = (uint32_t)Lp[p1] + 2u * (uint32_t)(popc64(G[p1] & s1) & 1);
+                        const uint32_t me[2] = {m1, m1 + d1};
+                        uint32_t Pc[2] = {P1, P1 ^ ((uint32_t)G[p1] & wmask)};
+                        uint32_t mm[2] = {me[0], me[1]};
+                        const uint64_t sb[2] = {s1, s1 | e1};
                         float acc[2][4];
                         gray_chunk_rot_any<MODE, 2>(E.wtab, sidx, Pc, Tg, Lp, dl, acc, a.dbg, sb, J.k0, mm, G,
-                                                (uint32_t)lomask);
-                        const uint32_t me[2] = {m1, m2};
-#pragma unroll
-                        for (int k = 0; k < 2; k++) {
-                            // S = i^{m_end} A
-                            const float2 r = quarter_turn(me[k] + (uint32_t)Lp[jl] + (((Pc[k] >> jl) & 1u) << 1));
-                            const double ax = (double)acc[k][0] + (double)acc[k][2];
-                            const double ay = (double)acc[k][1] + (double)acc[k][3];
-                            const double vx = (double)r.x * ax - (double)r.y * ay;
-                            const double vy = (double)r.y * ax + (double)r.x * ay;
-                            const double2 chi = chunk_high_weight(E, sb[k]);
-                            accx += vx * chi.x - vy * chi.y;
-                            accy += vx * chi.y + vy * chi.x;
-                        }
+                                                    (uint32_t)lomask);
+                        PQ_FINISH(2)
                     } else {
+                        const uint32_t me[1] = {m1};
                         uint32_t Pc[1] = {P1};
                         uint32_t mm[1] = {m1};
                         const uint64_t sb[1] = {s1};
                         float acc[1][4];
                         gray_chunk_rot_any<MODE, 1>(E.wtab, sidx, Pc, Tg, Lp, dl, acc, a.dbg, sb, J.k0, mm, G,
-                                                (uint32_t)lomask);
-                        const float2 r = quarter_turn(m1 + (uint32_t)Lp[jl] + (((P1 >> jl) & 1u) << 1));
-                        const double ax = (double)acc[0][0] + (double)acc[0][2];
-                        const double ay = (double)acc[0][1] + (double)acc[0][3];
-                        const double vx = (double)r.x * ax - (double)r.y * ay;
-                        const double vy = (double)r.y * ax + (double)r.x * ay;
-                        const double2 chi = chunk_high_weight(E, s1);
-                        accx += vx * chi.x - vy * chi.y;
-                        accy += vx * chi.y + vy * chi.x;
+                                                    (uint32_t)lomask);
+                        PQ_FINISH(1)
                     }
+#undef PQ_FINISH
                     continue;
                 }
-                for (int kc = 0; kc < (pb < 0 ? 1 : 2); kc++) {
-                    const uint64_t s = s1 | (kc ? sp : 0ull);
+                for (int kc = 0; kc < nk; kc++) {
+                    const uint64_t s = s1 | ((kc & 1) ? e1 : 0ull) | ((kc & 2) ? e2 : 0ull);
                     uint32_t m;
                     uint64_t yy;
                     chunk_start(Lp, G, R, J.y0, s, m, yy);

@@ -261,13 +261,13 @@ def test_autotune_keeps_results(gpu):
     tuning, ms = s.autotune([0] * 128, ys, reps=1)
     assert ms > 0.0
     assert s.tuning() == tuning
-    assert tuning["blocks_per_sm"] in (3, 4) and 8 <= tuning["inner_dims"] <= 10
+    assert tuning["blocks_per_sm"] in (2, 3, 4) and 8 <= tuning["inner_dims"] <= 10
     after, err = s.amplitudes([0] * 128, ys, with_error=True)
     scale = float(np.max(np.abs(before)))
     assert np.all(np.abs(after - before) <= err + 1e-12 * scale)
     want = O.OracleSim(c).amplitudes([0] * 24, ys[:24])
     assert_amps(after[:24], want, err[:24])
-    for bps in (3, 4):
+    for bps in (2, 3, 4):
         set_old = get_tuning()
         try:
             set_tuning(blocks_per_sm=bps)
