@@ -200,6 +200,10 @@ def run_gb300(args):
     N.check(L.pq_init(local))
     circ, ys = workload()
     n = len(ys)
+    if args.tuning:
+        vals = [int(v) for v in args.tuning.split(",")]
+        pq.set_tuning(inner_dims=vals[0], chunks_per_lane=vals[1], block_warps=vals[2], blocks_per_sm=vals[3])
+        args.no_autotune = True
     sim = pq.Simulator(circ, "auto")
     stats = sim.stats_full()
     tune_s = time.perf_counter()
@@ -628,6 +632,8 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=24)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default launch shape")
+    ap.add_argument("--tuning", default="", help="fixed launch shape inner_dims,chunks_per_lane,block_warps,"
+                    "blocks_per_sm (implies --no-autotune)")
     ap.add_argument("--boundaries", type=int, default=4096, help="boundary count (profiling of smaller cases)")
     ap.add_argument("--workload", default="many_boundaries",
                     choices=["many_boundaries", "batched", "serve", "small", "rotations"])

@@ -77,6 +77,7 @@ typedef struct pq_tuning {
     int32_t block_warps;     /* warps per CTA of the enumeration kernel (1..8) */
     int32_t max_branch_dim;  /* admission cap on d per branch engine (<= 62) */
     int32_t blocks_per_sm;   /* enumeration kernel register budget: 2, 3 or 4 blocks of 256 per SM */
+    int32_t unit_chunks;     /* at most this many chunks (1, 2, 4, 8) share each weight-table load */
 } pq_tuning;
 
 /* ---- library ------------------------------------------------------------------------ */

@@ -47,9 +47,9 @@ struct EngineDev {
     int zero;
     int DI, nsl_tp, nsl_th;
     int joint;               // 1: weights from the joint hi/lo table; 0: FP64 product path
-    int pairc, pairc2;       // the two lowest coordinates >= DI with R = 0 (flipping one keeps
-                             // every table index), -1 if none: chunks that differ in them are
-                             // walked together
+    int npairc;              // pair coordinates: the lowest (<= 3) coordinates >= DI with R = 0
+    int pairc[3];            // (flipping one keeps every table index): chunks that differ only
+                             // in them are walked together
     double sum_abs_bound;
     double grid;             // hi parts of wtab are integer multiples of this power of two
     double errfac;           // bound on a job's FP32 lo-sum error (before the 2^{(mag2-h)/2} scale)
@@ -261,27 +261,23 @@ PQ_HD double pow2_half(int e) {
 }
 
 // Work shape of one job: chunks of 2^dl Gray steps (dl = min(d - 5, DI)), grouped into units --
-// one chunk, or, when the engine has pair coordinates and the joint table applies, the 2 or 4
-// chunks that differ in them (they read the same table entry at every step) -- and cpi units
-// per work item (at most 2^16 items per job, so partial buffers stay bounded).  jdl packs dl
-// (bits 0-7) and 1 + the pair coordinates' bits in the chunk index (bits 8-15 and 16-23; 0 =
-// none).
-PQ_HD void job_shape(const EngineDev &E, int cpl, int &jdl, unsigned long long &nunits, unsigned &cpi) {
+// one chunk, or, when the engine has pair coordinates and the joint table applies, the 2^np
+// chunks that differ in its first np pair coordinates (np <= log2(unit_max)): they read the
+// same table entry at every step -- and cpi units per work item (at most 2^16 items per job,
+// so partial buffers stay bounded).  jdl packs dl (bits 0-7) and np (bits 8-9).
+PQ_HD void job_shape(const EngineDev &E, int cpl, int unit_max, int &jdl, unsigned long long &nunits, unsigned &cpi) {
     const int d = E.d;
     const int dl = d <= 5 ? 0 : (d - 5 < E.DI ? d - 5 : E.DI);
     unsigned long long n = 1ull << (d - dl);
-    int pb1 = -1, pb2 = -1;
-    if (E.joint && dl >= 3 && E.pairc >= dl && n >= 2) {
-        pb1 = E.pairc - dl;
-        n >>= 1;
-        if (E.pairc2 > E.pairc && n >= 2) {
-            pb2 = E.pairc2 - dl;
+    int np = 0;
+    if (E.joint && dl >= 3)
+        while (np < E.npairc && (2 << np) <= unit_max && n >= 2) {
             n >>= 1;
+            np++;
         }
-    }
     unsigned long long per = 32ull * (unsigned long long)cpl;
     while ((n + per - 1) / per > (1ull << 16)) per *= 2;
-    jdl = dl | ((pb1 + 1) << 8) | ((pb2 + 1) << 16);
+    jdl = dl | (np << 8);
     nunits = n;
     cpi = (unsigned)(n < per ? n : per);
 }

@@ -35,7 +35,14 @@ namespace pq {
 thread_local std::string g_err;
 static std::mutex g_mu;
 static int g_device = 0;
-static pq_tuning g_tuning = {10, 4, 8, 48, 3};
+static pq_tuning g_tuning = {10, 16, 8, 48, 3, 4};
+
+// Chunks per unit a tuning allows: eight accumulating chunks per lane only fit the 128-register
+// (two blocks per SM) build of the enumeration kernel.
+static int unit_max_of(const pq_tuning &tu) {
+    const int u = tu.unit_chunks > 0 ? tu.unit_chunks : 4;
+    return tu.blocks_per_sm == 2 ? u : std::min(u, 4);
+}
 
 static pq_status fail(pq_status s, const std::string &m) {
     g_err = m;
@@ -277,7 +284,7 @@ static pq_status build_plan(const std::vector<Segment> &segs, int nw, cudaStream
         int j = perm[k];
         kinv[j] = k;
         const EngineDev &E = eng[jobs[j].engine];
-        job_shape(E, tu.chunks_per_lane, jdl[j], jnch[j], jcpi[j]);
+        job_shape(E, tu.chunks_per_lane, unit_max_of(tu), jdl[j], jnch[j], jcpi[j]);
         istart[k + 1] = istart[k] + (long long)((jnch[j] + jcpi[j] - 1) / jcpi[j]);
         P.branches += std::ldexp(1.0, E.d);
     }
@@ -557,6 +564,11 @@ PQ_API pq_status pq_set_default_tuning(const pq_tuning *t) {
     if (t->max_branch_dim) {
         if (t->max_branch_dim < 1 || t->max_branch_dim > kMaxD) return fail(PQ_ERR_INVALID_ARG, "max_branch_dim in 1..62");
         n.max_branch_dim = t->max_branch_dim;
+    }
+    if (t->unit_chunks) {
+        if (t->unit_chunks != 1 && t->unit_chunks != 2 && t->unit_chunks != 4 && t->unit_chunks != 8)
+            return fail(PQ_ERR_INVALID_ARG, "unit_chunks is 1, 2, 4 or 8");
+        n.unit_chunks = t->unit_chunks;
     }
     if (t->blocks_per_sm) {
         if (t->blocks_per_sm < 2 || t->blocks_per_sm > 4) return fail(PQ_ERR_INVALID_ARG, "blocks_per_sm is 2, 3 or 4");
@@ -988,14 +1000,21 @@ PQ_API pq_status pq_sim_autotune(pq_sim *s, int64_t n, const uint64_t *x, const 
     // candidate values per field; the search starts from the simulator's current tuning.  Lane
     // chunks stop at 2^10 steps: the plain-FP32 low-part sums lose accuracy as 4^inner_dims
     // (more terms on a coarser exact grid), and 2^12 already costs an order of magnitude.
-    const std::vector<int> axes[4] = {{8, 9, 10}, {1, 2, 4, 8, 16}, {2, 4, 8}, {2, 3, 4}};
-    auto field = [](pq_tuning &t, int k) -> int32_t & {
-        return k == 0 ? t.inner_dims : k == 1 ? t.chunks_per_lane : k == 2 ? t.block_warps : t.blocks_per_sm;
+    // (register budget, chunks per unit) move together: eight chunks per unit need two blocks per SM
+    const std::vector<int> axes[4] = {{8, 9, 10}, {1, 2, 4, 8, 16}, {2, 4, 8}, {28, 24, 34, 32, 44, 42}};
+    auto set_field = [](pq_tuning &t, int k, int v) {
+        if (k == 0) t.inner_dims = v;
+        else if (k == 1) t.chunks_per_lane = v;
+        else if (k == 2) t.block_warps = v;
+        else {
+            t.blocks_per_sm = v / 10;
+            t.unit_chunks = v % 10;
+        }
     };
-    std::map<std::array<int, 4>, double> seen;
+    std::map<std::array<int, 5>, double> seen;
     std::vector<double> scratch;
     auto eval = [&](pq_tuning t, double *ms) -> pq_status {
-        std::array<int, 4> key{t.inner_dims, t.chunks_per_lane, t.block_warps, t.blocks_per_sm};
+        std::array<int, 5> key{t.inner_dims, t.chunks_per_lane, t.block_warps, t.blocks_per_sm, unit_max_of(t)};
         auto it = seen.find(key);
         if (it != seen.end()) {
             *ms = it->second;
@@ -1016,7 +1035,7 @@ PQ_API pq_status pq_sim_autotune(pq_sim *s, int64_t n, const uint64_t *x, const 
         for (int k = 0; k < 4 && st == PQ_OK; k++) {
             for (int v : axes[k]) {
                 pq_tuning t = best;
-                field(t, k) = v;
+                set_field(t, k, v);
                 double ms = 0.0;
                 st = eval(t, &ms);
                 if (st != PQ_OK) break;
@@ -1071,7 +1090,7 @@ PQ_API pq_status pq_debug_engine_shape(const pq_sim *s, int32_t branch, int64_t 
             r0++;
             if (j >= tb.DI) r0hi++;
         }
-    const int64_t v[8] = {e.d, e.rank, tb.DI, tb.joint ? 1 : 0, pk.off.pairc, r0, r0hi, e.t};
+    const int64_t v[8] = {e.d, e.rank, tb.DI, tb.joint ? 1 : 0, pk.off.npairc ? pk.off.pairc[0] : -1, r0, r0hi, e.t};
     for (int i = 0; i < 8; i++) out[i] = v[i];
     return PQ_OK;
 }
@@ -1175,7 +1194,7 @@ static NoAllocScratch *g_na_ptr[64] = {nullptr};  // device address of the scrat
 // Same per-job work shape as the regular launch layout, so each job's partial sums come out
 // in the same order (and the results bit-identical to pq_amplitudes).
 // One block: job records, identity item order, per-job shapes and the item prefix sums.
-__global__ void __launch_bounds__(1024) na_layout_kernel(NoAllocScratch *S, int nreq, int nb, int cpl) {
+__global__ void __launch_bounds__(1024) na_layout_kernel(NoAllocScratch *S, int nreq, int nb, int cpl, int umax) {
     __shared__ long long part[1024];
     const int njobs = nreq * nb;
     const int per = (njobs + 1023) / 1024;
@@ -1190,7 +1209,7 @@ __global__ void __launch_bounds__(1024) na_layout_kernel(NoAllocScratch *S, int 
         S->perm[j] = j;
         S->kinv[j] = j;
         const EngineDev &E = S->engines[j % nb];
-        job_shape(E, cpl, S->jdl[j], S->jnch[j], S->jcpi[j]);
+        job_shape(E, cpl, umax, S->jdl[j], S->jnch[j], S->jcpi[j]);
         local += (long long)((S->jnch[j] + S->jcpi[j] - 1) / S->jcpi[j]);
     }
     part[threadIdx.x] = local;
@@ -1240,7 +1259,7 @@ extern "C" PQ_API pq_status pq_amplitudes_noalloc(pq_sim *s, int64_t n, const ui
             int dl;
             unsigned long long nch;
             unsigned cpi;
-            job_shape(E, tu.chunks_per_lane, dl, nch, cpi);
+            job_shape(E, tu.chunks_per_lane, std::min(unit_max_of(tu), 4), dl, nch, cpi);
             nitems += (long long)((nch + cpi - 1) / cpi);
         }
     if (nitems > kNaMaxItems)
@@ -1266,7 +1285,7 @@ extern "C" PQ_API pq_status pq_amplitudes_noalloc(pq_sim *s, int64_t n, const ui
     CU(cudaMemcpyAsync(&S->map, &s->main.iom_dev, sizeof(IoMapDev), cudaMemcpyHostToDevice, st));
     // counter and error flag must start at zero; everything else is fully rewritten below
     CU(cudaMemsetAsync(&S->counter, 0, sizeof(unsigned long long) + sizeof(int), st));
-    na_layout_kernel<<<1, 1024, 0, st>>>(S, (int)n, nb, tu.chunks_per_lane);
+    na_layout_kernel<<<1, 1024, 0, st>>>(S, (int)n, nb, tu.chunks_per_lane, std::min(unit_max_of(tu), 4));
     KArgs a{};
     a.engines = S->engines;
     a.maps = &S->map;
@@ -1346,7 +1365,7 @@ static int64_t request_bytes(const Target &T, const pq_tuning &tu) {
         int dl;
         unsigned long long nch;
         unsigned cpi;
-        job_shape(E, tu.chunks_per_lane, dl, nch, cpi);
+        job_shape(E, tu.chunks_per_lane, unit_max_of(tu), dl, nch, cpi);
         b += (int64_t)sizeof(JobDev) + 64 + 16 * (int64_t)((nch + cpi - 1) / cpi);
     }
     return b;

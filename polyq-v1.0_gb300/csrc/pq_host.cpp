@@ -692,17 +692,11 @@ PackedEngine pack_engine(const HostEngine& e, const EngineTables& T) {
     d.tlo64 = as_off<double2>(k.vec(T.tlo));
     d.tp64 = as_off<double2>(k.vec(T.tp));
     d.joint = T.joint ? 1 : 0;
-    d.pairc = d.pairc2 = -1;
+    d.npairc = 0;
+    d.pairc[0] = d.pairc[1] = d.pairc[2] = -1;
     if (T.joint)
-        for (int j = T.DI; j < e.d; j++)
-            if (e.R[(size_t)j] == 0) {
-                if (d.pairc < 0) {
-                    d.pairc = j;
-                } else {
-                    d.pairc2 = j;
-                    break;
-                }
-            }
+        for (int j = T.DI; j < e.d && d.npairc < 3; j++)
+            if (e.R[(size_t)j] == 0) d.pairc[d.npairc++] = j;
     // hi.re, hi.im, lo.re, lo.im with hi + lo = the FP64 weight.  hi lies on the grid g, a power
     // of two with 2^DI * max|w| <= 2^23 g: any sum of at most 2^DI hi parts (a chunk) is then an
     // integer multiple of g below 2^24 g, i.e. exact in FP32; lo = w - hi (|lo| <= g/2) carries

@@ -285,6 +285,87 @@ __device__ __forceinline__ void gray_chunk_rot_any(const float4 *__restrict__ W,
     }
 }
 
+// One unit of K chunks (K = 2^np: the chunk at s1 and those that differ from it in the first np
+// pair coordinates) on the FP32 joint-table path: folded start indices, c_j of the walked
+// coordinates, the rotating-frame walk, and each chunk's sum rotated to its last index, scaled
+// by its high-coordinate weight and added into (accx, accy).
+template <int MODE, int K>
+__device__ __forceinline__ void walk_unit(const EngineDev &E, const JobDev &J, const uint64_t *G, const uint64_t *R,
+                                          const uint8_t *Lp, const uint32_t *Tg, int dl, uint64_t s1, uint64_t lomask,
+                                          uint8_t *dbg, double &accx, double &accy) {
+    const uint64_t himask = ~lomask;
+    const uint32_t wmask = (1u << dl) - 1u;
+    uint32_t m1;
+    uint64_t yy;
+    chunk_start(Lp, G, R, J.y0, s1, m1, yy);
+    m1 -= 2u * quad_parity(G, s1 & lomask);  // the table holds the low-coordinate quadratic part
+    uint32_t P1 = 0;
+    for (int j = 0; j < dl; j++) P1 |= (uint32_t)(popc64(G[j] & s1 & himask) & 1) << j;
+    const uint32_t sidx = (uint32_t)((yy << E.DI) | (s1 & lomask));
+    // chunk k = s1 + the pair coordinates of the bits of k: its index grows by their linear terms
+    // at s1 plus 2 G between each two of them; its c_j by their G rows
+    uint32_t dlin[3] = {0u, 0u, 0u}, grow[3] = {0u, 0u, 0u};
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+        if ((1 << i) < K) {
+            const int p = E.pairc[i];
+            dlin[i] = (uint32_t)Lp[p] + 2u * (uint32_t)(popc64(G[p] & s1) & 1);
+            grow[i] = (uint32_t)G[p] & wmask;
+        }
+    // index and high-coordinate bits of chunk k, recomputed where needed to keep registers free
+    auto chunk_m = [&](int k) -> uint32_t {
+        uint32_t mk = m1;
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+            if ((1 << i) < K && ((k >> i) & 1)) {
+                mk += dlin[i];
+#pragma unroll
+                for (int i2 = 0; i2 < i; i2++)
+                    if ((k >> i2) & 1) mk += 2u * (uint32_t)((G[E.pairc[i]] >> E.pairc[i2]) & 1ull);
+            }
+        return mk;
+    };
+    auto chunk_s = [&](int k) -> uint64_t {
+        uint64_t sk = s1;
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+            if ((1 << i) < K && ((k >> i) & 1)) sk |= 1ull << E.pairc[i];
+        return sk;
+    };
+    uint32_t Pc[K], mm[K];
+    uint64_t sb[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        uint32_t pk = P1;
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+            if ((1 << i) < K && ((k >> i) & 1)) pk ^= grow[i];
+        Pc[k] = pk;
+        if (MODE == 2) {
+            mm[k] = chunk_m(k);
+            sb[k] = chunk_s(k);
+        } else {
+            mm[k] = 0u;
+            sb[k] = 0ull;
+        }
+    }
+    float acc[K][4];
+    gray_chunk_rot_any<MODE, K>(E.wtab, sidx, Pc, Tg, Lp, dl, acc, dbg, sb, J.k0, mm, G, (uint32_t)lomask);
+    const int jl = dl - 1;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        // S = i^{m_end} A, m_end = m + L'_{dl-1}
+        const float2 r = quarter_turn(chunk_m(k) + (uint32_t)Lp[jl] + (((Pc[k] >> jl) & 1u) << 1));
+        const double ax = (double)acc[k][0] + (double)acc[k][2];
+        const double ay = (double)acc[k][1] + (double)acc[k][3];
+        const double vx = (double)r.x * ax - (double)r.y * ay;
+        const double vy = (double)r.y * ax + (double)r.x * ay;
+        const double2 chi = chunk_high_weight(E, chunk_s(k));
+        accx += vx * chi.x - vy * chi.y;
+        accy += vx * chi.y + vy * chi.x;
+    }
+}
+
 // MODE 0: FP32 weights, compensated accumulation.  MODE 1: FP64 weights and accumulation.
 // MODE 2: record the Z8 index of every branch into dbg (single-job debug launches).
 // MINB: resident blocks of 256 threads per SM the register allocation is sized for (2: 128,
@@ -339,89 +420,39 @@ __global__ void __launch_bounds__(256, MINB) enum_kernel(KArgs a) {
         double accx = 0.0, accy = 0.0;
         if (!J.vanish) {
             const int dl = a.jdl[job] & 255;
-            const int pb1 = ((a.jdl[job] >> 8) & 255) - 1;  // bits of the pair coordinates in the
-            const int pb2 = ((a.jdl[job] >> 16) & 255) - 1;  // chunk index (-1: none)
-            const int nk = pb1 < 0 ? 1 : (pb2 < 0 ? 2 : 4);
+            const int np = (a.jdl[job] >> 8) & 3;  // pair coordinates used by this job's units
+            const int nk = 1 << np;
             const unsigned cpi = a.jcpi[job];
             const unsigned long long nun = a.jnch[job];
             const unsigned long long c0 = (unsigned long long)iin * cpi;
             unsigned long long cend = c0 + cpi;
             if (cend > nun) cend = nun;
             const uint64_t lomask = (E.DI >= 64) ? ~0ull : ((1ull << E.DI) - 1ull);
-            const uint64_t himask = ~lomask;
             const uint32_t steps = 1u << dl;
-            const uint64_t e1 = pb1 < 0 ? 0ull : (1ull << (pb1 + dl));  // = 1 << pairc
-            const uint64_t e2 = pb2 < 0 ? 0ull : (1ull << (pb2 + dl));  // = 1 << pairc2
             for (unsigned long long un = c0 + lane; un < cend; un += 32) {
-                // unit -> its first chunk (zeros inserted at the pair bits)
+                // unit -> its first chunk (zeros inserted at the pair coordinates' chunk bits)
                 unsigned long long ch = un;
-                if (pb1 >= 0) ch = insert_zero(ch, pb1);
-                if (pb2 >= 0) ch = insert_zero(ch, pb2);
+                for (int i = 0; i < np; i++) ch = insert_zero(ch, E.pairc[i] - dl);
                 const uint64_t s1 = (uint64_t)ch << dl;
                 if (MODE != 1 && E.joint && dl >= 3) {
-                    // FP32 rotating-frame walk over the sign-folded joint table: the folded start
-                    // index and c_j of the walked coordinates (high coordinates only)
-                    uint32_t m1;
-                    uint64_t yy;
-                    chunk_start(Lp, G, R, J.y0, s1, m1, yy);
-                    m1 -= 2u * quad_parity(G, s1 & lomask);
-                    uint32_t P1 = 0;
-                    for (int j = 0; j < dl; j++) P1 |= (uint32_t)(popc64(G[j] & s1 & himask) & 1) << j;
-                    const uint32_t sidx = (uint32_t)((yy << E.DI) | (s1 & lomask));
-                    const uint32_t wmask = steps - 1u;
-#define PQ_FINISH(K)                                                                                      \
-    _Pragma("unroll") for (int k = 0; k < K; k++) {                                                       \
-        /* S = i^{m_end} A, m_end = m + L'_{dl-1} */                                                      \
-        const int jl = dl - 1;                                                                            \
-        const float2 r = quarter_turn(me[k] + (uint32_t)Lp[jl] + (((Pc[k] >> jl) & 1u) << 1));            \
-        const double ax = (double)acc[k][0] + (double)acc[k][2];                                          \
-        const double ay = (double)acc[k][1] + (double)acc[k][3];                                          \
-        const double vx = (double)r.x * ax - (double)r.y * ay;                                            \
-        const double vy = (double)r.y * ax + (double)r.x * ay;                                            \
-        const double2 chi = chunk_high_weight(E, sb[k]);                                                  \
-        accx += vx * chi.x - vy * chi.y;                                                                  \
-        accy += vx * chi.y + vy * chi.x;                                                                  \
-    }
-                    if (nk == 4) {
-                        const int p1 = E.pairc, p2 = E.pairc2;
-                        const uint32_t d1 = (uint32_t)Lp[p1] + 2u * (uint32_t)(popc64(G[p1] & s1) & 1);
-                        const uint32_t d2 = (uint32_t)Lp[p2] + 2u * (uint32_t)(popc64(G[p2] & s1) & 1);
-                        const uint32_t d12 = 2u * (uint32_t)((G[p2] >> p1) & 1ull);
-                        const uint32_t g1 = (uint32_t)G[p1] & wmask, g2 = (uint32_t)G[p2] & wmask;
-                        const uint32_t me[4] = {m1, m1 + d1, m1 + d2, m1 + d1 + d2 + d12};
-                        uint32_t Pc[4] = {P1, P1 ^ g1, P1 ^ g2, P1 ^ g1 ^ g2};
-                        uint32_t mm[4] = {me[0], me[1], me[2], me[3]};
-                        const uint64_t sb[4] = {s1, s1 | e1, s1 | e2, s1 | e1 | e2};
-                        float acc[4][4];
-                        gray_chunk_rot_any<MODE, 4>(E.wtab, sidx, Pc, Tg, Lp, dl, acc, a.dbg, sb, J.k0, mm, G,
-                                                    (uint32_t)lomask);
-                        PQ_FINISH(4)
-                    } else if (nk == 2) {
-                        const int p1 = E.pairc;
-                        const uint32_t d1 = (uint32_t)Lp[p1] + 2u * (uint32_t)(popc64(G[p1] & s1) & 1);
-                        const uint32_t me[2] = {m1, m1 + d1};
-                        uint32_t Pc[2] = {P1, P1 ^ ((uint32_t)G[p1] & wmask)};
-                        uint32_t mm[2] = {me[0], me[1]};
-                        const uint64_t sb[2] = {s1, s1 | e1};
-                        float acc[2][4];
-                        gray_chunk_rot_any<MODE, 2>(E.wtab, sidx, Pc, Tg, Lp, dl, acc, a.dbg, sb, J.k0, mm, G,
-                                                    (uint32_t)lomask);
-                        PQ_FINISH(2)
-                    } else {
-                        const uint32_t me[1] = {m1};
-                        uint32_t Pc[1] = {P1};
-                        uint32_t mm[1] = {m1};
-                        const uint64_t sb[1] = {s1};
-                        float acc[1][4];
-                        gray_chunk_rot_any<MODE, 1>(E.wtab, sidx, Pc, Tg, Lp, dl, acc, a.dbg, sb, J.k0, mm, G,
-                                                    (uint32_t)lomask);
-                        PQ_FINISH(1)
-                    }
-#undef PQ_FINISH
+                    if (np == 3) {
+                        if (MINB == 2) {  // eight accumulators per lane: only with the 128-register budget
+                            walk_unit<MODE, (MINB == 2 ? 8 : 4)>(E, J, G, R, Lp, Tg, dl, s1, lomask, a.dbg, accx, accy);
+                        } else {
+                            walk_unit<MODE, 4>(E, J, G, R, Lp, Tg, dl, s1, lomask, a.dbg, accx, accy);
+                            walk_unit<MODE, 4>(E, J, G, R, Lp, Tg, dl, s1 | (1ull << E.pairc[2]), lomask, a.dbg, accx,
+                                               accy);
+                        }
+                    } else if (np == 2) walk_unit<MODE, 4>(E, J, G, R, Lp, Tg, dl, s1, lomask, a.dbg, accx, accy);
+                    else if (np == 1) walk_unit<MODE, 2>(E, J, G, R, Lp, Tg, dl, s1, lomask, a.dbg, accx, accy);
+                    else walk_unit<MODE, 1>(E, J, G, R, Lp, Tg, dl, s1, lomask, a.dbg, accx, accy);
                     continue;
                 }
+                const uint64_t himask = ~lomask;
                 for (int kc = 0; kc < nk; kc++) {
-                    const uint64_t s = s1 | ((kc & 1) ? e1 : 0ull) | ((kc & 2) ? e2 : 0ull);
+                    uint64_t s = s1;
+                    for (int i = 0; i < np; i++)
+                        if ((kc >> i) & 1) s |= 1ull << E.pairc[i];
                     uint32_t m;
                     uint64_t yy;
                     chunk_start(Lp, G, R, J.y0, s, m, yy);
