@@ -3,7 +3,7 @@
 Workload: a seeded Clifford+T circuit with n=50 qubits, 2000 gates from {H,S,CX,CZ,T}
 (exactly 32 T, seed 0: the radical-constrained branch subspace of the cached engine has
 2^29 > 2^22 branches), 4096 uniform output bitstrings y, x = 0, strategy auto (the
-reference's Simulator::new default: 16 branch engines of d = 19..21).  One step evaluates
+reference's Simulator::new default: 16 branch engines of d = 20..22).  One step evaluates
 all 4096 amplitudes.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
@@ -12,9 +12,11 @@ value      branches/s with boundaries resident in HBM (pq_amplitudes_device), CU
            the launching stream, L2 flushed (512 MiB write) between steps outside the events
 e2e        same metric through the public host-buffer call pq_amplitudes (H2D of the
            boundaries and D2H of amplitudes + error bounds inside the timed region)
-roofline   enumeration kernel: reference-form integer ops (5 W_o + 6 W_g int64 per branch)
-           per launch over its event-timed duration, against the integer-pipe rate measured
-           on the device (lop3 / popc microbenchmark)
+roofline   enumeration kernel: its FP32 FMA-pipe work (4 ops per enumerated branch) per launch
+           over its event-timed duration, against the fma.f32 rate measured on the device;
+           reference_form beside it: the reference engine's integer work for the same branches
+           (5 W_o + 6 W_g int64 ops each) against the measured lop3 / popc rates
+workloads  --workload many_boundaries (default) | batched | serve | small | rotations
 cpu_baseline  the CPU oracle (a restatement of the reference engine) on all host threads
 --impl reference  times the same CPU restatement on the same workload (bounded sample)
 """
@@ -34,6 +36,11 @@ sys.path.insert(0, os.path.join(REPO, "polyq-v1.0_gb300"))
 
 WORKLOAD = {"n_qubits": 50, "gates": 2000, "t_count": 32, "circuit_seed": 0, "boundaries": 4096,
             "output_seed": 1, "strategy": "auto"}
+# FP32 FMA-pipe operations per enumerated branch in the enumeration kernel's walk
+FMA_OPS_PER_BRANCH = 4
+# DRAM bytes of one full-size enumeration launch (ncu, dram__bytes_read.sum + dram__bytes_write.sum)
+TRAFFIC_BYTES_PER_LAUNCH = 8934912
+
 METRIC = "branches/s and amplitudes/s at <=1e-6 rel err vs FP64; served p50/p99 latency"
 
 
@@ -201,8 +208,9 @@ def run_gb300(args):
     circ, ys = workload()
     n = len(ys)
     if args.tuning:
-        vals = [int(v) for v in args.tuning.split(",")]
-        pq.set_tuning(inner_dims=vals[0], chunks_per_lane=vals[1], block_warps=vals[2], blocks_per_sm=vals[3])
+        vals = [int(v) for v in args.tuning.split(",")] + [0]
+        pq.set_tuning(inner_dims=vals[0], chunks_per_lane=vals[1], block_warps=vals[2], blocks_per_sm=vals[3],
+                      unit_chunks=vals[4])
         args.no_autotune = True
     sim = pq.Simulator(circ, "auto")
     stats = sim.stats_full()
@@ -288,15 +296,19 @@ def run_gb300(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_ms = float(t.item())
     e2e_value = ws * branches_step / (e2e_ms * 1e-3)
-    # roofline of the enumeration kernel (reference-form integer work)
+    # roofline of the enumeration kernel.  Its arithmetic per branch is two quarter-turn-and-add
+    # updates (hi and lo complex pairs), four FP32 FMA-pipe ops; table loads and index xors are
+    # shared by the chunks of a unit.  Peak: the measured fma.f32 rate of this device.
     enum_avg = sum(enum_ms) / len(enum_ms)
-    lop3, popcr = peaks[0], peaks[1]
-    # the reference form needs 2 popc.b32 per 64-bit popcount and 2 lop3.b32 per 64-bit logic op:
-    # at the measured pipe rates one launch's work takes at least t_peak seconds
+    lop3, popcr, fmar = peaks[0], peaks[1], peaks[2]
+    fma_step = FMA_OPS_PER_BRANCH * branches_step
+    achieved = fma_step / (enum_avg * 1e-3)
+    # the reference engine's form of the same work: 5 W_o + 6 W_g int64 ops per branch, 2 popc.b32
+    # per 64-bit popcount and 2 lop3.b32 per 64-bit logic op, at the measured pipe rates
     t_peak = max(2.0 * popc_step / popcr, 2.0 * logic_step / lop3)
     ops_branch = ops_step / branches_step
-    peak_ops = ops_step / t_peak
-    achieved = ops_step / (enum_avg * 1e-3)
+    ref_peak = ops_step / t_peak
+    ref_achieved = ops_step / (enum_avg * 1e-3)
     cpu = None
     if rank == 0 and not args.no_cpu:
         threads = cpu_threads()
@@ -321,11 +333,20 @@ def run_gb300(args):
                 "h2d_bytes_per_step": int(xs_h.nbytes + ys_h.nbytes),
                 "d2h_bytes_per_step": int(out_h.nbytes + err_h.nbytes + 4)},
         "gpu_launches": 4 * args.steps,
-        "roofline": {"bound": "int", "achieved": achieved / 1e12, "peak": peak_ops / 1e12, "unit": "Tops/s",
-                     "frac": achieved / peak_ops, "traffic": None,
-                     "kernel": "enum_kernel", "kernel_ms": enum_avg, "ops": "reference-form int64 ops/branch %.1f" %
-                     ops_branch, "peak_source": "measured lop3.b32 %.3e/s, popc.b32 %.3e/s on this device" %
-                     (lop3, popcr)},
+        "roofline": {"bound": "fp32", "achieved": achieved / 1e12, "peak": fmar / 1e12, "unit": "Tops/s",
+                     "frac": achieved / fmar, "traffic": TRAFFIC_BYTES_PER_LAUNCH,
+                     "kernel": "enum_kernel", "kernel_ms": enum_avg,
+                     "ops": "%d FP32 FMA-pipe ops per enumerated branch" % FMA_OPS_PER_BRANCH,
+                     "peak_source": "measured fma.f32 rate on this device (pq_measure_peaks), not a vendor figure",
+                     "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one full-size launch, "
+                                       "ncu capture in profiles/enum_kernel_many_boundaries.md",
+                     "reference_form": {
+                         "ops_per_branch": ops_branch, "achieved": ref_achieved / 1e12, "peak": ref_peak / 1e12,
+                         "unit": "Tops/s", "frac": ref_achieved / ref_peak,
+                         "note": "the reference engine's int64 XOR/AND/POPC work per branch (5 W_o + 6 W_g) per "
+                                 "second, against the rate its binding pipe allows at the measured lop3.b32 %.3e/s "
+                                 "and popc.b32 %.3e/s; above 1 because the enumeration here does not execute "
+                                 "that form" % (lop3, popcr)}},
         "clocks": clocks,
     }
     if cpu:
@@ -370,6 +391,13 @@ def run_batched(args):
     b = pq.Batch(sims, [64] * len(sims))
     xs, ys = b.pack([[0] * 64] * len(sims), outs)
     n = 64 * len(sims)
+    t_tune = time.perf_counter()
+    if args.no_autotune:
+        tuning = None
+    else:
+        # chunk size, warps per block and chunks per table load chosen by the library's autotuner
+        tuning, _ = b.autotune(xs, ys, reps=2)
+    t_tune = time.perf_counter() - t_tune
     dx = torch.from_numpy(xs.view(np.int64)).cuda()
     dy = torch.from_numpy(ys.view(np.int64)).cuda()
     dout = torch.zeros(2 * n, dtype=torch.float64, device="cuda")
@@ -401,13 +429,18 @@ def run_batched(args):
         s.amplitudes([0] * 64, o)  # plans and graphs built outside the timing
     per_circ = []
     same = True
+    plain_amps = []
     t0 = time.perf_counter()
     for i, (s, o) in enumerate(zip(sims, outs)):
         t1 = time.perf_counter()
         a = s.amplitudes([0] * 64, o)
         per_circ.append(time.perf_counter() - t1)
-        same = same and np.array_equal(a, got[64 * i:64 * i + 64])
+        plain_amps.append(a)
     plain_circ_s = time.perf_counter() - t0
+    plain_all = np.concatenate(plain_amps)
+    same = bool(np.array_equal(plain_all, got))
+    scale = np.maximum(np.abs(plain_all), 1e-300)
+    max_rel_diff = float(np.max(np.abs(plain_all - got) / scale))
     # plain path 2: one launch per (circuit, boundary)
     for s, o in zip(sims, outs):
         s.amplitudes_plain([0], o[:1])
@@ -429,12 +462,14 @@ def run_batched(args):
             "speedup_vs_plain_per_circuit": plain_circ_s / (batched_ms * 1e-3),
             "speedup_vs_plain_per_boundary": plain_bnd_s / (batched_ms * 1e-3),
             "batched_equals_per_circuit_bitwise": bool(same),
+            "batched_vs_per_circuit_max_rel_diff": max_rel_diff,
             "kernel_ms_last_step": {"prepare": kms[0], "enumerate": kms[1], "reduce": kms[2]},
             "per_d_bucket_amps_per_s_plain": {k: v[0] / v[1] for k, v in buckets.items()},
             "config": {"workload": "256 circuits, n~U[16,64], 40n gates, T~U[8,36] (seed 3), 64 uniform y each, "
                                    "strategy auto", "branches_enumerated_per_step": benum[0],
                        "branches_all_engines_per_step": b.branches, "host_build_s": build_s,
-                       "l2": "flushed between steps"}}
+                       "l2": "flushed between steps", "tuning": tuning,
+                       "tuning_source": "fixed" if tuning is None else "pq_batch_autotune (%.1f s)" % t_tune}}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -633,7 +668,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default launch shape")
     ap.add_argument("--tuning", default="", help="fixed launch shape inner_dims,chunks_per_lane,block_warps,"
-                    "blocks_per_sm (implies --no-autotune)")
+                    "blocks_per_sm[,unit_chunks] (implies --no-autotune)")
     ap.add_argument("--boundaries", type=int, default=4096, help="boundary count (profiling of smaller cases)")
     ap.add_argument("--workload", default="many_boundaries",
                     choices=["many_boundaries", "batched", "serve", "small", "rotations"])

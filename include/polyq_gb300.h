@@ -188,6 +188,11 @@ PQ_API pq_status pq_server_drain(pq_server *s, double timeout_s);
  * receives the tuning, best_ms (optional) its device time. */
 PQ_API pq_status pq_sim_autotune(pq_sim *sim, int64_t n, const uint64_t *x, const uint64_t *y, int32_t reps,
                                  pq_tuning *best, double *best_ms);
+/* The same search for a batch (pq_batch_run inputs x, y), over chunks_per_lane, block_warps and
+ * (blocks_per_sm, unit_chunks); the lane chunk length stays that of the simulators' tables.
+ * The batch's later launches use the fastest shape. */
+PQ_API pq_status pq_batch_autotune(pq_batch *b, const uint64_t *x, const uint64_t *y, int32_t reps, pq_tuning *best,
+                                   double *best_ms);
 /* The launch shape the simulator's plans use. */
 PQ_API pq_status pq_sim_get_tuning(const pq_sim *sim, pq_tuning *out);
 
@@ -207,7 +212,7 @@ PQ_API pq_status pq_batch_enumerated(pq_batch *b, double *out);
 /* Work items of the simulator's size-n plan (-1 if it has no such plan yet). */
 PQ_API int64_t pq_sim_launch_items(pq_sim *sim, int64_t n);
 /* Issue rates measured on the current device: [0] lop3.b32 ops/s, [1] popc.b32 ops/s,
- * [2] add.f32 ops/s, [3] SM count. */
+ * [2] fma.f32 ops/s, [3] SM count. */
 PQ_API pq_status pq_measure_peaks(double out[4]);
 
 /* ---- checks (bit-exact comparisons against a CPU restatement) ------------------------ */

@@ -35,7 +35,7 @@ namespace pq {
 thread_local std::string g_err;
 static std::mutex g_mu;
 static int g_device = 0;
-static pq_tuning g_tuning = {10, 16, 8, 48, 3, 4};
+static pq_tuning g_tuning = {10, 4, 8, 48, 3, 4};
 
 // Chunks per unit a tuning allows: eight accumulating chunks per lane only fit the 128-register
 // (two blocks per SM) build of the enumeration kernel.
@@ -516,6 +516,8 @@ struct pq_sim {
 
 struct pq_batch {
     std::vector<pq_sim *> sims;
+    std::vector<Segment> segs;
+    pq_tuning tu{};
     std::unique_ptr<Plan> plan;
     std::mutex mu;
 };
@@ -860,6 +862,8 @@ PQ_API pq_status pq_batch_create(int32_t nsims, pq_sim *const *sims, const int64
         tu = g_tuning;
     }
     CU(cudaSetDevice(g_device));
+    B->segs = segs;
+    B->tu = tu;
     B->plan = std::make_unique<Plan>();
     pq_status st = build_plan(segs, nw, nullptr, tu, *B->plan);
     if (st != PQ_OK) return st;
@@ -987,20 +991,17 @@ static pq_status time_tuning(pq_sim *s, int64_t n, const uint64_t *x, const uint
     return PQ_OK;
 }
 
-PQ_API pq_status pq_sim_autotune(pq_sim *s, int64_t n, const uint64_t *x, const uint64_t *y, int32_t reps,
-                                 pq_tuning *best_out, double *best_ms) {
-    if (!s || !x || !y) return fail(PQ_ERR_INVALID_ARG, "null argument");
-    pq_status st = check_n(n);
-    if (st != PQ_OK) return st;
-    if (reps < 0 || reps > 1000) return fail(PQ_ERR_INVALID_ARG, "reps in 0..1000");
-    if (reps == 0) reps = 3;
-    std::lock_guard<std::mutex> lk(s->mu);
-    if (s->host_only) return fail(PQ_ERR_NO_DEVICE, "simulator was created by pq_analyze (host structures only)");
-    CU(cudaSetDevice(s->device));
-    // candidate values per field; the search starts from the simulator's current tuning.  Lane
-    // chunks stop at 2^10 steps: the plain-FP32 low-part sums lose accuracy as 4^inner_dims
-    // (more terms on a coarser exact grid), and 2^12 already costs an order of magnitude.
-    // (register budget, chunks per unit) move together: eight chunks per unit need two blocks per SM
+}  // extern "C"
+
+// Coordinate descent over the launch shape from `start`: one field at a time over its
+// candidate values, keeping the fastest (by more than 2%, so timing noise does not flip
+// choices), until a full pass changes nothing (at most three passes).  `time_of` returns the
+// device time of one launch under a tuning.  Lane chunks stop at 2^10 steps: the plain-FP32
+// low-part sums lose accuracy as 4^inner_dims (more terms on a coarser exact grid), and 2^12
+// already costs an order of magnitude.  The register budget and the chunks per unit move
+// together: eight chunks per unit need two blocks per SM.
+template <class TimeOf>
+static pq_status tune_search(pq_tuning start, bool tune_inner, TimeOf time_of, pq_tuning &best, double &best_t) {
     const std::vector<int> axes[4] = {{8, 9, 10}, {1, 2, 4, 8, 16}, {2, 4, 8}, {28, 24, 34, 32, 44, 42}};
     auto set_field = [](pq_tuning &t, int k, int v) {
         if (k == 0) t.inner_dims = v;
@@ -1012,34 +1013,29 @@ PQ_API pq_status pq_sim_autotune(pq_sim *s, int64_t n, const uint64_t *x, const 
         }
     };
     std::map<std::array<int, 5>, double> seen;
-    std::vector<double> scratch;
-    auto eval = [&](pq_tuning t, double *ms) -> pq_status {
+    auto eval = [&](const pq_tuning &t, double *ms) -> pq_status {
         std::array<int, 5> key{t.inner_dims, t.chunks_per_lane, t.block_warps, t.blocks_per_sm, unit_max_of(t)};
         auto it = seen.find(key);
         if (it != seen.end()) {
             *ms = it->second;
             return PQ_OK;
         }
-        pq_status e = time_tuning(s, n, x, y, reps, t, scratch, ms);
+        pq_status e = time_of(t, ms);
         if (e == PQ_OK) seen[key] = *ms;
         return e;
     };
-    pq_tuning best = s->tu;
-    best.inner_dims = s->di_max;
-    double best_t = 0.0;
-    st = eval(best, &best_t);
-    // coordinate descent: sweep one field at a time, keep the fastest, until a full pass
-    // changes nothing (at most three passes)
+    best = start;
+    pq_status st = eval(best, &best_t);
     for (int pass = 0; st == PQ_OK && pass < 3; pass++) {
         bool changed = false;
-        for (int k = 0; k < 4 && st == PQ_OK; k++) {
+        for (int k = tune_inner ? 0 : 1; k < 4 && st == PQ_OK; k++) {
             for (int v : axes[k]) {
                 pq_tuning t = best;
                 set_field(t, k, v);
                 double ms = 0.0;
                 st = eval(t, &ms);
                 if (st != PQ_OK) break;
-                if (ms < best_t * 0.98) {  // a 2% margin keeps timing noise from flipping choices
+                if (ms < best_t * 0.98) {
                     best = t;
                     best_t = ms;
                     changed = true;
@@ -1048,6 +1044,28 @@ PQ_API pq_status pq_sim_autotune(pq_sim *s, int64_t n, const uint64_t *x, const 
         }
         if (!changed) break;
     }
+    return st;
+}
+
+extern "C" {
+
+PQ_API pq_status pq_sim_autotune(pq_sim *s, int64_t n, const uint64_t *x, const uint64_t *y, int32_t reps,
+                                 pq_tuning *best_out, double *best_ms) {
+    if (!s || !x || !y) return fail(PQ_ERR_INVALID_ARG, "null argument");
+    pq_status st = check_n(n);
+    if (st != PQ_OK) return st;
+    if (reps < 0 || reps > 1000) return fail(PQ_ERR_INVALID_ARG, "reps in 0..1000");
+    if (reps == 0) reps = 3;
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->host_only) return fail(PQ_ERR_NO_DEVICE, "simulator was created by pq_analyze (host structures only)");
+    CU(cudaSetDevice(s->device));
+    std::vector<double> scratch;
+    pq_tuning start = s->tu, best;
+    start.inner_dims = s->di_max;
+    double best_t = 0.0;
+    st = tune_search(start, true,
+                     [&](const pq_tuning &t, double *ms) { return time_tuning(s, n, x, y, reps, t, scratch, ms); },
+                     best, best_t);
     // whatever happened, leave the simulator on its best known tuning
     pq_status st2 = PQ_OK;
     if (best.inner_dims != s->di_max) st2 = retable_sim(s, best.inner_dims);
@@ -1055,6 +1073,46 @@ PQ_API pq_status pq_sim_autotune(pq_sim *s, int64_t n, const uint64_t *x, const 
     s->plans.clear();
     if (st != PQ_OK) return st;
     if (st2 != PQ_OK) return st2;
+    if (best_out) *best_out = best;
+    if (best_ms) *best_ms = best_t;
+    return PQ_OK;
+}
+
+PQ_API pq_status pq_batch_autotune(pq_batch *b, const uint64_t *x, const uint64_t *y, int32_t reps, pq_tuning *best_out,
+                                   double *best_ms) {
+    if (!b || !x || !y) return fail(PQ_ERR_INVALID_ARG, "null argument");
+    if (reps < 0 || reps > 1000) return fail(PQ_ERR_INVALID_ARG, "reps in 0..1000");
+    if (reps == 0) reps = 3;
+    std::lock_guard<std::mutex> lk(b->mu);
+    CU(cudaSetDevice(g_device));
+    std::vector<double> scratch((size_t)2 * b->plan->nout);
+    auto time_of = [&](const pq_tuning &t, double *ms_out) -> pq_status {
+        Plan P;
+        pq_status e = build_plan(b->segs, b->plan->nw, nullptr, t, P);
+        if (e != PQ_OK) return e;
+        double bt = 1e300;
+        for (int r = 0; r <= reps; r++) {
+            e = run_host(P, x, y, scratch.data(), nullptr, false);
+            if (e != PQ_OK) return e;
+            float ms[3];
+            e = last_kernel_ms(P, ms);
+            if (e != PQ_OK) return e;
+            if (r > 0) bt = std::min(bt, (double)ms[0] + ms[1] + ms[2]);
+        }
+        *ms_out = bt;
+        return PQ_OK;
+    };
+    // the simulators' weight tables are shared with other users: the lane chunk length stays
+    pq_tuning best;
+    double best_t = 0.0;
+    pq_status st = tune_search(b->tu, false, time_of, best, best_t);
+    if (st != PQ_OK) return st;
+    auto P = std::make_unique<Plan>();
+    st = build_plan(b->segs, b->plan->nw, nullptr, best, *P);
+    if (st != PQ_OK) return st;
+    CU(cudaStreamSynchronize(b->plan->stream));
+    b->plan = std::move(P);
+    b->tu = best;
     if (best_out) *best_out = best;
     if (best_ms) *best_ms = best_t;
     return PQ_OK;

@@ -1,9 +1,10 @@
 // pq_peak.cu -- measured issue rates of the pipes the enumeration kernel uses.
 //
-// The roofline of the amplitude path is integer logic / popcount / FP32-add work, for which no
-// vendor peak is published per chip configuration; these kernels measure it on the device:
-// eight independent dependency chains per thread of one instruction type (lop3.b32, popc.b32,
-// add.f32) over a persistent grid, timed with CUDA events.  Every thread writes one word to
+// The enumeration's arithmetic is FP32 fused multiply-add work (the reference form of the same
+// sum is integer logic / popcount work), for which no vendor peak is published per chip
+// configuration; these kernels measure the rates on the device: eight independent dependency
+// chains per thread of one instruction type (lop3.b32, popc.b32, fma.rn.f32) over a persistent
+// grid, timed with CUDA events.  Every thread writes one word to
 // `out` (grid * block words) so the chains are not removed.
 #include <cuda_runtime.h>
 
@@ -37,12 +38,12 @@ __global__ void __launch_bounds__(256) peak_popc(uint32_t *out, int iters) {
     out[blockIdx.x * blockDim.x + threadIdx.x] = a0 ^ a1 ^ a2 ^ a3 ^ a4 ^ a5 ^ a6 ^ a7;
 }
 
-__global__ void __launch_bounds__(256) peak_fadd(uint32_t *out, int iters) {
+__global__ void __launch_bounds__(256) peak_ffma(uint32_t *out, int iters) {
     float a0 = threadIdx.x * 1e-3f, a1 = a0 + 1.f, a2 = a0 + 2.f, a3 = a0 + 3.f;
     float a4 = a0 + 4.f, a5 = a0 + 5.f, a6 = a0 + 6.f, a7 = a0 + 7.f;
-    const float c = 1e-7f * (float)(blockIdx.x + 1);
+    const float c = 1e-7f * (float)(blockIdx.x + 1), s = 0.999f;
     for (int i = 0; i < iters; i++) {
-#define PQ_FADD(x) asm volatile("add.rn.f32 %0, %0, %1;" : "+f"(x) : "f"(c))
+#define PQ_FADD(x) asm volatile("fma.rn.f32 %0, %0, %1, %2;" : "+f"(x) : "f"(s), "f"(c))
         PQ_FADD(a0); PQ_FADD(a1); PQ_FADD(a2); PQ_FADD(a3); PQ_FADD(a4); PQ_FADD(a5); PQ_FADD(a6); PQ_FADD(a7);
 #undef PQ_FADD
     }
@@ -54,7 +55,7 @@ __global__ void __launch_bounds__(256) peak_fadd(uint32_t *out, int iters) {
 using namespace pq;
 
 extern "C" PQ_API pq_status pq_measure_peaks(double out[4]) {
-    // out: lop3.b32 ops/s, popc.b32 ops/s, add.f32 ops/s, SM count
+    // out: lop3.b32 ops/s, popc.b32 ops/s, fma.f32 ops/s, SM count
     if (!out) return PQ_ERR_INVALID_ARG;
     int dev = 0;
     cudaDeviceProp p;
@@ -66,7 +67,7 @@ extern "C" PQ_API pq_status pq_measure_peaks(double out[4]) {
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    void (*kern[3])(uint32_t *, int) = {peak_lop3, peak_popc, peak_fadd};
+    void (*kern[3])(uint32_t *, int) = {peak_lop3, peak_popc, peak_ffma};
     pq_status st = PQ_OK;
     for (int k = 0; k < 3 && st == PQ_OK; k++) {
         kern[k]<<<grid, block>>>(buf, iters);  // warm-up

@@ -93,6 +93,7 @@ SIGNATURES = {
     "pq_measure_peaks": (ct.c_int, [f64p]),
     "pq_sim_autotune": (ct.c_int, [P, ct.c_int64, u64p, u64p, ct.c_int32, ct.POINTER(Tuning), f64p]),
     "pq_sim_get_tuning": (ct.c_int, [P, ct.POINTER(Tuning)]),
+    "pq_batch_autotune": (ct.c_int, [P, u64p, u64p, ct.c_int32, ct.POINTER(Tuning), f64p]),
     "pq_debug_engine_dump": (ct.c_int64, [P, ct.c_int32, u64p, ct.c_int64]),
     "pq_debug_engine_shape": (ct.c_int, [P, ct.c_int32, i64p]),
     "pq_debug_branch_phases": (ct.c_int32, [P, ct.c_int32, u64p, u64p, u8p]),

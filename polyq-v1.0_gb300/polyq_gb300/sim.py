@@ -241,6 +241,15 @@ class Batch:
         amps = out.view(np.complex128)
         return (amps, err) if with_error else amps
 
+    def autotune(self, xs, ys, reps: int = 3):
+        """Pick the fastest launch shape for this batch on packed boundaries (pq_batch_autotune);
+        returns (tuning dict, device ms of one launch)."""
+        t = N.Tuning()
+        ms = ct.c_double(0.0)
+        N.check(self._L.pq_batch_autotune(self._h, _p(xs, ct.c_uint64), _p(ys, ct.c_uint64), reps, ct.byref(t),
+                                          ct.byref(ms)))
+        return {k: getattr(t, k) for k, _ in N.Tuning._fields_}, ms.value
+
     def run_device(self, x_ptr, y_ptr, out_ptr, err_ptr=None, stream=None):
         N.check(self._L.pq_batch_run_device(self._h, x_ptr, y_ptr, out_ptr, err_ptr, stream))
 

@@ -276,3 +276,20 @@ def test_autotune_keeps_results(gpu):
             np.testing.assert_allclose(s2.amplitudes([0] * 128, ys), before, rtol=0, atol=1e-13 * scale)
         finally:
             set_tuning(blocks_per_sm=set_old["blocks_per_sm"])
+
+
+def test_batch_autotune_keeps_results(gpu):
+    circs = workload_batch(8, seed=3, t_max=14)
+    sims = [Simulator(c) for c, _ in circs]
+    outs = [random_outputs(c.num_qubits, 5, i) for i, (c, _) in enumerate(circs)]
+    b = Batch(sims, [5] * len(sims))
+    xs, ys = b.pack([[0] * 5] * len(sims), outs)
+    before, err = b.run(xs, ys, with_error=True)
+    tuning, ms = b.autotune(xs, ys, reps=1)
+    assert ms > 0.0 and tuning["blocks_per_sm"] in (2, 3, 4) and tuning["unit_chunks"] in (2, 4, 8)
+    after = b.run(xs, ys)
+    # only the FP64 summation order of work-item partials may change
+    assert np.all(np.abs(after - before) <= err + 1e-13 * np.abs(before))
+    for i, s in enumerate(sims[:3]):
+        r = O.OracleSim(circs[i][0])
+        assert_amps(after[5 * i:5 * i + 5], r.amplitudes([0] * 5, outs[i]))
