@@ -124,6 +124,24 @@ def dist_init(args):
     return None, 0, 1, 0
 
 
+def max_over_ranks(dist, x):
+    """Max of x over all ranks of the process group (x itself without one): the replica
+    timing rule, a step lasts as long as the slowest rank."""
+    if not dist:
+        return x
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(world_size, units_per_rank, ms):
+    """Whole-job throughput of N independent replicas: all ranks' units over the slowest
+    rank's time (ms)."""
+    return world_size * units_per_rank / (ms * 1e-3)
+
+
 def cpu_threads():
     try:
         return len(os.sched_getaffinity(0))
@@ -265,11 +283,8 @@ def run_gb300(args):
             t_wall = time.perf_counter() - t_wall0
         clocks = clk.summary()
         ms = sum(step_ms) / len(step_ms)
-        if dist:
-            t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
-        value = ws * branches_step / (ms * 1e-3)
+        ms = max_over_ranks(dist, ms)
+        value = replica_rate(ws, branches_step, ms)
         # FP32-compensated results of the last step against the device FP64 mode
         got = dout.cpu().numpy().view(np.complex128).copy()
         errb = derr.cpu().numpy().copy()
@@ -291,11 +306,8 @@ def run_gb300(args):
                                 P(err_h, ct.c_double)))
         e2e_s.append(time.perf_counter() - t0)
     e2e_ms = 1e3 * sum(e2e_s) / len(e2e_s)
-    if dist:
-        t = torch.tensor([e2e_ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e_value = ws * branches_step / (e2e_ms * 1e-3)
+    e2e_ms = max_over_ranks(dist, e2e_ms)
+    e2e_value = replica_rate(ws, branches_step, e2e_ms)
     # roofline of the enumeration kernel.  Its arithmetic per branch is two quarter-turn-and-add
     # updates (hi and lo complex pairs), four FP32 FMA-pipe ops; table loads and index xors are
     # shared by the chunks of a unit.  Peak: the measured fma.f32 rate of this device.
