@@ -110,6 +110,11 @@ PQ_API pq_status pq_probabilities(pq_sim *sim, int64_t n, const uint64_t *x, con
  * pairs.  The sandwich engine of each distinct measured-qubit set is built once and cached. */
 PQ_API pq_status pq_marginal(pq_sim *sim, const uint64_t *x, int32_t nmeas, const int32_t *qubits,
                              const uint8_t *outcomes, double *out);
+/* Simulator::sample_many -- sim.rs:253-284: `shots` computational-basis samples of C|x>, drawn
+ * by the chain rule over qubit prefixes with the reference's SplitMix64 streams (one seed per
+ * shot from seed), so the same seed gives the reference's samples.  out: shots bitstrings.
+ * All shots advance together: one launch per qubit over the cached prefix engines. */
+PQ_API pq_status pq_sample_many(pq_sim *sim, const uint64_t *x, int64_t shots, uint64_t seed, uint64_t *out);
 /* Device-resident variant of pq_amplitudes: x, y, out, errbound are device pointers; the work
  * is ordered after, and waited for by, `stream` (cudaStream_t; NULL = the legacy default
  * stream) without a host synchronisation. */

@@ -57,6 +57,7 @@ def lib():
             L.pqo_last_branches.argtypes = [P]
             L.pqo_marginal.restype = ct.c_double
             L.pqo_marginal.argtypes = [P, u64p, ct.c_int, i32p, u8p]
+            L.pqo_sample_many.argtypes = [P, u64p, ct.c_int64, ct.c_uint64, u64p]
             L.pqo_brute_force.restype = ct.c_int
             L.pqo_brute_force.argtypes = [P, u64p, u64p, f64p]
             L.pqo_dense_statevector.argtypes = [ct.c_int, ct.c_int, u8p, i32p, i32p, u32p, u64p, f64p]
@@ -154,6 +155,15 @@ class OracleSim:
         bs = np.array([int(b) for _, b in measured] or [0], dtype=np.uint8)
         return float(self.L.pqo_marginal(self.h, _ptr(xs, ct.c_uint64), len(measured), _ptr(qs, ct.c_int32),
                                          _ptr(bs, ct.c_uint8)))
+
+    def sample_many(self, x, shots, seed):
+        """Simulator::sample_many (src/sim.rs:272-284): shots basis-state indices."""
+        xs = pack_bits([x], self.nq)
+        nw = xs.shape[1]
+        out = np.zeros((shots, nw), dtype=np.uint64)
+        self.L.pqo_sample_many(self.h, _ptr(xs, ct.c_uint64), shots, ct.c_uint64(seed & (2**64 - 1)),
+                               _ptr(out, ct.c_uint64))
+        return [sum(int(out[i, w]) << (64 * w) for w in range(nw)) for i in range(shots)]
 
     def brute_force(self, x, y):
         xs = pack_bits([x], self.nq)

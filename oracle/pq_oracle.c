@@ -1198,6 +1198,52 @@ int pqo_brute_force(pqo_sim *s, const uint64_t *x, const uint64_t *y, double out
 
 double pqo_last_branches(const pqo_sim *s) { return s->last_branches; }
 
+/* SplitMix64 (src/rng.rs:12-27): new(seed) = seed + golden; next_u64 advances by golden and mixes;
+ * next_f64 = (next_u64 >> 11) / 2^53. */
+typedef struct { uint64_t s; } srng;
+static srng srng_new(uint64_t seed) { srng r = {seed + 0x9E3779B97F4A7C15ull}; return r; }
+static uint64_t srng_u64(srng *r) {
+    r->s += 0x9E3779B97F4A7C15ull;
+    uint64_t z = r->s;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+static double srng_f64(srng *r) { return (double)(srng_u64(r) >> 11) / 9007199254740992.0; }
+
+/* Simulator::sample / sample_many (src/sim.rs:253-284): one seed per shot from Rng::new(seed);
+ * per shot, qubit by qubit, p0 = min(prefix marginal with the new bit 0, p_prev) and the bit is 1
+ * iff next_f64() * p_prev >= p0.  Prefix marginals are marginal_probability of qubits 0..l
+ * (src/sim.rs:232-249 uses the same engines, cached).  out: shots x words bitstrings. */
+void pqo_sample_many(pqo_sim *s, const uint64_t *x, int64_t shots, uint64_t seed, uint64_t *out) {
+    const int nq = s->ps.nq, nw = nq > 0 ? (nq + 63) / 64 : 1;
+    srng r = srng_new(seed);
+    uint64_t *seeds = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)(shots > 0 ? shots : 1));
+    for (int64_t i = 0; i < shots; i++) seeds[i] = srng_u64(&r);
+    int32_t *qs = (int32_t *)malloc(sizeof(int32_t) * (size_t)(nq + 1));
+    uint8_t *bs = (uint8_t *)malloc((size_t)nq + 1);
+    for (int q = 0; q < nq; q++) qs[q] = q;
+    for (int64_t i = 0; i < shots; i++) {
+        srng ri = srng_new(seeds[i]);
+        uint64_t *y = out + (size_t)i * (size_t)nw;
+        for (int w = 0; w < nw; w++) y[w] = 0;
+        double p_prev = 1.0;
+        for (int l = 0; l < nq; l++) {
+            bs[l] = 0;
+            double p0 = pqo_marginal(s, x, l + 1, qs, bs);
+            if (p0 > p_prev) p0 = p_prev;
+            if (srng_f64(&ri) * p_prev >= p0) {
+                bs[l] = 1;
+                y[l >> 6] |= 1ull << (l & 63);
+                p_prev = p_prev - p0 > 0.0 ? p_prev - p0 : 0.0;
+            } else {
+                p_prev = p0;
+            }
+        }
+    }
+    free(bs); free(qs); free(seeds);
+}
+
 /* ------------------------------------------------------------------ dense reference (src/dense.rs) */
 static void diag1(cx *sv, uint64_t dim, int q, cx ph) {
     uint64_t m = 1ull << q;

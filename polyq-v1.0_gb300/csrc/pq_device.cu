@@ -504,7 +504,8 @@ struct pq_sim {
     std::vector<uint8_t> jneg;
     struct Marg {
         Target tg;
-        std::unique_ptr<Plan> plan;
+        std::unique_ptr<Plan> plan;                          // one boundary (pq_marginal)
+        std::map<int64_t, std::unique_ptr<Plan>> many;       // n boundaries (sampling)
     };
     std::map<std::vector<int>, std::unique_ptr<Marg>> marg;
     ~pq_sim() {
@@ -835,6 +836,90 @@ PQ_API pq_status pq_marginal(pq_sim *s, const uint64_t *x, int32_t nmeas, const 
     st = run_host(*M->plan, x, yv.data(), amp, nullptr, false);
     if (st != PQ_OK) return st;
     *out = amp[0] > 0.0 ? amp[0] : 0.0;
+    return PQ_OK;
+}
+
+// ---------------------------------------------------------------- sampling
+// SplitMix64 (src/rng.rs:12-27).
+struct SplitMix {
+    uint64_t s;
+    explicit SplitMix(uint64_t seed) : s(seed + 0x9E3779B97F4A7C15ull) {}
+    uint64_t u64() {
+        s += 0x9E3779B97F4A7C15ull;
+        uint64_t z = s;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    }
+    double f64() { return (double)(u64() >> 11) / 9007199254740992.0; }
+};
+
+// Simulator::sample_many (src/sim.rs:253-284) with the shots batched per qubit: level l
+// evaluates, for every shot at once, the marginal of qubits 0..l with the shot's decided prefix
+// and bit l = 0 (the sandwich engines of prefix l, src/sim.rs:232-249), in one launch; each
+// shot then draws its uniform and takes bit l exactly as the reference does.  A decision whose
+// margin |u * p_prev - p0| lies within the FP32 path's error bound is re-taken on that
+// level's FP64 evaluation, so decisions follow FP64 marginals.
+PQ_API pq_status pq_sample_many(pq_sim *s, const uint64_t *x, int64_t shots, uint64_t seed, uint64_t *out) {
+    if (!s || !x || !out) return fail(PQ_ERR_INVALID_ARG, "null argument");
+    pq_status st = check_n(shots);
+    if (st != PQ_OK) return st;
+    if (s->host_only) return fail(PQ_ERR_NO_DEVICE, "simulator was created by pq_analyze (host structures only)");
+    std::lock_guard<std::mutex> lk(s->mu);
+    CU(cudaSetDevice(s->device));
+    const int nq = s->circ.nq, nw = s->nw;
+    const size_t ns = (size_t)shots;
+    SplitMix root(seed);
+    std::vector<SplitMix> rng;
+    rng.reserve(ns);
+    for (size_t i = 0; i < ns; i++) rng.emplace_back(root.u64());
+    std::vector<uint64_t> X(ns * nw), Y(ns * nw, 0ull);
+    for (size_t i = 0; i < ns; i++) std::memcpy(&X[i * nw], x, sizeof(uint64_t) * nw);
+    std::vector<double> p_prev(ns, 1.0), amp(2 * ns), err(ns), u(ns);
+    std::vector<char> tie(ns, 0);
+    std::vector<int32_t> qs(nq);
+    for (int q = 0; q < nq; q++) qs[q] = q;
+    for (int l = 0; l < nq; l++) {
+        pq_sim::Marg *M = nullptr;
+        st = marg_target(s, qs.data(), l + 1, &M);
+        if (st != PQ_OK) return st;
+        auto &slot = M->many[shots];
+        if (!slot) {
+            auto P = std::make_unique<Plan>();
+            std::vector<Segment> segs{{&M->tg, shots}};
+            st = build_plan(segs, nw, s->stream, s->tu, *P);
+            if (st != PQ_OK) return st;
+            slot = std::move(P);
+        }
+        Plan &P = *slot;
+        st = run_host(P, X.data(), Y.data(), amp.data(), err.data(), false);
+        if (st != PQ_OK) return st;
+        bool any_tie = false;
+        for (size_t i = 0; i < ns; i++) {
+            u[i] = rng[i].f64();
+            const double p0 = std::min(std::max(amp[2 * i], 0.0), p_prev[i]);
+            tie[i] = std::fabs(u[i] * p_prev[i] - p0) <= err[i] + 1e-15 * p0;
+            any_tie = any_tie || tie[i];
+        }
+        if (any_tie) {
+            CU(enqueue_core(P, 1));
+            CU(cudaMemcpyAsync(P.hout.p, P.out.p, ns * 16, cudaMemcpyDeviceToHost, P.stream));
+            CU(cudaStreamSynchronize(P.stream));
+            const double *ho = P.hout.as<double>();
+            for (size_t i = 0; i < ns; i++)
+                if (tie[i]) amp[2 * i] = ho[2 * i];
+        }
+        for (size_t i = 0; i < ns; i++) {
+            const double p0 = std::min(std::max(amp[2 * i], 0.0), p_prev[i]);
+            if (u[i] * p_prev[i] >= p0) {
+                Y[i * nw + (l >> 6)] |= 1ull << (l & 63);
+                p_prev[i] = std::max(p_prev[i] - p0, 0.0);
+            } else {
+                p_prev[i] = p0;
+            }
+        }
+    }
+    std::memcpy(out, Y.data(), sizeof(uint64_t) * ns * nw);
     return PQ_OK;
 }
 

@@ -178,6 +178,16 @@ class Simulator:
                                     _p(bs, ct.c_uint8), _p(out, ct.c_double)))
         return float(out[0])
 
+    def sample_many(self, input: int, shots: int, seed: int):
+        """src/sim.rs:272-284 / src/pybind.rs sample_many: `shots` measurement outcomes of C|input>
+        as basis-state indices (the reference's SplitMix64 streams: same seed, same samples)."""
+        xs = pack_bits([input], self.num_qubits)
+        nw = xs.shape[1]
+        out = np.zeros((int(shots), nw), dtype=np.uint64)
+        N.check(self._L.pq_sample_many(self._h, _p(xs, ct.c_uint64), int(shots), ct.c_uint64(seed & (2**64 - 1)),
+                                       _p(out, ct.c_uint64)))
+        return [sum(int(out[i, w]) << (64 * w) for w in range(nw)) for i in range(int(shots))]
+
     def statevector(self, input: int = 0) -> np.ndarray:
         """All 2^n amplitudes for one input (src/sim.rs:201-213), as one batched launch."""
         n = self.num_qubits

@@ -261,3 +261,15 @@ def test_known_answer_fixture_matches_oracle():
         s = O.OracleSim(c)
         for x, y, re, im in case["values"]:
             assert abs(s.amplitude(x, y) - complex(re, im)) < case["tol"]
+
+
+def test_sampling_follows_the_distribution():
+    # src/sim.rs:382-399 (shots reduced from 40000 to 4000, tolerance scaled by sqrt(10))
+    c = Circuit(3)
+    c.h(0).t(0).h(0).cx(0, 1).h(2).t(2).h(2).cz(1, 2).h(1).t(1).h(1)
+    sv = O.dense_statevector(c, 0)
+    sim = O.OracleSim(c)
+    shots = 4000
+    hist = np.bincount(sim.sample_many(0, shots, 1234), minlength=8)
+    for y in range(8):
+        assert abs(abs(sv[y]) ** 2 - hist[y] / shots) < 0.012 * 10 ** 0.5
