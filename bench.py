@@ -16,7 +16,7 @@ roofline   enumeration kernel: its FP32 FMA-pipe work (4 ops per enumerated bran
            over its event-timed duration, against the fma.f32 rate measured on the device;
            reference_form beside it: the reference engine's integer work for the same branches
            (5 W_o + 6 W_g int64 ops each) against the measured lop3 / popc rates
-workloads  --workload many_boundaries (default) | batched | serve | small | rotations
+workloads  --workload many_boundaries (default) | batched | serve | small | rotations | sample
 cpu_baseline  the CPU oracle (a restatement of the reference engine) on all host threads
 --impl reference  times the same CPU restatement on the same workload (bounded sample)
 """
@@ -618,6 +618,41 @@ def run_small(args):
     return 0
 
 
+def run_sample(args):
+    """Simulator::sample_many on the small circuit (n=20, 200 gates, 16 T, seed 2): shots/s on the
+    device (all shots advance together, one launch per qubit) beside the CPU restatement on a
+    bounded number of shots; the two give identical samples for the same seed."""
+    pq, N = _gpu_setup()
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    from polyq_gb300.rng import workload_small
+    c = workload_small(2)
+    sim = pq.Simulator(c)
+    shots = 4096
+    sim.sample_many(0, shots, 1)  # prefix engines built and plans captured outside the timing
+    times = []
+    for k in range(max(1, args.steps)):
+        t0 = time.perf_counter()
+        got = sim.sample_many(0, shots, 100 + k)
+        times.append(time.perf_counter() - t0)
+    gpu_rate = shots / (sum(times) / len(times))
+    cpu_shots = 512
+    osim = oracle.OracleSim(c)
+    osim.sample_many(0, 2, 1)
+    t0 = time.perf_counter()
+    want = osim.sample_many(0, cpu_shots, 100)
+    cpu_s = time.perf_counter() - t0
+    line = {"metric": METRIC, "workload": "sample", "value": gpu_rate, "unit": "shots/s", "n_gpus": 1,
+            "higher_is_better": True, "data": "synthetic", "shots_per_step": shots,
+            "ms_per_step": 1e3 * sum(times) / len(times),
+            "same_samples_as_cpu_restatement": sim.sample_many(0, cpu_shots, 100) == want,
+            "cpu_baseline": {"value": cpu_shots / cpu_s, "unit": "shots/s", "cores": cpu_threads(), "kind": "port",
+                             "sample": "%d shots; prefix engines built per call, shots in parallel" % cpu_shots},
+            "config": {"workload": "sample_many: n=20, 200 gates, 16 T (seed 2), x=0, %d shots" % shots}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_rotations(args):
     """Arbitrary angles: rz(theta) slots plus CCZ layers, FP32-compensated vs device FP64 per
     amplitude; a 20-qubit variant also against the dense statevector."""
@@ -683,7 +718,7 @@ def main():
                     "blocks_per_sm[,unit_chunks] (implies --no-autotune)")
     ap.add_argument("--boundaries", type=int, default=4096, help="boundary count (profiling of smaller cases)")
     ap.add_argument("--workload", default="many_boundaries",
-                    choices=["many_boundaries", "batched", "serve", "small", "rotations"])
+                    choices=["many_boundaries", "batched", "serve", "small", "rotations", "sample"])
     ap.add_argument("--rate", type=float, default=5000.0, help="serve: offered requests/s")
     ap.add_argument("--duration", type=float, default=2.0, help="serve: seconds of arrivals")
     ap.add_argument("--slots", type=int, default=256, help="serve: requests per wave")
@@ -700,6 +735,8 @@ def main():
         return run_serve(args)
     if args.workload == "small":
         return run_small(args)
+    if args.workload == "sample":
+        return run_sample(args)
     if args.workload == "rotations":
         return run_rotations(args)
     return run_gb300(args)

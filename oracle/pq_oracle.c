@@ -1213,35 +1213,66 @@ static double srng_f64(srng *r) { return (double)(srng_u64(r) >> 11) / 900719925
 
 /* Simulator::sample / sample_many (src/sim.rs:253-284): one seed per shot from Rng::new(seed);
  * per shot, qubit by qubit, p0 = min(prefix marginal with the new bit 0, p_prev) and the bit is 1
- * iff next_f64() * p_prev >= p0.  Prefix marginals are marginal_probability of qubits 0..l
- * (src/sim.rs:232-249 uses the same engines, cached).  out: shots x words bitstrings. */
+ * iff next_f64() * p_prev >= p0.  The prefix marginal of qubits 0..l is the sandwich engine with
+ * those junctions fixed, built once per prefix length as the reference's prefix_engines
+ * (src/sim.rs:232-249); all shots' marginals of one prefix length are evaluated in one call
+ * (threads over shots and chunks, as the reference's parallel map over shots).
+ * out: shots x words bitstrings. */
 void pqo_sample_many(pqo_sim *s, const uint64_t *x, int64_t shots, uint64_t seed, uint64_t *out) {
     const int nq = s->ps.nq, nw = nq > 0 ? (nq + 63) / 64 : 1;
+    if (!s->have_sw) {
+        s->junction = (int *)malloc(sizeof(int) * (size_t)(nq + 1));
+        s->jneg = (uint8_t *)malloc((size_t)nq + 1);
+        s->sw = ps_sandwich(&s->c, s->junction, s->jneg);
+        s->have_sw = 1;
+    }
+    const size_t ns = (size_t)(shots > 0 ? shots : 0);
     srng r = srng_new(seed);
-    uint64_t *seeds = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)(shots > 0 ? shots : 1));
-    for (int64_t i = 0; i < shots; i++) seeds[i] = srng_u64(&r);
-    int32_t *qs = (int32_t *)malloc(sizeof(int32_t) * (size_t)(nq + 1));
-    uint8_t *bs = (uint8_t *)malloc((size_t)nq + 1);
-    for (int q = 0; q < nq; q++) qs[q] = q;
-    for (int64_t i = 0; i < shots; i++) {
-        srng ri = srng_new(seeds[i]);
-        uint64_t *y = out + (size_t)i * (size_t)nw;
-        for (int w = 0; w < nw; w++) y[w] = 0;
-        double p_prev = 1.0;
-        for (int l = 0; l < nq; l++) {
-            bs[l] = 0;
-            double p0 = pqo_marginal(s, x, l + 1, qs, bs);
-            if (p0 > p_prev) p0 = p_prev;
-            if (srng_f64(&ri) * p_prev >= p0) {
-                bs[l] = 1;
-                y[l >> 6] |= 1ull << (l & 63);
-                p_prev = p_prev - p0 > 0.0 ? p_prev - p0 : 0.0;
+    srng *rs = (srng *)malloc(sizeof(srng) * (ns + 1));
+    for (size_t i = 0; i < ns; i++) rs[i] = srng_new(srng_u64(&r));
+    double *p_prev = (double *)malloc(sizeof(double) * (ns + 1));
+    for (size_t i = 0; i < ns; i++) p_prev[i] = 1.0;
+    for (size_t i = 0; i < ns * (size_t)nw; i++) out[i] = 0;
+    const int amax = 2 * nq + nq + 1;
+    asg_t *abuf = (asg_t *)malloc(sizeof(asg_t) * (ns + 1) * (size_t)amax);
+    asg_t **al = (asg_t **)malloc(sizeof(asg_t *) * (ns + 1));
+    int *an = (int *)malloc(sizeof(int) * (ns + 1));
+    size_t *slot = (size_t *)malloc(sizeof(size_t) * (ns + 1));
+    cx *val = (cx *)malloc(sizeof(cx) * (ns + 1));
+    int *f = (int *)malloc(sizeof(int) * (size_t)(amax + 1));
+    for (int l = 0; l < nq; l++) {
+        int nf = ps_io_vars(&s->sw, f);
+        for (int q = 0; q <= l; q++) {
+            int j = s->junction[q], seen = 0;
+            for (int k = 0; k < nf; k++) if (f[k] == j) { seen = 1; break; }
+            if (!seen) f[nf++] = j;
+        }
+        rank_engine eng = build_engine(&s->sw, f, nf, s->strategy, s->pairs);
+        size_t nv = 0;
+        for (size_t i = 0; i < ns; i++) {
+            const uint64_t *y = out + i * (size_t)nw;  /* decided prefix, bit l still 0 */
+            asg_t *a = abuf + i * (size_t)amax;
+            int na = 0, ok = 1;
+            for (int q = 0; q < nq && ok; q++) ok = asg_put(a, &na, q, bit_of(x, q));
+            for (int q = 0; q < nq && ok; q++) ok = asg_put(a, &na, s->sw.outputs[q], bit_of(x, q) ^ s->sw.out_neg[q]);
+            for (int q = 0; q <= l && ok; q++) ok = asg_put(a, &na, s->junction[q], bit_of(y, q) ^ s->jneg[q]);
+            slot[i] = ok ? nv : (size_t)-1;
+            if (ok) { al[nv] = a; an[nv] = na; nv++; }
+        }
+        if (nv) eval_many(&eng, (int)nv, al, an, val, default_threads(0));
+        rank_free(&eng);
+        for (size_t i = 0; i < ns; i++) {
+            double p0 = slot[i] == (size_t)-1 ? 0.0 : (val[slot[i]].re > 0.0 ? val[slot[i]].re : 0.0);
+            if (p0 > p_prev[i]) p0 = p_prev[i];
+            if (srng_f64(&rs[i]) * p_prev[i] >= p0) {
+                out[i * (size_t)nw + (size_t)(l >> 6)] |= 1ull << (l & 63);
+                p_prev[i] = p_prev[i] - p0 > 0.0 ? p_prev[i] - p0 : 0.0;
             } else {
-                p_prev = p0;
+                p_prev[i] = p0;
             }
         }
     }
-    free(bs); free(qs); free(seeds);
+    free(f); free(val); free(slot); free(an); free(al); free(abuf); free(p_prev); free(rs);
 }
 
 /* ------------------------------------------------------------------ dense reference (src/dense.rs) */
