@@ -110,6 +110,13 @@ PQ_API pq_status pq_probabilities(pq_sim *sim, int64_t n, const uint64_t *x, con
  * pairs.  The sandwich engine of each distinct measured-qubit set is built once and cached. */
 PQ_API pq_status pq_marginal(pq_sim *sim, const uint64_t *x, int32_t nmeas, const int32_t *qubits,
                              const uint8_t *outcomes, double *out);
+/* Simulator::amplitude_estimate -- sim.rs:184-193 / rank.rs:149-171: unbiased Monte-Carlo
+ * estimate of <y|C|x> from `samples` draws with the reference's seeding.  One branch engine:
+ * points of its branch subspace (engine.rs:616-659; the exact sum when 2^d <= samples; d <= 64);
+ * 2^p engines: branch engines drawn uniformly and evaluated exactly.  out: (re, im);
+ * stderr (optional): the standard error. */
+PQ_API pq_status pq_amplitude_estimate(pq_sim *sim, const uint64_t *x, const uint64_t *y, int64_t samples,
+                                       uint64_t seed, double *out, double *stderr_out);
 /* Simulator::sample_many -- sim.rs:253-284: `shots` computational-basis samples of C|x>, drawn
  * by the chain rule over qubit prefixes with the reference's SplitMix64 streams (one seed per
  * shot from seed), so the same seed gives the reference's samples.  out: shots bitstrings.

@@ -58,6 +58,7 @@ def lib():
             L.pqo_marginal.restype = ct.c_double
             L.pqo_marginal.argtypes = [P, u64p, ct.c_int, i32p, u8p]
             L.pqo_sample_many.argtypes = [P, u64p, ct.c_int64, ct.c_uint64, u64p]
+            L.pqo_amplitude_estimate.argtypes = [P, u64p, u64p, ct.c_int64, ct.c_uint64, f64p]
             L.pqo_brute_force.restype = ct.c_int
             L.pqo_brute_force.argtypes = [P, u64p, u64p, f64p]
             L.pqo_dense_statevector.argtypes = [ct.c_int, ct.c_int, u8p, i32p, i32p, u32p, u64p, f64p]
@@ -155,6 +156,15 @@ class OracleSim:
         bs = np.array([int(b) for _, b in measured] or [0], dtype=np.uint8)
         return float(self.L.pqo_marginal(self.h, _ptr(xs, ct.c_uint64), len(measured), _ptr(qs, ct.c_int32),
                                          _ptr(bs, ct.c_uint8)))
+
+    def amplitude_estimate(self, x, y, samples, seed):
+        """Simulator::amplitude_estimate (src/sim.rs:184-193): (re, im, standard error)."""
+        xs = pack_bits([x], self.nq)
+        ys = pack_bits([y], self.nq)
+        out = np.zeros(3, dtype=np.float64)
+        self.L.pqo_amplitude_estimate(self.h, _ptr(xs, ct.c_uint64), _ptr(ys, ct.c_uint64), samples,
+                                      ct.c_uint64(seed & (2**64 - 1)), _ptr(out, ct.c_double))
+        return float(out[0]), float(out[1]), float(out[2])
 
     def sample_many(self, x, shots, seed):
         """Simulator::sample_many (src/sim.rs:272-284): shots basis-state indices."""

@@ -1211,6 +1211,106 @@ static uint64_t srng_u64(srng *r) {
 }
 static double srng_f64(srng *r) { return (double)(srng_u64(r) >> 11) / 9007199254740992.0; }
 
+/* Engine::estimate (src/engine.rs:616-659): prepare; the exact sum when 2^d <= samples;
+ * otherwise samples in chunks of 1024, chunk ci drawing from Rng::new(seed ^ ci * golden),
+ * one fresh word per 64 coordinates; x = weight(sv) * ROOT8[phase8(u)].  Chunk sums are
+ * accumulated in chunk order (the reference's rayon reduce groups them differently). */
+static void engine_estimate(const engine *E, const uint8_t *values, int64_t samples, uint64_t seed, cx *val, double *se) {
+    const uint64_t golden = 0x9E3779B97F4A7C15ull;
+    *val = C(0, 0);
+    *se = 0.0;
+    prep_t p;
+    prep_init(&p, E);
+    if (!engine_prepare(E, values, &p)) { prep_free(&p); return; }
+    const elim_t *e = &E->el;
+    const int d = e->d;
+    const cx norm = cscale(phase_to_complex(p.phase), engine_magnitude(E));
+    if (d < 63 && (1ull << d) <= (uint64_t)samples) {
+        cx sum = C(0, 0);
+        for (uint64_t ch = 0; ch < (1ull << engine_nchunks_log2(E)); ch++) sum = cadd(sum, engine_chunk(E, &p, ch));
+        *val = cmul(norm, sum);
+        prep_free(&p);
+        return;
+    }
+    const int64_t chunks = (samples + 1023) / 1024;
+    cx sum = C(0, 0);
+    double sq = 0.0;
+    uvec u; uv_init(&u, &E->st);
+    bv sv = bv_clone(&p.s0);
+    for (int64_t ci = 0; ci < chunks; ci++) {
+        srng r = srng_new(seed ^ ((uint64_t)ci * golden));
+        const int64_t n_here = samples - ci * 1024 < 1024 ? samples - ci * 1024 : 1024;
+        for (int64_t k = 0; k < n_here; k++) {
+            uv_copy(&u, &p.u);
+            bv_free(&sv);
+            sv = bv_clone(&p.s0);
+            uint64_t word = 0;
+            for (int j = 0; j < d; j++) {
+                if (j % 64 == 0) word = srng_u64(&r);
+                if ((word >> (j % 64)) & 1) { uv_xor(&u, &e->kernel_u[j]); bv_xor(&sv, &e->kernel[j]); }
+            }
+            const cx x = cmul(engine_weight(E, &sv), ROOT8[phase8(&E->dg, &u)]);
+            sum = cadd(sum, x);
+            sq += x.re * x.re + x.im * x.im;
+        }
+    }
+    uv_free(&u); bv_free(&sv); prep_free(&p);
+    const double n = (double)samples;
+    const cx mean = C(sum.re / n, sum.im / n);
+    double var = sq / n - (mean.re * mean.re + mean.im * mean.im);
+    if (var < 0.0) var = 0.0;
+    const double scale = ldexp(1.0, d);
+    *val = cscale(cmul(norm, mean), scale);
+    *se = sqrt(norm.re * norm.re + norm.im * norm.im) * scale * sqrt(var / n);
+}
+
+/* Simulator::amplitude_estimate (src/sim.rs:184-193) -> RankEngine::estimate (src/rank.rs:149-171):
+ * one engine: Engine::estimate; 2^p engines: samples i draw Rng::new(seed ^ i * golden).below(nb)
+ * and evaluate that engine exactly; value nb * mean, stderr nb * sqrt(var / n). */
+void pqo_amplitude_estimate(pqo_sim *s, const uint64_t *x, const uint64_t *y, int64_t samples, uint64_t seed,
+                            double out[3]) {
+    const uint64_t golden = 0x9E3779B97F4A7C15ull;
+    out[0] = out[1] = out[2] = 0.0;
+    asg_t *a = (asg_t *)malloc(sizeof(asg_t) * (size_t)(2 * s->ps.nq + 1));
+    int na = ps_boundary(&s->ps, x, y, a);
+    if (na < 0) { free(a); return; }
+    const rank_engine *r = &s->eng;
+    if (r->nbr == 1) {
+        const engine *E = r->br[0];
+        uint8_t *vals = (uint8_t *)malloc((size_t)E->nf + 1);
+        values_from_asg(E, a, na, vals);
+        cx v; double se;
+        engine_estimate(E, vals, samples, seed, &v, &se);
+        out[0] = v.re; out[1] = v.im; out[2] = se;
+        free(vals); free(a);
+        return;
+    }
+    /* exact value of every branch engine once, then the sampled mean */
+    rank_engine one; one.nbr = 1; one.pairs = 0;
+    cx *vb = (cx *)malloc(sizeof(cx) * (size_t)r->nbr);
+    asg_t *al[1] = {a};
+    int an[1] = {na};
+    for (int b = 0; b < r->nbr; b++) {
+        engine *eb = r->br[b];
+        one.br = &eb;
+        eval_many(&one, 1, al, an, &vb[b], default_threads(0));
+    }
+    cx sum = C(0, 0);
+    double sq = 0.0;
+    for (int64_t i = 0; i < samples; i++) {
+        srng ri = srng_new(seed ^ ((uint64_t)i * golden));
+        const cx v = vb[srng_u64(&ri) % (uint64_t)r->nbr];
+        sum = cadd(sum, v);
+        sq += v.re * v.re + v.im * v.im;
+    }
+    const double n = (double)samples, nb = (double)r->nbr;
+    const cx mean = C(sum.re / n, sum.im / n);
+    double var = sq / n - (mean.re * mean.re + mean.im * mean.im);
+    if (var < 0.0) var = 0.0;
+    out[0] = mean.re * nb; out[1] = mean.im * nb; out[2] = nb * sqrt(var / n);
+    free(vb); free(a);
+}
+
 /* Simulator::sample / sample_many (src/sim.rs:253-284): one seed per shot from Rng::new(seed);
  * per shot, qubit by qubit, p0 = min(prefix marginal with the new bit 0, p_prev) and the bit is 1
  * iff next_f64() * p_prev >= p0.  The prefix marginal of qubits 0..l is the sandwich engine with

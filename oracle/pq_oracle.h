@@ -45,6 +45,8 @@ double pqo_marginal(pqo_sim *s, const uint64_t *x, int nmeas, const int32_t *qub
 /* Path-sum brute force (src/pathsum.rs:454-489) of <y|C|x>; returns -1 if > 26 free vars. */
 int pqo_brute_force(pqo_sim *s, const uint64_t *x, const uint64_t *y, double out[2]);
 void pqo_sample_many(pqo_sim *s, const uint64_t *x, int64_t shots, uint64_t seed, uint64_t *out);
+void pqo_amplitude_estimate(pqo_sim *s, const uint64_t *x, const uint64_t *y, int64_t samples, uint64_t seed,
+                            double out[3]);
 
 /* Dense statevector (src/dense.rs:12-27); out has 2*2^nq doubles. */
 void pqo_dense_statevector(int nq, int ngates, const uint8_t *op, const int32_t *q0, const int32_t *q1,

@@ -16,6 +16,7 @@
 #include <array>
 #include <chrono>
 #include <cmath>
+#include <complex>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
@@ -839,7 +840,7 @@ PQ_API pq_status pq_marginal(pq_sim *s, const uint64_t *x, int32_t nmeas, const 
     return PQ_OK;
 }
 
-// ---------------------------------------------------------------- sampling
+// ---------------------------------------------------------------- Monte-Carlo estimate
 // SplitMix64 (src/rng.rs:12-27).
 struct SplitMix {
     uint64_t s;
@@ -854,6 +855,122 @@ struct SplitMix {
     double f64() { return (double)(u64() >> 11) / 9007199254740992.0; }
 };
 
+static std::complex<double> phase_value(uint32_t p) {  // src/phase.rs:60-66
+    static const double h = 0.70710678118654752440;
+    static const double r8[16] = {1, 0, h, h, 0, 1, -h, h, -1, 0, -h, -h, 0, -1, h, -h};
+    if ((p & ((1u << 29) - 1u)) == 0) {
+        const int k = (int)(p >> 29);
+        return {r8[2 * k], r8[2 * k + 1]};
+    }
+    const double th = 2.0 * M_PI * (double)p / 4294967296.0;
+    return {std::cos(th), std::sin(th)};
+}
+
+// Simulator::amplitude_estimate (src/sim.rs:184-193) -> RankEngine::estimate (src/rank.rs:149-171).
+PQ_API pq_status pq_amplitude_estimate(pq_sim *s, const uint64_t *x, const uint64_t *y, int64_t samples,
+                                       uint64_t seed, double *out, double *stderr_out) {
+    if (!s || !x || !y || !out) return fail(PQ_ERR_INVALID_ARG, "null argument");
+    if (samples <= 0 || samples > (1LL << 40)) return fail(PQ_ERR_INVALID_ARG, "samples must be in 1..2^40");
+    if (s->host_only) return fail(PQ_ERR_NO_DEVICE, "simulator was created by pq_analyze (host structures only)");
+    std::lock_guard<std::mutex> lk(s->mu);
+    CU(cudaSetDevice(s->device));
+    const uint64_t golden = 0x9E3779B97F4A7C15ull;
+    const int nb = (int)s->main.dev.size();
+    const int nw = s->nw;
+    out[0] = out[1] = 0.0;
+    if (stderr_out) *stderr_out = 0.0;
+    if (nb > 1) {
+        // 2^p stabiliser branches: sample branch indices, evaluate each distinct one exactly
+        std::map<int, int64_t> mult;
+        for (int64_t i = 0; i < samples; i++) {
+            SplitMix r(seed ^ ((uint64_t)i * golden));
+            mult[(int)(r.u64() % (uint64_t)nb)]++;
+        }
+        std::vector<Target> views(mult.size());
+        std::vector<Segment> segs;
+        std::vector<int64_t> counts;
+        size_t v = 0;
+        for (const auto &kv : mult) {
+            views[v].dev.push_back(s->main.dev[(size_t)kv.first]);
+            views[v].iom_dev = s->main.iom_dev;
+            views[v].max_words = s->main.max_words;
+            segs.push_back({&views[v], 1});
+            counts.push_back(kv.second);
+            v++;
+        }
+        Plan P;
+        pq_status st = build_plan(segs, nw, s->stream, s->tu, P);
+        if (st != PQ_OK) return st;
+        std::vector<uint64_t> X(segs.size() * nw), Y(segs.size() * nw);
+        for (size_t k = 0; k < segs.size(); k++) {
+            std::memcpy(&X[k * nw], x, sizeof(uint64_t) * nw);
+            std::memcpy(&Y[k * nw], y, sizeof(uint64_t) * nw);
+        }
+        std::vector<double> amp(2 * segs.size());
+        st = run_host(P, X.data(), Y.data(), amp.data(), nullptr, false);
+        if (st != PQ_OK) return st;
+        double sx = 0.0, sy = 0.0, sq = 0.0;
+        for (size_t k = 0; k < segs.size(); k++) {
+            const double m = (double)counts[k];
+            sx += m * amp[2 * k];
+            sy += m * amp[2 * k + 1];
+            sq += m * (amp[2 * k] * amp[2 * k] + amp[2 * k + 1] * amp[2 * k + 1]);
+        }
+        const double n = (double)samples, mx = sx / n, my = sy / n;
+        const double var = std::max(sq / n - (mx * mx + my * my), 0.0);
+        out[0] = mx * nb;
+        out[1] = my * nb;
+        if (stderr_out) *stderr_out = nb * std::sqrt(var / n);
+        return PQ_OK;
+    }
+    const EngineDev &E = s->main.dev[0];
+    if (E.d < 63 && (1LL << E.d) <= samples) {  // small subspace: the exact sum
+        Plan *P = nullptr;
+        pq_status st = sim_plan(s, 1, &P);
+        if (st != PQ_OK) return st;
+        return run_host(*P, x, y, out, nullptr, false);
+    }
+    if (E.d > 64) return fail(PQ_ERR_UNSUPPORTED, "Monte-Carlo estimate supports branch dimensions up to 64");
+    Plan *P = nullptr;
+    pq_status st = sim_plan(s, 1, &P);
+    if (st != PQ_OK) return st;
+    const size_t bw = (size_t)nw * 8;
+    CU(cudaMemcpyAsync(P->x.p, x, bw, cudaMemcpyHostToDevice, P->stream));
+    CU(cudaMemcpyAsync(P->y.p, y, bw, cudaMemcpyHostToDevice, P->stream));
+    prepare_kernel<<<P->grid_prep, 128, (size_t)4 * P->smem_words * 8, P->stream>>>(P->args);
+    CU(cudaGetLastError());
+    const int grid = (int)std::max<long long>(1, std::min<long long>((samples + 255) / 256, (long long)sm_count() * 8));
+    DevMem part;
+    CU(part.alloc((size_t)grid * 3 * sizeof(double)));
+    mc_kernel<<<grid, 256, 0, P->stream>>>(P->engines.as<EngineDev>(), P->jobs.as<JobDev>(), seed, (long long)samples,
+                                            part.as<double>());
+    CU(cudaGetLastError());
+    JobDev J;
+    std::vector<double> hp((size_t)grid * 3);
+    CU(cudaMemcpyAsync(&J, P->jobs.p, sizeof(JobDev), cudaMemcpyDeviceToHost, P->stream));
+    CU(cudaMemcpyAsync(hp.data(), part.p, hp.size() * sizeof(double), cudaMemcpyDeviceToHost, P->stream));
+    CU(cudaStreamSynchronize(P->stream));
+    if (J.vanish) return PQ_OK;  // prepare found no surviving subspace: (0, 0), src/engine.rs:618
+    double sx = 0.0, sy = 0.0, sq = 0.0;
+    for (int b = 0; b < grid; b++) {
+        sx += hp[3 * b];
+        sy += hp[3 * b + 1];
+        sq += hp[3 * b + 2];
+    }
+    const double n = (double)samples;
+    const std::complex<double> mean(sx / n, sy / n);
+    const double var = std::max(sq / n - std::norm(mean), 0.0);
+    const double scale = std::ldexp(1.0, E.d);
+    // norm = phase * magnitude (src/engine.rs:620), and the Z8 root of the index at s = 0
+    const std::complex<double> norm = phase_value(J.phase) * phase_value((J.k0 & 7u) << 29) * pow2_half(E.mag2 - E.num_h);
+    const std::complex<double> val = norm * mean * scale;
+    out[0] = val.real();
+    out[1] = val.imag();
+    if (stderr_out) *stderr_out = std::abs(norm) * scale * std::sqrt(var / n);
+    return PQ_OK;
+}
+
+// ---------------------------------------------------------------- sampling
 // Simulator::sample_many (src/sim.rs:253-284) with the shots batched per qubit: level l
 // evaluates, for every shot at once, the marginal of qubits 0..l with the shot's decided prefix
 // and bit l = 0 (the sandwich engines of prefix l, src/sim.rs:232-249), in one launch; each

@@ -588,4 +588,63 @@ __global__ void out_reduce_kernel(KArgs a) {
     }
 }
 
+// ------------------------------------------------------------------------------ Monte Carlo
+// Engine::estimate (src/engine.rs:616-659): the mean of c(s) i^{m(s)} over `samples` points s of
+// the branch subspace.  Sample k belongs to chunk ci = k / 1024, whose generator is
+// Rng::new(seed ^ ci * golden) (src/rng.rs:12-27); its point is the (k mod 1024)-th next_u64 of
+// that stream (one word: d <= 64), masked to d bits.  SplitMix64's state after n draws is
+// init + n * golden, so every sample's word is computed directly.  FP64 throughout; one
+// (sum.re, sum.im, sum |x|^2) partial per block, summed on the host in block order.
+__device__ __forceinline__ uint64_t splitmix_at(uint64_t state) {
+    uint64_t z = state;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+__global__ void __launch_bounds__(256) mc_kernel(const EngineDev *__restrict__ Ep, const JobDev *__restrict__ Jp,
+                                                 uint64_t seed, long long samples, double *partials) {
+    const uint64_t golden = 0x9E3779B97F4A7C15ull;
+    const EngineDev &E = *Ep;
+    const JobDev &J = *Jp;
+    __shared__ uint64_t sG[64], sR[64];
+    __shared__ uint8_t sLp[64];
+    __shared__ double red[3][256];
+    for (int j = threadIdx.x; j < E.d; j += blockDim.x) {
+        sG[j] = E.G[j];
+        sR[j] = E.R[j];
+        sLp[j] = J.Lp[j];
+    }
+    __syncthreads();
+    const uint64_t dmask = E.d >= 64 ? ~0ull : ((1ull << E.d) - 1ull);
+    const uint64_t lomask = E.DI >= 64 ? ~0ull : ((1ull << E.DI) - 1ull);
+    double sx = 0.0, sy = 0.0, sq = 0.0;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < samples;
+         k += (long long)gridDim.x * blockDim.x) {
+        const uint64_t ci = (uint64_t)(k >> 10), kk = (uint64_t)(k & 1023);
+        const uint64_t s = splitmix_at((seed ^ (ci * golden)) + golden + (kk + 1ull) * golden) & dmask;
+        uint32_t m;
+        uint64_t yy;
+        chunk_start(sLp, sG, sR, J.y0, s, m, yy);
+        double2 w = E.tlo64[s & lomask];
+        for (int sl = 0; sl < E.nsl_tp; sl++) w = cmul_d(w, E.tp64[sl * 256 + (int)((yy >> (8 * sl)) & 255ull)]);
+        w = cmul_d(w, chunk_high_weight(E, s));
+        w = rot4d(w, m & 3u);
+        sx += w.x;
+        sy += w.y;
+        sq += w.x * w.x + w.y * w.y;
+    }
+    red[0][threadIdx.x] = sx;
+    red[1][threadIdx.x] = sy;
+    red[2][threadIdx.x] = sq;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o)
+            for (int q = 0; q < 3; q++) red[q][threadIdx.x] += red[q][threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int q = 0; q < 3; q++) partials[3 * blockIdx.x + q] = red[q][0];
+}
+
 }  // namespace pq

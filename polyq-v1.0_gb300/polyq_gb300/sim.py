@@ -178,6 +178,18 @@ class Simulator:
                                     _p(bs, ct.c_uint8), _p(out, ct.c_double)))
         return float(out[0])
 
+    def amplitude_estimate(self, input: int, output: int, samples: int, seed: int):
+        """src/pybind.rs:150-153 / src/sim.rs:184-193: (re, im, standard_error) of an unbiased
+        Monte-Carlo estimate of <output|C|input>."""
+        xs = pack_bits([input], self.num_qubits)
+        ys = pack_bits([output], self.num_qubits)
+        out = np.zeros(2, dtype=np.float64)
+        se = np.zeros(1, dtype=np.float64)
+        N.check(self._L.pq_amplitude_estimate(self._h, _p(xs, ct.c_uint64), _p(ys, ct.c_uint64), int(samples),
+                                              ct.c_uint64(seed & (2**64 - 1)), _p(out, ct.c_double),
+                                              _p(se, ct.c_double)))
+        return float(out[0]), float(out[1]), float(se[0])
+
     def sample_many(self, input: int, shots: int, seed: int):
         """src/sim.rs:272-284 / src/pybind.rs sample_many: `shots` measurement outcomes of C|input>
         as basis-state indices (the reference's SplitMix64 streams: same seed, same samples)."""

@@ -273,3 +273,37 @@ def test_sampling_follows_the_distribution():
     hist = np.bincount(sim.sample_many(0, shots, 1234), minlength=8)
     for y in range(8):
         assert abs(abs(sv[y]) ** 2 - hist[y] / shots) < 0.012 * 10 ** 0.5
+
+
+def _mc_cases(seed, iters, nq, lo, hi):
+    rng = Rng(seed)
+    for _ in range(iters):
+        c = random_layered(nq, 3, rng)
+        sim = O.OracleSim(c)
+        st = sim.stats()
+        if st["branch_dim"] < lo or st["branch_dim"] > hi or st["pairs"] != 0:
+            continue
+        yield c, sim, rng.below(1 << nq)
+
+
+def test_subspace_monte_carlo_is_unbiased():
+    # src/approx.rs:188-207 (there 2^d <= samples: the exact fallback)
+    tested = 0
+    for c, sim, y in _mc_cases(61, 40, 4, 6, 12):
+        tested += 1
+        want = O.dense_statevector(c, 0)[y]
+        re, im, se = sim.amplitude_estimate(0, y, 200_000, 3)
+        assert abs(complex(re, im) - want) < 6.0 * se + 5e-3
+    assert tested >= 3
+
+
+def test_subspace_monte_carlo_sampled():
+    # fewer samples than branches: the sampled estimate, unbiased within its standard error
+    tested = 0
+    for c, sim, y in _mc_cases(61, 40, 4, 6, 12):
+        tested += 1
+        want = O.dense_statevector(c, 0)[y]
+        re, im, se = sim.amplitude_estimate(0, y, 40, 11)
+        assert se > 0.0
+        assert abs(complex(re, im) - want) < 6.0 * se + 5e-3
+    assert tested >= 3
