@@ -251,13 +251,18 @@ __device__ __forceinline__ void gray_chunk_rot(const float4 *__restrict__ W, uin
         const int j = 3 + ctz32(g + 1);
         const uint32_t down = (sidx >> j) & 1u;  // bit j is set before a down flip
         const uint32_t Lpj = Lp[j];
+        // rho = -1 iff bit 1 of L'_j = Lp_j + 2 c_j is set, negated on an odd down-flip: its sign
+        // bit is c_j xor a warp-uniform bit, placed at bit 31 of +1.0f
+        const uint32_t u31 = ((((Lpj >> 1) ^ (down & Lpj)) & 1u) << 31) | 0x3F800000u;
+#define PQ_RHO_J __uint_as_float(((Pc[k] >> j) << 31) ^ u31)
+#define PQ_DM_J (down ? 0u - (Lpj + (((Pc[k] >> j) & 1u) << 1)) : Lpj + (((Pc[k] >> j) & 1u) << 1))
         if (Lpj & 1u) {
-            PQ_Q(1, Tg[j], down ? -rho_of(Lpj + (((Pc[k] >> j) & 1u) << 1)) : rho_of(Lpj + (((Pc[k] >> j) & 1u) << 1)),
-                 down ? 0u - (Lpj + (((Pc[k] >> j) & 1u) << 1)) : Lpj + (((Pc[k] >> j) & 1u) << 1));
+            PQ_Q(1, Tg[j], PQ_RHO_J, PQ_DM_J);
         } else {
-            PQ_Q(0, Tg[j], rho_of(Lpj + (((Pc[k] >> j) & 1u) << 1)),
-                 down ? 0u - (Lpj + (((Pc[k] >> j) & 1u) << 1)) : Lpj + (((Pc[k] >> j) & 1u) << 1));
+            PQ_Q(0, Tg[j], PQ_RHO_J, PQ_DM_J);
         }
+#undef PQ_RHO_J
+#undef PQ_DM_J
     }
 #undef PQ_L0
 #undef PQ_L1
