@@ -176,41 +176,64 @@ __device__ __forceinline__ uint32_t quad_parity(const uint64_t *G, uint64_t x) {
 //   T_j    (1 << j) | (R_j << DI): the change of sidx when coordinate j flips
 // On return acc[k] = (hi.re, hi.im, lo.re, lo.im) of chunk k's A at the last branch, whose
 // folded index is m[k] + L'_{dl-1} (the walk ends on the unit vector of coordinate dl-1).
-template <int ODD>
-__device__ __forceinline__ void qturn_add(float &hr, float &hi, float &lr, float &li, float rho, const float4 &w) {
-    if (ODD) {
-        const float t = hr, u = lr;
-        hr = fmaf(rho, hi, w.x);
-        hi = fmaf(-rho, t, w.y);
-        lr = fmaf(rho, li, w.z);
-        li = fmaf(-rho, u, w.w);
-    } else {
-        hr = fmaf(rho, hr, w.x);
-        hi = fmaf(rho, hi, w.y);
-        lr = fmaf(rho, lr, w.z);
-        li = fmaf(rho, li, w.w);
-    }
+// Accumulators and table entries travel as pairs of FP32 in one 64-bit register, (re, im): an
+// even quarter-turn-and-add is then one fma.rn.f32x2 per pair (same rounding as two fmaf); an
+// odd one swaps re and im and is done on the halves.
+__device__ __forceinline__ uint64_t pk2(float a, float b) {
+    uint64_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void up2(uint64_t p, float &a, float &b) { asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(p)); }
+__device__ __forceinline__ float lo2(uint64_t p) {
+    float a, b;
+    up2(p, a, b);
+    return a;
+}
+__device__ __forceinline__ uint64_t ffma2(uint64_t a, uint64_t b, uint64_t c) {
+    uint64_t d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
+// even: A <- rho A + w (rho2 = (rho, rho)); odd: (re, im) <- rho (im, -re) + w
+__device__ __forceinline__ void qturn_even(uint64_t &H, uint64_t &L, uint64_t rho2, const ulonglong2 &w) {
+    H = ffma2(rho2, H, w.x);
+    L = ffma2(rho2, L, w.y);
+}
+__device__ __forceinline__ void qturn_odd(uint64_t &H, uint64_t &L, float rho, const ulonglong2 &w) {
+    float hr, hi, lr, li, wx, wy, wz, ww;
+    up2(H, hr, hi);
+    up2(L, lr, li);
+    up2(w.x, wx, wy);
+    up2(w.y, wz, ww);
+    H = pk2(fmaf(rho, hi, wx), fmaf(-rho, hr, wy));
+    L = pk2(fmaf(rho, li, wz), fmaf(-rho, lr, ww));
 }
 
 __device__ __forceinline__ float rho_of(uint32_t L) { return (L & 2u) ? -1.0f : 1.0f; }
 
 template <int MODE, int K, int PAR>
-__device__ __forceinline__ void gray_chunk_rot(const float4 *__restrict__ W, uint32_t sidx, const uint32_t (&Pc)[K],
+__device__ __forceinline__ void gray_chunk_rot(const float4 *__restrict__ W4, uint32_t sidx, const uint32_t (&Pc)[K],
                                                const uint32_t *Tg, const uint8_t *Lp, int dl, float (&acc)[K][4],
                                                uint8_t *dbg, const uint64_t (&sbase)[K], uint32_t k0,
                                                uint32_t (&m)[K], const uint64_t *G, uint32_t lomask) {
     constexpr int O0 = PAR & 1, O1 = (PAR >> 1) & 1, O2 = (PAR >> 2) & 1;
+    const ulonglong2 *__restrict__ W = reinterpret_cast<const ulonglong2 *>(W4);
     const uint32_t T0 = Tg[0], T1 = Tg[1], T2 = Tg[2];
     const uint32_t Lp0 = Lp[0], Lp1 = Lp[1], Lp2 = Lp[2];
-    float p0[K], p1[K], p2[K];
-    float hr[K], hi[K], lr[K], li[K];
-    const float4 w0 = __ldg(&W[sidx]);
+    uint64_t p0[K], p1[K], p2[K];  // (rho, rho) of coordinates 0..2 per chunk
+    uint64_t H[K], L[K];
+    const ulonglong2 w0 = __ldg(&W[sidx]);
 #pragma unroll
     for (int k = 0; k < K; k++) {
-        p0[k] = rho_of(Lp0 + ((Pc[k] & 1u) << 1));
-        p1[k] = rho_of(Lp1 + (Pc[k] & 2u));
-        p2[k] = rho_of(Lp2 + ((Pc[k] >> 1) & 2u));
-        hr[k] = w0.x; hi[k] = w0.y; lr[k] = w0.z; li[k] = w0.w;
+        const float r0 = rho_of(Lp0 + ((Pc[k] & 1u) << 1)), r1 = rho_of(Lp1 + (Pc[k] & 2u)),
+                    r2 = rho_of(Lp2 + ((Pc[k] >> 1) & 2u));
+        p0[k] = pk2(r0, r0);
+        p1[k] = pk2(r1, r1);
+        p2[k] = pk2(r2, r2);
+        H[k] = w0.x;
+        L[k] = w0.y;
     }
     const uint32_t inner = (1u << dl) - 1u;
     const uint32_t ngroups = 1u << (dl - 3);
@@ -218,16 +241,18 @@ __device__ __forceinline__ void gray_chunk_rot(const float4 *__restrict__ W, uin
 #define PQ_REC(k)                                                                                        \
     if (MODE == 2)                                                                                       \
         dbg[sbase[k] | (sidx & inner)] = (uint8_t)((k0 + 2u * (m[k] + 2u * quad_parity(G, sidx & lomask))) & 7u);
-    // flip by T, then A <- quarter-turn(A) + w for every chunk of the unit
-#define PQ_Q(ODD, T, RHO, DM)                                                     \
-    {                                                                             \
-        sidx ^= (T);                                                              \
-        const float4 w = __ldg(&W[sidx]);                                         \
-        _Pragma("unroll") for (int k = 0; k < K; k++) {                           \
-            qturn_add<ODD>(hr[k], hi[k], lr[k], li[k], (RHO), w);                 \
-            if (MODE == 2) m[k] += (DM);                                          \
-            PQ_REC(k)                                                             \
-        }                                                                         \
+    // flip by T, then A <- quarter-turn(A) + w for every chunk of the unit.  RHO2: the (rho, rho)
+    // pair of an even step; RHO: the signed rho of an odd step.
+#define PQ_Q(ODD, T, RHO2, RHO, DM)                                                \
+    {                                                                              \
+        sidx ^= (T);                                                               \
+        const ulonglong2 w = __ldg(&W[sidx]);                                      \
+        _Pragma("unroll") for (int k = 0; k < K; k++) {                            \
+            if (ODD) qturn_odd(H[k], L[k], (RHO), w);                              \
+            else qturn_even(H[k], L[k], (RHO2), w);                                \
+            if (MODE == 2) m[k] += (DM);                                           \
+            PQ_REC(k)                                                              \
+        }                                                                          \
     }
     if (MODE == 2) {
 #pragma unroll
@@ -237,16 +262,16 @@ __device__ __forceinline__ void gray_chunk_rot(const float4 *__restrict__ W, uin
 #define PQ_L1 (Lp1 + (Pc[k] & 2u))
 #define PQ_L2 (Lp2 + ((Pc[k] >> 1) & 2u))
     for (uint32_t g = 0;; ++g) {
-        PQ_Q(O0, T0, p0[k], PQ_L0);
-        PQ_Q(O1, T1, p1[k], PQ_L1);
-        PQ_Q(O0, T0, O0 ? -p0[k] : p0[k], 0u - PQ_L0);
+        PQ_Q(O0, T0, p0[k], lo2(p0[k]), PQ_L0);
+        PQ_Q(O1, T1, p1[k], lo2(p1[k]), PQ_L1);
+        PQ_Q(O0, T0, p0[k], -lo2(p0[k]), 0u - PQ_L0);
         {
             const bool up = (sidx ^ T2) & 4u;
-            PQ_Q(O2, T2, (O2 && !up) ? -p2[k] : p2[k], up ? PQ_L2 : 0u - PQ_L2);
+            PQ_Q(O2, T2, p2[k], up ? lo2(p2[k]) : -lo2(p2[k]), up ? PQ_L2 : 0u - PQ_L2);
         }
-        PQ_Q(O0, T0, p0[k], PQ_L0);
-        PQ_Q(O1, T1, O1 ? -p1[k] : p1[k], 0u - PQ_L1);
-        PQ_Q(O0, T0, O0 ? -p0[k] : p0[k], 0u - PQ_L0);
+        PQ_Q(O0, T0, p0[k], lo2(p0[k]), PQ_L0);
+        PQ_Q(O1, T1, p1[k], -lo2(p1[k]), 0u - PQ_L1);
+        PQ_Q(O0, T0, p0[k], -lo2(p0[k]), 0u - PQ_L0);
         if (g + 1 == ngroups) break;
         const int j = 3 + ctz32(g + 1);
         const uint32_t down = (sidx >> j) & 1u;  // bit j is set before a down flip
@@ -257,9 +282,9 @@ __device__ __forceinline__ void gray_chunk_rot(const float4 *__restrict__ W, uin
 #define PQ_RHO_J __uint_as_float(((Pc[k] >> j) << 31) ^ u31)
 #define PQ_DM_J (down ? 0u - (Lpj + (((Pc[k] >> j) & 1u) << 1)) : Lpj + (((Pc[k] >> j) & 1u) << 1))
         if (Lpj & 1u) {
-            PQ_Q(1, Tg[j], PQ_RHO_J, PQ_DM_J);
+            PQ_Q(1, Tg[j], 0ull, PQ_RHO_J, PQ_DM_J);
         } else {
-            PQ_Q(0, Tg[j], PQ_RHO_J, PQ_DM_J);
+            PQ_Q(0, Tg[j], pk2(PQ_RHO_J, PQ_RHO_J), 0.f, PQ_DM_J);
         }
 #undef PQ_RHO_J
 #undef PQ_DM_J
@@ -271,7 +296,8 @@ __device__ __forceinline__ void gray_chunk_rot(const float4 *__restrict__ W, uin
 #undef PQ_REC
 #pragma unroll
     for (int k = 0; k < K; k++) {
-        acc[k][0] = hr[k]; acc[k][1] = hi[k]; acc[k][2] = lr[k]; acc[k][3] = li[k];
+        up2(H[k], acc[k][0], acc[k][1]);
+        up2(L[k], acc[k][2], acc[k][3]);
     }
 }
 
