@@ -200,9 +200,10 @@ PQ_API pq_status pq_server_drain(pq_server *s, double timeout_s);
  * receives the tuning, best_ms (optional) its device time. */
 PQ_API pq_status pq_sim_autotune(pq_sim *sim, int64_t n, const uint64_t *x, const uint64_t *y, int32_t reps,
                                  pq_tuning *best, double *best_ms);
-/* The same search for a batch (pq_batch_run inputs x, y), over chunks_per_lane, block_warps and
- * (blocks_per_sm, unit_chunks); the lane chunk length stays that of the simulators' tables.
- * The batch's later launches use the fastest shape. */
+/* The same search for a batch (pq_batch_run inputs x, y).  A candidate lane chunk length
+ * rebuilds the member simulators' weight tables (their own cached launch plans are rebuilt on
+ * next use), so do not run the members concurrently with this call.  The batch's later
+ * launches use the fastest shape. */
 PQ_API pq_status pq_batch_autotune(pq_batch *b, const uint64_t *x, const uint64_t *y, int32_t reps, pq_tuning *best,
                                    double *best_ms);
 /* The launch shape the simulator's plans use. */

@@ -23,6 +23,7 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <set>
 #include <string>
 #include <thread>
 #include <vector>
@@ -518,6 +519,7 @@ struct pq_sim {
 
 struct pq_batch {
     std::vector<pq_sim *> sims;
+    int nw = 1;
     std::vector<Segment> segs;
     pq_tuning tu{};
     std::unique_ptr<Plan> plan;
@@ -1065,6 +1067,7 @@ PQ_API pq_status pq_batch_create(int32_t nsims, pq_sim *const *sims, const int64
     }
     CU(cudaSetDevice(g_device));
     B->segs = segs;
+    B->nw = nw;
     B->tu = tu;
     B->plan = std::make_unique<Plan>();
     pq_status st = build_plan(segs, nw, nullptr, tu, *B->plan);
@@ -1077,17 +1080,19 @@ PQ_API void pq_batch_destroy(pq_batch *b) {
     if (b->plan && b->plan->stream) cudaStreamSynchronize(b->plan->stream);
     delete b;
 }
-PQ_API int32_t pq_batch_words(const pq_batch *b) { return b ? b->plan->nw : 0; }
-PQ_API int64_t pq_batch_branches(const pq_batch *b) { return b ? (int64_t)b->plan->branches : 0; }
+PQ_API int32_t pq_batch_words(const pq_batch *b) { return b ? b->nw : 0; }
+PQ_API int64_t pq_batch_branches(const pq_batch *b) { return b && b->plan ? (int64_t)b->plan->branches : 0; }
 PQ_API pq_status pq_batch_run(pq_batch *b, const uint64_t *x, const uint64_t *y, double *out, double *err) {
     if (!b || !x || !y || !out) return fail(PQ_ERR_INVALID_ARG, "null argument");
     std::lock_guard<std::mutex> lk(b->mu);
+    if (!b->plan) return fail(PQ_ERR_INTERNAL, "batch has no launch plan (a failed autotune left none)");
     return run_host(*b->plan, x, y, out, err, false);
 }
 PQ_API pq_status pq_batch_run_device(pq_batch *b, const uint64_t *x, const uint64_t *y, double *out, double *err,
                                      void *stream) {
     if (!b || !x || !y || !out) return fail(PQ_ERR_INVALID_ARG, "null argument");
     std::lock_guard<std::mutex> lk(b->mu);
+    if (!b->plan) return fail(PQ_ERR_INTERNAL, "batch has no launch plan (a failed autotune left none)");
     return run_device(*b->plan, x, y, out, err, (cudaStream_t)stream);
 }
 
@@ -1102,7 +1107,7 @@ PQ_API pq_status pq_sim_kernel_ms(pq_sim *s, int64_t n, float *ms) {
 PQ_API pq_status pq_batch_kernel_ms(pq_batch *b, float *ms) {
     if (!b || !ms) return fail(PQ_ERR_INVALID_ARG, "null argument");
     std::lock_guard<std::mutex> lk(b->mu);
-    if (!b->plan->graph_ready) return fail(PQ_ERR_INVALID_ARG, "batch has not run yet");
+    if (!b->plan || !b->plan->graph_ready) return fail(PQ_ERR_INVALID_ARG, "batch has not run yet");
     CU(cudaEventSynchronize(b->plan->tev[3]));
     return last_kernel_ms(*b->plan, ms);
 }
@@ -1142,7 +1147,7 @@ PQ_API pq_status pq_sim_enumerated(pq_sim *s, int64_t n, double *out, double *pe
 PQ_API pq_status pq_batch_enumerated(pq_batch *b, double *out) {
     if (!b || !out) return fail(PQ_ERR_INVALID_ARG, "null argument");
     std::lock_guard<std::mutex> lk(b->mu);
-    if (!b->plan->graph_ready) return fail(PQ_ERR_INVALID_ARG, "batch has not run yet");
+    if (!b->plan || !b->plan->graph_ready) return fail(PQ_ERR_INVALID_ARG, "batch has not run yet");
     return plan_enumerated(*b->plan, out, nullptr);
 }
 PQ_API int64_t pq_sim_launch_items(pq_sim *s, int64_t n) {
@@ -1288,9 +1293,33 @@ PQ_API pq_status pq_batch_autotune(pq_batch *b, const uint64_t *x, const uint64_
     std::lock_guard<std::mutex> lk(b->mu);
     CU(cudaSetDevice(g_device));
     std::vector<double> scratch((size_t)2 * b->plan->nout);
+    // the lane chunk length is a property of each member simulator's weight tables: a candidate
+    // with another length rebuilds them (and drops the simulators' own cached plans)
+    int cur_di = b->sims[0]->di_max;
+    auto retable_all = [&](int di) -> pq_status {
+        std::set<pq_sim *> seen;
+        for (pq_sim *sp : b->sims) {
+            if (!seen.insert(sp).second) continue;
+            std::lock_guard<std::mutex> l2(sp->mu);
+            if (sp->di_max != di) {
+                pq_status e = retable_sim(sp, di);
+                if (e != PQ_OK) return e;
+            }
+        }
+        cur_di = di;
+        return PQ_OK;
+    };
+    if (b->plan) {
+        CU(cudaStreamSynchronize(b->plan->stream));
+        b->plan.reset();  // its engine records point into tables that may be rebuilt
+    }
     auto time_of = [&](const pq_tuning &t, double *ms_out) -> pq_status {
+        if (t.inner_dims != cur_di) {
+            pq_status e = retable_all(t.inner_dims);
+            if (e != PQ_OK) return e;
+        }
         Plan P;
-        pq_status e = build_plan(b->segs, b->plan->nw, nullptr, t, P);
+        pq_status e = build_plan(b->segs, b->nw, nullptr, t, P);
         if (e != PQ_OK) return e;
         double bt = 1e300;
         for (int r = 0; r <= reps; r++) {
@@ -1304,17 +1333,20 @@ PQ_API pq_status pq_batch_autotune(pq_batch *b, const uint64_t *x, const uint64_
         *ms_out = bt;
         return PQ_OK;
     };
-    // the simulators' weight tables are shared with other users: the lane chunk length stays
-    pq_tuning best;
+    pq_tuning start = b->tu, best = b->tu;
+    start.inner_dims = cur_di;
     double best_t = 0.0;
-    pq_status st = tune_search(b->tu, false, time_of, best, best_t);
-    if (st != PQ_OK) return st;
+    pq_status st = tune_search(start, true, time_of, best, best_t);
+    // whatever happened, leave the batch on its best known shape
+    pq_status st2 = best.inner_dims != cur_di ? retable_all(best.inner_dims) : PQ_OK;
     auto P = std::make_unique<Plan>();
-    st = build_plan(b->segs, b->plan->nw, nullptr, best, *P);
+    pq_status st3 = st2 == PQ_OK ? build_plan(b->segs, b->nw, nullptr, best, *P) : st2;
+    if (st3 == PQ_OK) {
+        b->plan = std::move(P);
+        b->tu = best;
+    }
     if (st != PQ_OK) return st;
-    CU(cudaStreamSynchronize(b->plan->stream));
-    b->plan = std::move(P);
-    b->tu = best;
+    if (st3 != PQ_OK) return st3;
     if (best_out) *best_out = best;
     if (best_ms) *best_ms = best_t;
     return PQ_OK;
