@@ -293,3 +293,19 @@ def test_batch_autotune_keeps_results(gpu):
     for i, s in enumerate(sims[:3]):
         r = O.OracleSim(circs[i][0])
         assert_amps(after[5 * i:5 * i + 5], r.amplitudes([0] * 5, outs[i]))
+
+
+def test_batched_workload_full_fp32_vs_device_fp64(gpu):
+    # the uneven batch at full size (256 circuits, 64 boundaries each) through one launch, each
+    # amplitude against the device FP64 mode: within its bound, <= 1e-6 relative
+    circs = workload_batch(256, seed=3)
+    sims = [Simulator(c) for c, _ in circs]
+    outs = [random_outputs(c.num_qubits, 64, 1000 + i) for i, (c, _) in enumerate(circs)]
+    b = Batch(sims, [64] * len(sims))
+    xs, ys = b.pack([[0] * 64] * len(sims), outs)
+    got, err = b.run(xs, ys, with_error=True)
+    ref = np.concatenate([s.amplitudes_fp64([0] * 64, o) for s, o in zip(sims, outs)])
+    diff = np.abs(got - ref)
+    assert np.all(diff <= err + 1e-300)
+    for i in range(len(sims)):
+        assert_amps(got[64 * i:64 * i + 64], ref[64 * i:64 * i + 64], err[64 * i:64 * i + 64])
