@@ -84,7 +84,13 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
+
+    def wait_first(self, timeout=3.0):
+        """Block until the sampler has produced its first line (so the timed region is covered)."""
+        t0 = time.perf_counter()
+        while self.proc and not self.lines and time.perf_counter() - t0 < timeout:
+            time.sleep(0.01)
 
     def __exit__(self, *a):
         if self.proc:
@@ -94,10 +100,15 @@ class ClockSampler:
             except subprocess.TimeoutExpired:
                 self.proc.kill()
 
-    def summary(self):
+    def summary(self, t0=None, t1=None):
+        """Median SM clock and active throttle reasons of the samples taken in [t0, t1] (all
+        samples when no window is given or none fell inside it)."""
         sm, mx, reasons = [], [], set()
         names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
-        for ln in self.lines:
+        lines = [ln for t, ln in self.lines if t0 is None or (t0 <= t <= t1 + 0.25)]
+        if not lines:
+            lines = [ln for _, ln in self.lines]
+        for ln in lines:
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -267,6 +278,7 @@ def run_gb300(args):
         torch.cuda.synchronize()
         step_ms, enum_ms = [], []
         with ClockSampler(local) as clk:
+            clk.wait_first()
             t_wall0 = time.perf_counter()
             for _ in range(args.steps):
                 flush.zero_()
@@ -280,8 +292,9 @@ def run_gb300(args):
                 N.check(L.pq_sim_kernel_ms(sim.handle, n, kms))
                 enum_ms.append(kms[1])
             torch.cuda.synchronize()
-            t_wall = time.perf_counter() - t_wall0
-        clocks = clk.summary()
+            t_wall1 = time.perf_counter()
+            t_wall = t_wall1 - t_wall0
+        clocks = clk.summary(t_wall0, t_wall1)
         ms = sum(step_ms) / len(step_ms)
         ms = max_over_ranks(dist, ms)
         value = replica_rate(ws, branches_step, ms)
@@ -707,10 +720,10 @@ def run_rotations(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--cpu-sample", type=int, default=48)
+    ap.add_argument("--cpu-sample", type=int, default=320)
     ap.add_argument("--ref-sample", type=int, default=24)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default launch shape")
