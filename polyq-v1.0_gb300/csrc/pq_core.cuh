@@ -131,15 +131,6 @@ PQ_HD int src_bit(int32_t src, const uint64_t *x, const uint64_t *y) {
 }
 PQ_HD int bit_at(const uint64_t *v, int i) { return (int)((v[i >> 6] >> (i & 63)) & 1ull); }
 
-// Error-free transformation: a + b = s + e exactly (Knuth's TwoSum).
-PQ_HD void two_sum_acc(float &acc, float &comp, float b) {
-    float s = acc + b;
-    float bb = s - acc;
-    float e = (acc - (s - bb)) + (b - bb);
-    acc = s;
-    comp += e;
-}
-
 // Multiply the hi and lo parts of a weight by i^q (q in 0..3) exactly.
 PQ_HD float4 rot4q(float4 w, uint32_t q) {
     const bool sw = q & 1;
@@ -155,14 +146,6 @@ PQ_HD float4 rot4q(float4 w, uint32_t q) {
 }
 
 // Multiply by i^q (q in 0..3) exactly.
-PQ_HD float2 rot4f(float2 w, uint32_t q) {
-    float a = (q & 1) ? w.y : w.x;
-    float b = (q & 1) ? w.x : w.y;
-    float2 r;
-    r.x = (q == 1 || q == 2) ? -a : a;
-    r.y = (q >= 2) ? -b : b;
-    return r;
-}
 PQ_HD double2 rot4d(double2 w, uint32_t q) {
     double a = (q & 1) ? w.y : w.x;
     double b = (q & 1) ? w.x : w.y;
