@@ -70,9 +70,13 @@ class Circuit:
     def cx(self, c, t): return self.push(CX, c, t)
     def swap(self, a, b): return self.push(SWAP, a, b)
 
-    def p(self, q, phase: int):
-        """diag(1, e^{i theta}) with an exact ring phase (src/circuit.rs:130-132)."""
-        return self.push(P, q, 0, phase)
+    def p(self, q, phase):
+        """diag(1, e^{i theta}).  An int is an exact ring phase (2 pi phase / 2^32, the Rust
+        Circuit::p, src/circuit.rs:130-132); a float is an angle in radians, as the reference's
+        Python binding takes it (src/pybind.rs:80-82)."""
+        if isinstance(phase, float):
+            return self.push(P, q, 0, phase_from_radians(phase))
+        return self.push(P, q, 0, int(phase) & MASK32)
 
     def p_radians(self, q, radians: float):
         return self.push(P, q, 0, phase_from_radians(radians))
@@ -110,9 +114,22 @@ class Circuit:
                 out.ops.append((code, a, b, ph))
         return out
 
-    def extend(self, other: "Circuit") -> "Circuit":
-        self.num_qubits = max(self.num_qubits, other.num_qubits)
-        self.ops.extend(other.ops)
+    _NAMED = {"H": (H, 1), "X": (X, 1), "Y": (Y, 1), "Z": (Z, 1), "S": (S, 1), "SDG": (SDG, 1), "T": (T, 1),
+              "TDG": (TDG, 1), "CX": (CX, 2), "CZ": (CZ, 2), "SWAP": (SWAP, 2)}
+
+    def extend(self, other) -> "Circuit":
+        """Append another Circuit's gates, or a flat list of (name, qubits) ops as the reference's
+        Python binding takes them (src/pybind.rs:101-121; a bad op raises ValueError)."""
+        if isinstance(other, Circuit):
+            self.num_qubits = max(self.num_qubits, other.num_qubits)
+            self.ops.extend(other.ops)
+            return self
+        for name, qs in other:
+            qs = list(qs)
+            code = self._NAMED.get(name)
+            if code is None or len(qs) != code[1]:
+                raise ValueError("bad op %s %s" % (name, qs))
+            self.push(code[0], *qs)
         return self
 
     def copy(self) -> "Circuit":
