@@ -309,3 +309,16 @@ def test_batched_workload_full_fp32_vs_device_fp64(gpu):
     assert np.all(diff <= err + 1e-300)
     for i in range(len(sims)):
         assert_amps(got[64 * i:64 * i + 64], ref[64 * i:64 * i + 64], err[64 * i:64 * i + 64])
+
+
+def test_probabilities_within_1e12_absolute(gpu):
+    # probabilities are certified to 1e-12 absolute (FP64 re-evaluation when the FP32 bound
+    # cannot show it): many-boundaries workload against the device FP64 mode and the oracle
+    c = workload_many_boundaries(0)
+    s = Simulator(c)
+    ys = random_outputs(50, 512, 31)
+    p = s.probabilities([0] * 512, ys)
+    ref = np.abs(s.amplitudes_fp64([0] * 512, ys)) ** 2
+    assert np.max(np.abs(p - ref)) <= 1e-12
+    want = np.abs(O.OracleSim(c).amplitudes([0] * 16, ys[:16])) ** 2
+    assert np.max(np.abs(p[:16] - want)) <= 1e-12
