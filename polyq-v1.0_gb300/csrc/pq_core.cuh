@@ -64,6 +64,8 @@ struct EngineDev {
     const uint64_t *cons;    // ncons x we consistency rows
     const int32_t *pivcol;   // rank
     const uint64_t *G;       // d   quadratic form of the Z8 phase over kernel coordinates
+    const uint64_t *Gw;      // d x dw  the same for any d (Monte-Carlo sampling above 64)
+    int dw;
     const uint64_t *R;       // d   pivot masks
     const float2 *tlo;       // 2^DI
     const float2 *tp;        // nsl_tp x 256

@@ -217,8 +217,10 @@ static int sm_count() {
 // what else shares the launch): chunks of 2^dl Gray steps, 32 * cpl chunks per item.
 // `light`: a one-shot plan (serving waves): device buffers come from the stream-ordered pool
 // and are released in stream order; no pinned host staging.
+// `prepare_only`: job records for the prepare kernel alone (Monte-Carlo sampling of engines
+// beyond the enumeration's limits): no dimension cap, no work items.
 static pq_status build_plan(const std::vector<Segment> &segs, int nw, cudaStream_t stream, const pq_tuning &tu,
-                            Plan &P, bool light = false) {
+                            Plan &P, bool light = false, bool prepare_only = false) {
     P.nw = nw;
     P.stream = stream;
     if (!P.stream) {
@@ -242,8 +244,9 @@ static pq_status build_plan(const std::vector<Segment> &segs, int nw, cudaStream
         Target *T = segs[si].tg;
         const int ebase = (int)eng.size();
         for (auto &e : T->dev) {
-            if (e.d > kMaxD || e.rank > kMaxPivots) return fail(PQ_ERR_UNSUPPORTED, "branch engine outside kernel limits");
-            if (e.d > tu.max_branch_dim)
+            if (e.rank > kMaxPivots || (e.d > kMaxD && !prepare_only))
+                return fail(PQ_ERR_UNSUPPORTED, "branch engine outside kernel limits");
+            if (e.d > tu.max_branch_dim && !prepare_only)
                 return fail(PQ_ERR_ADMISSION_REFUSED, "branch dimension " + std::to_string(e.d) + " above the cap " +
                                                           std::to_string(tu.max_branch_dim));
             eng.push_back(e);
@@ -286,7 +289,13 @@ static pq_status build_plan(const std::vector<Segment> &segs, int nw, cudaStream
         int j = perm[k];
         kinv[j] = k;
         const EngineDev &E = eng[jobs[j].engine];
-        job_shape(E, tu.chunks_per_lane, unit_max_of(tu), jdl[j], jnch[j], jcpi[j]);
+        if (prepare_only) {
+            jdl[j] = 0;
+            jnch[j] = 0;
+            jcpi[j] = 1;
+        } else {
+            job_shape(E, tu.chunks_per_lane, unit_max_of(tu), jdl[j], jnch[j], jcpi[j]);
+        }
         istart[k + 1] = istart[k] + (long long)((jnch[j] + jcpi[j] - 1) / jcpi[j]);
         P.branches += std::ldexp(1.0, E.d);
     }
@@ -868,6 +877,30 @@ static std::complex<double> phase_value(uint32_t p) {  // src/phase.rs:60-66
     return {std::cos(th), std::sin(th)};
 }
 
+// Estimate and standard error from the per-block (sum, sum |x|^2) of the sampled points:
+// norm * 2^d * mean and |norm| * 2^d * sqrt(var / n) (src/engine.rs:650-658).
+static pq_status mc_finish(const EngineDev &E, const JobDev &J, const std::vector<double> &hp, int grid,
+                           int64_t samples, double *out, double *stderr_out) {
+    if (J.vanish) return PQ_OK;  // prepare found no surviving subspace: (0, 0), src/engine.rs:618
+    double sx = 0.0, sy = 0.0, sq = 0.0;
+    for (int b = 0; b < grid; b++) {
+        sx += hp[3 * b];
+        sy += hp[3 * b + 1];
+        sq += hp[3 * b + 2];
+    }
+    const double n = (double)samples;
+    const std::complex<double> mean(sx / n, sy / n);
+    const double var = std::max(sq / n - std::norm(mean), 0.0);
+    const double scale = std::ldexp(1.0, E.d);
+    // norm = phase * magnitude (src/engine.rs:620), and the Z8 root of the index at s = 0
+    const std::complex<double> norm = phase_value(J.phase) * phase_value((J.k0 & 7u) << 29) * pow2_half(E.mag2 - E.num_h);
+    const std::complex<double> val = norm * mean * scale;
+    out[0] = val.real();
+    out[1] = val.imag();
+    if (stderr_out) *stderr_out = std::abs(norm) * scale * std::sqrt(var / n);
+    return PQ_OK;
+}
+
 // Simulator::amplitude_estimate (src/sim.rs:184-193) -> RankEngine::estimate (src/rank.rs:149-171).
 PQ_API pq_status pq_amplitude_estimate(pq_sim *s, const uint64_t *x, const uint64_t *y, int64_t samples,
                                        uint64_t seed, double *out, double *stderr_out) {
@@ -932,7 +965,35 @@ PQ_API pq_status pq_amplitude_estimate(pq_sim *s, const uint64_t *x, const uint6
         if (st != PQ_OK) return st;
         return run_host(*P, x, y, out, nullptr, false);
     }
-    if (E.d > 64) return fail(PQ_ERR_UNSUPPORTED, "Monte-Carlo estimate supports branch dimensions up to 64");
+    if (E.d > kMaxD) {
+        // beyond the enumeration's limits: prepare alone, then the multi-word sampler
+        if (E.d > 64 * MC_WORDS) return fail(PQ_ERR_UNSUPPORTED, "Monte-Carlo estimate supports branch dimensions up to 512");
+        Plan Q;
+        std::vector<Segment> segs{{&s->main, 1}};
+        pq_status st = build_plan(segs, nw, s->stream, s->tu, Q, false, true);
+        if (st != PQ_OK) return st;
+        DevMem lpx;
+        CU(lpx.alloc((size_t)E.d));
+        Q.args.lpx = lpx.as<uint8_t>();
+        Q.args.lpx_stride = E.d;
+        const size_t bwb = (size_t)nw * 8;
+        CU(cudaMemcpyAsync(Q.x.p, x, bwb, cudaMemcpyHostToDevice, Q.stream));
+        CU(cudaMemcpyAsync(Q.y.p, y, bwb, cudaMemcpyHostToDevice, Q.stream));
+        prepare_kernel<<<Q.grid_prep, 128, (size_t)4 * Q.smem_words * 8, Q.stream>>>(Q.args);
+        CU(cudaGetLastError());
+        const int grid = (int)std::max<long long>(1, std::min<long long>((samples + 255) / 256, (long long)sm_count() * 8));
+        DevMem part;
+        CU(part.alloc((size_t)grid * 3 * sizeof(double)));
+        mc_big_kernel<<<grid, 256, 0, Q.stream>>>(Q.engines.as<EngineDev>(), Q.jobs.as<JobDev>(), lpx.as<uint8_t>(),
+                                                   seed, (long long)samples, part.as<double>());
+        CU(cudaGetLastError());
+        JobDev J;
+        std::vector<double> hp((size_t)grid * 3);
+        CU(cudaMemcpyAsync(&J, Q.jobs.p, sizeof(JobDev), cudaMemcpyDeviceToHost, Q.stream));
+        CU(cudaMemcpyAsync(hp.data(), part.p, hp.size() * sizeof(double), cudaMemcpyDeviceToHost, Q.stream));
+        CU(cudaStreamSynchronize(Q.stream));
+        return mc_finish(E, J, hp, grid, samples, out, stderr_out);
+    }
     Plan *P = nullptr;
     pq_status st = sim_plan(s, 1, &P);
     if (st != PQ_OK) return st;
@@ -952,24 +1013,7 @@ PQ_API pq_status pq_amplitude_estimate(pq_sim *s, const uint64_t *x, const uint6
     CU(cudaMemcpyAsync(&J, P->jobs.p, sizeof(JobDev), cudaMemcpyDeviceToHost, P->stream));
     CU(cudaMemcpyAsync(hp.data(), part.p, hp.size() * sizeof(double), cudaMemcpyDeviceToHost, P->stream));
     CU(cudaStreamSynchronize(P->stream));
-    if (J.vanish) return PQ_OK;  // prepare found no surviving subspace: (0, 0), src/engine.rs:618
-    double sx = 0.0, sy = 0.0, sq = 0.0;
-    for (int b = 0; b < grid; b++) {
-        sx += hp[3 * b];
-        sy += hp[3 * b + 1];
-        sq += hp[3 * b + 2];
-    }
-    const double n = (double)samples;
-    const std::complex<double> mean(sx / n, sy / n);
-    const double var = std::max(sq / n - std::norm(mean), 0.0);
-    const double scale = std::ldexp(1.0, E.d);
-    // norm = phase * magnitude (src/engine.rs:620), and the Z8 root of the index at s = 0
-    const std::complex<double> norm = phase_value(J.phase) * phase_value((J.k0 & 7u) << 29) * pow2_half(E.mag2 - E.num_h);
-    const std::complex<double> val = norm * mean * scale;
-    out[0] = val.real();
-    out[1] = val.imag();
-    if (stderr_out) *stderr_out = std::abs(norm) * scale * std::sqrt(var / n);
-    return PQ_OK;
+    return mc_finish(E, J, hp, grid, samples, out, stderr_out);
 }
 
 // ---------------------------------------------------------------- sampling

@@ -472,8 +472,9 @@ std::unique_ptr<HostEngine> build_engine(const PathSum& ps, const std::vector<in
     // quadratic part of the Z8 phase over kernel coordinates: 4*G_ij is the second finite
     // difference of phase8 along kernel columns i and j, which does not depend on the base point
     const int d = E->d;
-    E->G.assign((size_t)d, 0ull);
-    if (d <= 64) {
+    E->dw = (d + 63) / 64;
+    E->Gw.assign((size_t)d * (size_t)E->dw, 0ull);
+    {
         std::vector<uint64_t> z((size_t)abo, 0ull), uij((size_t)abo);
         const int p0 = E->phase8(z.data());
         std::vector<int> p1((size_t)d);
@@ -483,9 +484,15 @@ std::unique_ptr<HostEngine> build_engine(const PathSum& ps, const std::vector<in
                 for (int w = 0; w < abo; w++) uij[w] = E->ku[(size_t)i * abo + w] ^ E->ku[(size_t)j * abo + w];
                 int dd = ((E->phase8(uij.data()) - p1[i] - p1[j] + p0) % 8 + 16) % 8;
                 if (dd != 0 && dd != 4) throw std::logic_error("phase is not quadratic over the kernel");
-                if (dd == 4) { E->G[i] |= 1ull << j; E->G[j] |= 1ull << i; }
+                if (dd == 4) {
+                    E->Gw[(size_t)i * E->dw + (size_t)(j >> 6)] |= 1ull << (j & 63);
+                    E->Gw[(size_t)j * E->dw + (size_t)(i >> 6)] |= 1ull << (i & 63);
+                }
             }
     }
+    // one word per row, the enumeration's form: complete for d <= 64, coordinates 0..63 above
+    E->G.assign((size_t)d, 0ull);
+    for (int j = 0; j < d; j++) E->G[(size_t)j] = E->Gw[(size_t)j * E->dw];
     // error-bound factor: sum_s |c(s)| <= prod_j (|a0|+|a1|)(free cols) * prod_i max(|a0|,|a1|)(pivots)
     double bound = 1.0;
     for (int j = 0; j < d; j++) {
@@ -682,6 +689,8 @@ PackedEngine pack_engine(const HostEngine& e, const EngineTables& T) {
     std::vector<int32_t> pc(e.piv_col.begin(), e.piv_col.end());
     d.pivcol = as_off<int32_t>(k.vec(pc));
     d.G = as_off<uint64_t>(k.vec(e.G));
+    d.Gw = as_off<uint64_t>(k.vec(e.Gw));
+    d.dw = e.dw;
     d.R = as_off<uint64_t>(k.vec(e.R));
     std::vector<float> tlo32, tp32;
     for (const auto& c : T.tlo) { tlo32.push_back((float)c.re); tlo32.push_back((float)c.im); }
@@ -752,7 +761,7 @@ EngineDev rebase_engine(const EngineDev& o, const uint8_t* base) {
     d.wem = shift(o.wem, base); d.ucols = shift(o.ucols, base); d.mcols = shift(o.mcols, base);
     d.ku = shift(o.ku, base); d.bfixed = shift(o.bfixed, base); d.fixed_v = shift(o.fixed_v, base);
     d.fixed_th = shift(o.fixed_th, base); d.pivrow = shift(o.pivrow, base); d.cons = shift(o.cons, base);
-    d.pivcol = shift(o.pivcol, base); d.G = shift(o.G, base); d.R = shift(o.R, base);
+    d.pivcol = shift(o.pivcol, base); d.G = shift(o.G, base); d.Gw = shift(o.Gw, base); d.R = shift(o.R, base);
     d.tlo = shift(o.tlo, base); d.tp = shift(o.tp, base); d.th = shift(o.th, base);
     d.tlo64 = shift(o.tlo64, base); d.tp64 = shift(o.tp64, base); d.wtab = shift(o.wtab, base);
     return d;

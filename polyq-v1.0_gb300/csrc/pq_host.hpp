@@ -145,6 +145,8 @@ struct HostEngine {
     std::vector<Cplx> alpha, beta;  // per term, FP64 (src/engine.rs:232-238)
     // device plan
     std::vector<uint64_t> G;        // d rows, quadratic part of the Z8 phase over kernel coordinates
+    std::vector<uint64_t> Gw;       // the same, d rows of dw words (any d)
+    int dw = 1;
     std::vector<uint64_t> R;        // d pivot masks (bit i: kernel_j hits pivot column i)
     std::vector<int> free_col;      // d: term index of kernel vector j's free column
     double sum_abs_bound = 0.0;     // upper bound of sum_s |c(s)| (for the per-result error bound)

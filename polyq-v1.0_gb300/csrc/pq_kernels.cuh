@@ -53,6 +53,8 @@ struct KArgs {
     int smem_words;             // per-warp words of the prepare kernel
     uint8_t *dbg;               // per-branch Z8 indices (debug mode)
     int *errflag;
+    uint8_t *lpx;               // optional: Lp of every coordinate, lpx_stride bytes per job (any d)
+    int lpx_stride;
 };
 
 __device__ __forceinline__ int warp_sum_i(int v) {
@@ -120,7 +122,8 @@ __global__ void __launch_bounds__(128) prepare_kernel(KArgs a) {
             phase8_partial(E, u, E.ku + (size_t)j * E.abo, 0, 1, a1, c1);
             uint32_t L = (phase8_finish(E, a1, c1) - k0) & 7u;
             lerr |= (int)(L & 1u);
-            J->Lp[j] = (uint8_t)(L >> 1);
+            if (j < 64) J->Lp[j] = (uint8_t)(L >> 1);
+            if (a.lpx) a.lpx[(size_t)jid * a.lpx_stride + j] = (uint8_t)(L >> 1);
         }
         lerr = __any_sync(PQ_FULL, lerr);
         if (lane == 0) {
@@ -664,6 +667,76 @@ __global__ void __launch_bounds__(256) mc_kernel(const EngineDev *__restrict__ E
         sx += w.x;
         sy += w.y;
         sq += w.x * w.x + w.y * w.y;
+    }
+    red[0][threadIdx.x] = sx;
+    red[1][threadIdx.x] = sy;
+    red[2][threadIdx.x] = sq;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o)
+            for (int q = 0; q < 3; q++) red[q][threadIdx.x] += red[q][threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int q = 0; q < 3; q++) partials[3 * blockIdx.x + q] = red[q][0];
+}
+
+// Engine::estimate for branch dimensions above 64 (up to 64 * MC_WORDS): the same per-chunk
+// streams, each point drawn as ceil(d / 64) consecutive words of its chunk's stream (the
+// reference takes a fresh word every 64 coordinates).  Z4 index from the multi-word quadratic
+// form (m = sum of Lp_j + 2 q(s), q from popcounts of G rows), pivot bits from R, weight from the
+// FP64 byte-slice tables.
+constexpr int MC_WORDS = 8;
+
+__device__ __forceinline__ uint32_t bits8_at(const uint64_t *s, int b) {
+    const int w = b >> 6, o = b & 63;
+    uint64_t v = s[w] >> o;
+    if (o > 56 && w + 1 < MC_WORDS) v |= s[w + 1] << (64 - o);
+    return (uint32_t)(v & 255ull);
+}
+
+__global__ void __launch_bounds__(256) mc_big_kernel(const EngineDev *__restrict__ Ep, const JobDev *__restrict__ Jp,
+                                                     const uint8_t *__restrict__ lp, uint64_t seed, long long samples,
+                                                     double *partials) {
+    const uint64_t golden = 0x9E3779B97F4A7C15ull;
+    const EngineDev &E = *Ep;
+    const JobDev &J = *Jp;
+    __shared__ double red[3][256];
+    const int d = E.d, nwd = (d + 63) >> 6;
+    const uint64_t lomask = E.DI >= 64 ? ~0ull : ((1ull << E.DI) - 1ull);
+    double sx = 0.0, sy = 0.0, sq = 0.0;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < samples;
+         k += (long long)gridDim.x * blockDim.x) {
+        const uint64_t ci = (uint64_t)(k >> 10), kk = (uint64_t)(k & 1023);
+        const uint64_t st0 = (seed ^ (ci * golden)) + golden;
+        uint64_t s[MC_WORDS];
+#pragma unroll
+        for (int w = 0; w < MC_WORDS; w++) {
+            s[w] = 0ull;
+            if (w < nwd) {
+                uint64_t v = splitmix_at(st0 + (kk * (uint64_t)nwd + (uint64_t)w + 1ull) * golden);
+                if (w == nwd - 1 && (d & 63)) v &= (1ull << (d & 63)) - 1ull;
+                s[w] = v;
+            }
+        }
+        uint32_t m = 0, t = 0;
+        uint64_t yy = J.y0;
+        for (int w = 0; w < nwd; w++)
+            for (uint64_t r = s[w]; r; r &= r - 1) {
+                const int j = (w << 6) + ctz64(r);
+                m += lp[j];
+                const uint64_t *g = E.Gw + (size_t)j * E.dw;
+                for (int w2 = 0; w2 < nwd; w2++) t += (uint32_t)popc64(g[w2] & s[w2]);
+                yy ^= E.R[j];
+            }
+        m += ((t >> 1) & 1u) << 1;
+        double2 wt = E.tlo64[s[0] & lomask];
+        for (int sl = 0; sl < E.nsl_tp; sl++) wt = cmul_d(wt, E.tp64[sl * 256 + (int)((yy >> (8 * sl)) & 255ull)]);
+        for (int sl = 0; sl < E.nsl_th; sl++) wt = cmul_d(wt, E.th[sl * 256 + (int)bits8_at(s, E.DI + 8 * sl)]);
+        wt = rot4d(wt, m & 3u);
+        sx += wt.x;
+        sy += wt.y;
+        sq += wt.x * wt.x + wt.y * wt.y;
     }
     red[0][threadIdx.x] = sx;
     red[1][threadIdx.x] = sy;

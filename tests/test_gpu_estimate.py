@@ -56,3 +56,20 @@ def test_branch_sampling_matches_oracle(gpu):
     scale = max(abs(complex(want[0], want[1])), want[2], 1e-12)
     assert abs(complex(got[0], got[1]) - complex(want[0], want[1])) <= 1e-6 * scale
     assert got[2] == pytest.approx(want[2], rel=1e-6, abs=1e-12)
+
+
+@pytest.mark.parametrize("per_layer", [2, 3, 8])
+def test_sampled_large_subspace_matches_oracle(gpu, per_layer):
+    # rotations with CCZ layers, one cached engine of d = 77, 104 and 239 (the last is the
+    # rotation workload as written): points of more than one 64-bit word, the same draws
+    from polyq_gb300.rng import workload_rotations
+    c = workload_rotations(n=40, ngates=1500, n_rz=24, ccz_layers=4, ccz_per_layer=per_layer, seed=4)
+    sim = Simulator(c, "cached")
+    assert sim.stats_full()["branch_dim"] > 64
+    ref = O.OracleSim(c, "cached")
+    for y, seed in ((12345, 7), (0, 8)):
+        got = sim.amplitude_estimate(0, y, 3000, seed)
+        want = ref.amplitude_estimate(0, y, 3000, seed)
+        scale = max(abs(complex(want[0], want[1])), want[2], 1e-300)
+        assert abs(complex(got[0], got[1]) - complex(want[0], want[1])) <= 1e-9 * scale
+        assert got[2] == pytest.approx(want[2], rel=1e-9)
