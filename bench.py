@@ -16,7 +16,7 @@ roofline   enumeration kernel: its FP32 FMA-pipe work (4 ops per enumerated bran
            over its event-timed duration, against the fma.f32 rate measured on the device;
            reference_form beside it: the reference engine's integer work for the same branches
            (5 W_o + 6 W_g int64 ops each) against the measured lop3 / popc rates
-workloads  --workload many_boundaries (default) | batched | serve | small | rotations | sample
+workloads  --workload many_boundaries (default) | batched | serve | small | rotations | sample | estimate
 cpu_baseline  the CPU oracle (a restatement of the reference engine) on all host threads
 --impl reference  times the same CPU restatement on the same workload (bounded sample)
 """
@@ -666,6 +666,44 @@ def run_sample(args):
     return 0
 
 
+def run_estimate(args):
+    """Simulator::amplitude_estimate on the rotation workload as written (n=40, 1500 gates, 24 rz,
+    4 layers of 8 CCZ; one cached engine of d = 239, beyond exact enumeration): sampled points
+    per second on the device beside the CPU restatement, same seeds, same draws."""
+    pq, N = _gpu_setup()
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    from polyq_gb300.rng import workload_rotations
+    c = workload_rotations(n=40, ngates=1500, n_rz=24, ccz_layers=4, ccz_per_layer=8, seed=4)
+    sim = pq.Simulator(c, "cached")
+    samples = 1 << 22
+    sim.amplitude_estimate(0, 12345, 1 << 12, 1)
+    times, est = [], None
+    for k in range(max(1, min(args.steps, 10))):
+        t0 = time.perf_counter()
+        est = sim.amplitude_estimate(0, 12345, samples, 100 + k)
+        times.append(time.perf_counter() - t0)
+    ref = oracle.OracleSim(c, "cached")
+    cpu_samples = 1 << 15
+    t0 = time.perf_counter()
+    want = ref.amplitude_estimate(0, 12345, cpu_samples, 100)
+    cpu_s = time.perf_counter() - t0
+    got = sim.amplitude_estimate(0, 12345, cpu_samples, 100)
+    line = {"metric": METRIC, "workload": "estimate", "value": samples / (sum(times) / len(times)),
+            "unit": "samples/s", "n_gpus": 1, "higher_is_better": True, "data": "synthetic",
+            "ms_per_step": 1e3 * sum(times) / len(times), "samples_per_step": samples,
+            "estimate": {"re": est[0], "im": est[1], "stderr": est[2]},
+            "same_draws_as_cpu_restatement_rel_diff": abs(complex(got[0], got[1]) - complex(want[0], want[1])) /
+            max(abs(complex(want[0], want[1])), want[2], 1e-300),
+            "branch_dim": sim.stats_full()["branch_dim"],
+            "cpu_baseline": {"value": cpu_samples / cpu_s, "unit": "samples/s", "cores": 1, "kind": "port",
+                             "sample": "%d samples, one thread (the restatement's sampler is sequential)" % cpu_samples},
+            "config": {"workload": "amplitude_estimate, rotations as written: n=40, 1500 gates, 24 rz, 4x8 CCZ "
+                                   "(seed 4), strategy cached, <12345|C|0>"}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_rotations(args):
     """Arbitrary angles: rz(theta) slots plus CCZ layers, FP32-compensated vs device FP64 per
     amplitude; a 20-qubit variant also against the dense statevector."""
@@ -731,7 +769,7 @@ def main():
                     "blocks_per_sm[,unit_chunks] (implies --no-autotune)")
     ap.add_argument("--boundaries", type=int, default=4096, help="boundary count (profiling of smaller cases)")
     ap.add_argument("--workload", default="many_boundaries",
-                    choices=["many_boundaries", "batched", "serve", "small", "rotations", "sample"])
+                    choices=["many_boundaries", "batched", "serve", "small", "rotations", "sample", "estimate"])
     ap.add_argument("--rate", type=float, default=5000.0, help="serve: offered requests/s")
     ap.add_argument("--duration", type=float, default=2.0, help="serve: seconds of arrivals")
     ap.add_argument("--slots", type=int, default=256, help="serve: requests per wave")
@@ -750,6 +788,8 @@ def main():
         return run_small(args)
     if args.workload == "sample":
         return run_sample(args)
+    if args.workload == "estimate":
+        return run_estimate(args)
     if args.workload == "rotations":
         return run_rotations(args)
     return run_gb300(args)
