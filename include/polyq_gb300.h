@@ -78,6 +78,9 @@ typedef struct pq_tuning {
     int32_t max_branch_dim;  /* admission cap on d per branch engine (<= 62) */
     int32_t blocks_per_sm;   /* enumeration kernel register budget: 2, 3 or 4 blocks of 256 per SM */
     int32_t unit_chunks;     /* at most this many chunks (1, 2, 4, 8) share each weight-table load */
+    int32_t chunk_tables;    /* 1: sum each chunk by one lookup in its engine's chunk-sum table (a
+                                Walsh transform of the weight table over the walked coordinates,
+                                FP64) instead of enumerating its branches; 2 or 0: enumerate */
 } pq_tuning;
 
 /* ---- library ------------------------------------------------------------------------ */

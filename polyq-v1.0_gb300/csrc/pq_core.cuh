@@ -73,6 +73,7 @@ struct EngineDev {
     const double2 *tlo64;    // 2^DI   (FP64 path)
     const double2 *tp64;     // nsl_tp x 256
     const float4 *wtab;      // 2^(DI + rank): (hi.re, hi.im, lo.re, lo.im) of tlo[s] * TP(y)
+    const double2 *ctab;     // 2^(rank + DI) chunk sums (null: none), index (y << DI) | b
 };
 
 // Boundary -> fixed-variable values.  src = q | vec << 24 | flip << 25 (vec 0: x, 1: y).

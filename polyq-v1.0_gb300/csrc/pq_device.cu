@@ -37,7 +37,7 @@ namespace pq {
 thread_local std::string g_err;
 static std::mutex g_mu;
 static int g_device = 0;
-static pq_tuning g_tuning = {10, 4, 8, 48, 3, 4};
+static pq_tuning g_tuning = {10, 4, 8, 48, 3, 4, 0};
 
 // Chunks per unit a tuning allows: eight accumulating chunks per lane only fit the 128-register
 // (two blocks per SM) build of the enumeration kernel.
@@ -344,6 +344,7 @@ static pq_status build_plan(const std::vector<Segment> &segs, int nw, cudaStream
     a.nitems = P.nitems;
     a.partials = P.partials.as<double2>();
     a.counter = P.counter.as<unsigned long long>();
+    a.use_ctab = tu.chunk_tables == 1 ? 1 : 0;
     a.job_vals = P.job_vals.as<double2>();
     a.job_err = P.job_err.as<double>();
     a.out_jobs = P.out_jobs.as<int>();
@@ -579,6 +580,10 @@ PQ_API pq_status pq_set_default_tuning(const pq_tuning *t) {
     if (t->max_branch_dim) {
         if (t->max_branch_dim < 1 || t->max_branch_dim > kMaxD) return fail(PQ_ERR_INVALID_ARG, "max_branch_dim in 1..62");
         n.max_branch_dim = t->max_branch_dim;
+    }
+    if (t->chunk_tables) {
+        if (t->chunk_tables != 1 && t->chunk_tables != 2) return fail(PQ_ERR_INVALID_ARG, "chunk_tables is 1 (on) or 2 (off)");
+        n.chunk_tables = t->chunk_tables;
     }
     if (t->unit_chunks) {
         if (t->unit_chunks != 1 && t->unit_chunks != 2 && t->unit_chunks != 4 && t->unit_chunks != 8)

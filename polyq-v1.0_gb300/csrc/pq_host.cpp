@@ -479,6 +479,9 @@ std::unique_ptr<HostEngine> build_engine(const PathSum& ps, const std::vector<in
         const int p0 = E->phase8(z.data());
         std::vector<int> p1((size_t)d);
         for (int j = 0; j < d; j++) p1[j] = E->phase8(&E->ku[(size_t)j * abo]);
+        // Z8 first differences are 2 Lp_j; the parity of Lp_j does not depend on the base point
+        E->lp0.assign((size_t)d, 0);
+        for (int j = 0; j < d; j++) E->lp0[(size_t)j] = (uint8_t)(((((p1[j] - p0) % 8 + 8) % 8) >> 1) & 1);
         for (int i = 0; i < d; i++)
             for (int j = i + 1; j < d; j++) {
                 for (int w = 0; w < abo; w++) uij[w] = E->ku[(size_t)i * abo + w] ^ E->ku[(size_t)j * abo + w];
@@ -751,6 +754,44 @@ PackedEngine pack_engine(const HostEngine& e, const EngineTables& T) {
         w32.push_back((float)(c.im - hi));
     }
     d.wtab = as_off<float4>(k.vec(w32));
+    // Chunk-sum table: a chunk walks all DI low coordinates, along which the folded Z4 index is
+    // linear, i^{m} = i^{m_start} prod_j i^{Lp0_j s_j} (-1)^{b_j s_j}, b_j = (Lp_j >> 1) ^ c_j; so
+    // its sum is i^{m_start} T[y_start][b] with
+    //   T[u][b] = sum_s i^{<Lp0, s>} (-1)^{<b, s>} W'[u ^ R_lo s][s],
+    // a Walsh-Hadamard transform over s for each pivot pattern u (FP64, once per engine).
+    d.ctab = nullptr;
+    if (T.joint && T.DI >= 1 && T.DI + e.rank <= 16) {
+        const size_t nlo = (size_t)1 << T.DI, nu = (size_t)1 << e.rank;
+        std::vector<Cplx> ct(nu * nlo);
+        for (size_t u = 0; u < nu; u++) {
+            Cplx *g = &ct[u * nlo];
+            for (size_t s = 0; s < nlo; s++) {
+                uint64_t y = u;
+                int ph = 0;
+                for (int j = 0; j < T.DI; j++)
+                    if ((s >> j) & 1) {
+                        y ^= e.R[(size_t)j];
+                        ph += e.lp0[(size_t)j];
+                    }
+                Cplx w = T.w[(y << T.DI) | s];
+                if (qsign[s]) w = Cplx{-w.re, -w.im};
+                switch (ph & 3) {  // times i^ph
+                    case 0: g[s] = w; break;
+                    case 1: g[s] = Cplx{-w.im, w.re}; break;
+                    case 2: g[s] = Cplx{-w.re, -w.im}; break;
+                    default: g[s] = Cplx{w.im, -w.re}; break;
+                }
+            }
+            for (size_t h = 1; h < nlo; h <<= 1)  // in-place transform, T[b] = sum_s (-1)^{<b,s>} g[s]
+                for (size_t i = 0; i < nlo; i += 2 * h)
+                    for (size_t k2 = i; k2 < i + h; k2++) {
+                        const Cplx a = g[k2], b = g[k2 + h];
+                        g[k2] = Cplx{a.re + b.re, a.im + b.im};
+                        g[k2 + h] = Cplx{a.re - b.re, a.im - b.im};
+                    }
+        }
+        d.ctab = as_off<double2>(k.vec(ct));
+    }
     P.blob.swap(k.blob);
     return P;
 }
@@ -764,6 +805,7 @@ EngineDev rebase_engine(const EngineDev& o, const uint8_t* base) {
     d.pivcol = shift(o.pivcol, base); d.G = shift(o.G, base); d.Gw = shift(o.Gw, base); d.R = shift(o.R, base);
     d.tlo = shift(o.tlo, base); d.tp = shift(o.tp, base); d.th = shift(o.th, base);
     d.tlo64 = shift(o.tlo64, base); d.tp64 = shift(o.tp64, base); d.wtab = shift(o.wtab, base);
+    d.ctab = o.ctab ? shift(o.ctab, base) : nullptr;
     return d;
 }
 

@@ -146,6 +146,7 @@ struct HostEngine {
     // device plan
     std::vector<uint64_t> G;        // d rows, quadratic part of the Z8 phase over kernel coordinates
     std::vector<uint64_t> Gw;       // the same, d rows of dw words (any d)
+    std::vector<uint8_t> lp0;       // d: parity of each coordinate's Z4 increment (any boundary)
     int dw = 1;
     std::vector<uint64_t> R;        // d pivot masks (bit i: kernel_j hits pivot column i)
     std::vector<int> free_col;      // d: term index of kernel vector j's free column

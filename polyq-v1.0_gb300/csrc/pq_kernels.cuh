@@ -55,6 +55,7 @@ struct KArgs {
     int *errflag;
     uint8_t *lpx;               // optional: Lp of every coordinate, lpx_stride bytes per job (any d)
     int lpx_stride;
+    int use_ctab;               // chunk sums from the engines' chunk-sum tables where they apply
 };
 
 __device__ __forceinline__ int warp_sum_i(int v) {
@@ -468,6 +469,25 @@ __global__ void __launch_bounds__(256, MINB) enum_kernel(KArgs a) {
                 unsigned long long ch = un;
                 for (int i = 0; i < np; i++) ch = insert_zero(ch, E.pairc[i] - dl);
                 const uint64_t s1 = (uint64_t)ch << dl;
+                if (MODE == 0 && a.use_ctab && E.ctab && dl == E.DI) {
+                    // chunk-sum tables: one FP64 lookup per chunk instead of its 2^DI-step walk
+                    for (int kc = 0; kc < nk; kc++) {
+                        uint64_t s = s1;
+                        for (int i = 0; i < np; i++)
+                            if ((kc >> i) & 1) s |= 1ull << E.pairc[i];
+                        uint32_t m;
+                        uint64_t yy;
+                        chunk_start(Lp, G, R, J.y0, s, m, yy);
+                        uint32_t b = 0;
+                        for (int j = 0; j < dl; j++)
+                            b |= (((uint32_t)(Lp[j] >> 1) ^ (uint32_t)popc64(G[j] & s)) & 1u) << j;
+                        const double2 v = rot4d(E.ctab[(yy << E.DI) | b], m & 3u);
+                        const double2 chi = chunk_high_weight(E, s);
+                        accx += v.x * chi.x - v.y * chi.y;
+                        accy += v.x * chi.y + v.y * chi.x;
+                    }
+                    continue;
+                }
                 if (MODE != 1 && E.joint && dl >= 3) {
                     if (np == 3) {
                         if (MINB == 2) {  // eight accumulators per lane: only with the 128-register budget

@@ -40,7 +40,8 @@ class Stats(ct.Structure):
 
 class Tuning(ct.Structure):
     _fields_ = [("inner_dims", ct.c_int32), ("chunks_per_lane", ct.c_int32), ("block_warps", ct.c_int32),
-                ("max_branch_dim", ct.c_int32), ("blocks_per_sm", ct.c_int32), ("unit_chunks", ct.c_int32)]
+                ("max_branch_dim", ct.c_int32), ("blocks_per_sm", ct.c_int32), ("unit_chunks", ct.c_int32),
+                ("chunk_tables", ct.c_int32)]
 
 
 class Request(ct.Structure):

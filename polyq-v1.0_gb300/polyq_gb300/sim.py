@@ -287,9 +287,10 @@ class Batch:
             pass
 
 
-def set_tuning(inner_dims=0, chunks_per_lane=0, block_warps=0, max_branch_dim=0, blocks_per_sm=0, unit_chunks=0):
+def set_tuning(inner_dims=0, chunks_per_lane=0, block_warps=0, max_branch_dim=0, blocks_per_sm=0, unit_chunks=0,
+               chunk_tables=0):
     """Defaults for simulators and batches created afterwards (0 keeps a field unchanged)."""
-    t = N.Tuning(inner_dims, chunks_per_lane, block_warps, max_branch_dim, blocks_per_sm, unit_chunks)
+    t = N.Tuning(inner_dims, chunks_per_lane, block_warps, max_branch_dim, blocks_per_sm, unit_chunks, chunk_tables)
     N.check(N.lib().pq_set_default_tuning(ct.byref(t)))
 
 

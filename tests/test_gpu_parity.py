@@ -322,3 +322,30 @@ def test_probabilities_within_1e12_absolute(gpu):
     assert np.max(np.abs(p - ref)) <= 1e-12
     want = np.abs(O.OracleSim(c).amplitudes([0] * 16, ys[:16])) ** 2
     assert np.max(np.abs(p[:16] - want)) <= 1e-12
+
+
+def test_chunk_tables_match_fp64(gpu):
+    # opt-in chunk-sum tables (one FP64 lookup per chunk): the FP64 enumeration's amplitudes to
+    # FP64 rounding (relative to the summed magnitudes), on the many-boundaries workload and an
+    # uneven batch
+    old = get_tuning()
+    try:
+        set_tuning(chunk_tables=1)
+        c = workload_many_boundaries(0)
+        s = Simulator(c)
+        ys = random_outputs(50, 512, 3)
+        got = s.amplitudes([0] * 512, ys)
+        ref = s.amplitudes_fp64([0] * 512, ys)
+        scale = float(np.max(np.abs(ref)))
+        assert np.max(np.abs(got - ref)) <= 1e-12 * scale
+        want = O.OracleSim(c).amplitudes([0] * 12, ys[:12])
+        assert_amps(got[:12], want)
+        circs = workload_batch(24, seed=3, t_max=20)
+        sims = [Simulator(cc) for cc, _ in circs]
+        for sm, (cc, _) in zip(sims, circs):
+            ys2 = random_outputs(cc.num_qubits, 6, 9)
+            a, err = sm.amplitudes([0] * 6, ys2, with_error=True)
+            r = sm.amplitudes_fp64([0] * 6, ys2)
+            assert_amps(a, r, err)  # within the reported bound; FP64 rounding of cancelling sums
+    finally:
+        set_tuning(chunk_tables=2)
