@@ -45,6 +45,11 @@ static int unit_max_of(const pq_tuning &tu) {
     const int u = tu.unit_chunks > 0 ? tu.unit_chunks : 4;
     return tu.blocks_per_sm == 2 ? u : std::min(u, 4);
 }
+// Per engine: chunks summed from the chunk-sum table are visited one by one in Gray order
+// (units of one chunk).
+static int unit_max_for(const EngineDev &E, const pq_tuning &tu) {
+    return (tu.chunk_tables == 1 && E.ctab) ? 1 : unit_max_of(tu);
+}
 
 static pq_status fail(pq_status s, const std::string &m) {
     g_err = m;
@@ -294,7 +299,7 @@ static pq_status build_plan(const std::vector<Segment> &segs, int nw, cudaStream
             jnch[j] = 0;
             jcpi[j] = 1;
         } else {
-            job_shape(E, tu.chunks_per_lane, unit_max_of(tu), jdl[j], jnch[j], jcpi[j]);
+            job_shape(E, tu.chunks_per_lane, unit_max_for(E, tu), jdl[j], jnch[j], jcpi[j]);
         }
         istart[k + 1] = istart[k] + (long long)((jnch[j] + jcpi[j] - 1) / jcpi[j]);
         P.branches += std::ldexp(1.0, E.d);
@@ -1706,7 +1711,7 @@ static int64_t request_bytes(const Target &T, const pq_tuning &tu) {
         int dl;
         unsigned long long nch;
         unsigned cpi;
-        job_shape(E, tu.chunks_per_lane, unit_max_of(tu), dl, nch, cpi);
+        job_shape(E, tu.chunks_per_lane, unit_max_for(E, tu), dl, nch, cpi);
         b += (int64_t)sizeof(JobDev) + 64 + 16 * (int64_t)((nch + cpi - 1) / cpi);
     }
     return b;

@@ -464,30 +464,57 @@ __global__ void __launch_bounds__(256, MINB) enum_kernel(KArgs a) {
             if (cend > nun) cend = nun;
             const uint64_t lomask = (E.DI >= 64) ? ~0ull : ((1ull << E.DI) - 1ull);
             const uint32_t steps = 1u << dl;
+            if (MODE == 0 && a.use_ctab && E.ctab && dl == E.DI && np == 0 && (cpi & (cpi - 1)) == 0) {
+                // Chunk-sum tables: lane l sums the item's chunks base .. base + q - 1 (base =
+                // c0 + l q, q = cpi / 32 a power of two) in Gray order, one FP64 table lookup per
+                // chunk.  A step flips one high coordinate j: the folded index gains
+                // +-Lp_j + 2 parity(G_j & s), the pivot bits R_j, the low-coordinate signs b the
+                // row G_j; chunks past the item's end are walked but not added.
+                const unsigned long long q = (unsigned long long)(cpi >> 5) ? (unsigned long long)(cpi >> 5) : 1ull;
+                const unsigned long long base = c0 + (unsigned long long)lane * q;
+                if (base < cend) {
+                    uint64_t s = (uint64_t)base << dl;
+                    uint32_t m;
+                    uint64_t yy;
+                    chunk_start(Lp, G, R, J.y0, s, m, yy);
+                    uint32_t b = 0;
+                    for (int j = 0; j < dl; j++)
+                        b |= (((uint32_t)(Lp[j] >> 1) ^ (uint32_t)popc64(G[j] & s)) & 1u) << j;
+                    const uint32_t lm32 = (uint32_t)lomask;
+                    // the run varies the coordinates dl .. dl + log2(q) - 1; when they all lie in
+                    // the first byte slice of the high weight, the other slices are one factor
+                    const bool one_slice = (dl + ctz64(q)) <= E.DI + 8;
+                    double rx = 0.0, ry = 0.0;
+                    for (unsigned long long i = 0;; ++i) {
+                        const unsigned long long ch = base + (i ^ (i >> 1));
+                        if (ch < cend) {
+                            const double2 v = rot4d(E.ctab[(yy << E.DI) | b], m & 3u);
+                            const double2 chi = one_slice ? (E.nsl_th > 0 ? E.th[(int)((s >> E.DI) & 255ull)]
+                                                                          : make_double2(1.0, 0.0))
+                                                          : chunk_high_weight(E, s);
+                            rx += v.x * chi.x - v.y * chi.y;
+                            ry += v.x * chi.y + v.y * chi.x;
+                        }
+                        if (i + 1 == q) break;
+                        const int j = dl + ctz64(i + 1);
+                        m += (((s >> j) & 1ull) ? Lm[j] : Lp[j]) + 2u * (uint32_t)(popc64(G[j] & s) & 1);
+                        yy ^= R[j];
+                        b ^= (uint32_t)G[j] & lm32;
+                        s ^= 1ull << j;
+                    }
+                    double2 rest = make_double2(1.0, 0.0);
+                    if (one_slice)
+                        for (int sl = 1; sl < E.nsl_th; sl++)
+                            rest = cmul_d(rest, E.th[sl * 256 + (int)((s >> (E.DI + 8 * sl)) & 255ull)]);
+                    accx += rx * rest.x - ry * rest.y;
+                    accy += rx * rest.y + ry * rest.x;
+                }
+            } else
             for (unsigned long long un = c0 + lane; un < cend; un += 32) {
                 // unit -> its first chunk (zeros inserted at the pair coordinates' chunk bits)
                 unsigned long long ch = un;
                 for (int i = 0; i < np; i++) ch = insert_zero(ch, E.pairc[i] - dl);
                 const uint64_t s1 = (uint64_t)ch << dl;
-                if (MODE == 0 && a.use_ctab && E.ctab && dl == E.DI) {
-                    // chunk-sum tables: one FP64 lookup per chunk instead of its 2^DI-step walk
-                    for (int kc = 0; kc < nk; kc++) {
-                        uint64_t s = s1;
-                        for (int i = 0; i < np; i++)
-                            if ((kc >> i) & 1) s |= 1ull << E.pairc[i];
-                        uint32_t m;
-                        uint64_t yy;
-                        chunk_start(Lp, G, R, J.y0, s, m, yy);
-                        uint32_t b = 0;
-                        for (int j = 0; j < dl; j++)
-                            b |= (((uint32_t)(Lp[j] >> 1) ^ (uint32_t)popc64(G[j] & s)) & 1u) << j;
-                        const double2 v = rot4d(E.ctab[(yy << E.DI) | b], m & 3u);
-                        const double2 chi = chunk_high_weight(E, s);
-                        accx += v.x * chi.x - v.y * chi.y;
-                        accy += v.x * chi.y + v.y * chi.x;
-                    }
-                    continue;
-                }
                 if (MODE != 1 && E.joint && dl >= 3) {
                     if (np == 3) {
                         if (MINB == 2) {  // eight accumulators per lane: only with the 128-register budget
