@@ -47,6 +47,7 @@ struct EngineDev {
     int zero;
     int DI, nsl_tp, nsl_th;
     int joint;               // 1: weights from the joint hi/lo table; 0: FP64 product path
+    uint8_t cperm[16];       // reference coordinate of device coordinate j < DI (identity above)
     int npairc;              // pair coordinates: the lowest (<= 3) coordinates >= DI with R = 0
     int pairc[3];            // (flipping one keeps every table index): chunks that differ only
                              // in them are walked together
@@ -271,6 +272,15 @@ PQ_HD void job_shape(const EngineDev &E, int cpl, int unit_max, int &jdl, unsign
 // Index with a zero bit inserted at position b.
 PQ_HD unsigned long long insert_zero(unsigned long long x, int b) {
     return ((x >> b) << (b + 1)) | (x & ((1ull << b) - 1ull));
+}
+
+// A point of the branch subspace in the reference's coordinates, in the device's order (the
+// low DI coordinates are reordered when the engine is packed).
+PQ_HD uint64_t to_device_order(const EngineDev &E, uint64_t s_ref) {
+    const uint64_t lomask = E.DI >= 64 ? ~0ull : ((1ull << E.DI) - 1ull);
+    uint64_t s = s_ref & ~lomask;
+    for (int j = 0; j < E.DI && j < 16; j++) s |= ((s_ref >> E.cperm[j]) & 1ull) << j;
+    return s;
 }
 
 // Chunk start: Z4 index m and pivot bits y at kernel point s (bits in ascending order).

@@ -137,8 +137,12 @@ static pq_status upload_target(Target &T, int di_max) {
     T.bytes = 0;
     T.branches_per_amp = 0.0;
     for (auto &e : T.rs.branches) {
-        EngineTables tb = build_tables(*e, di_max);
-        PackedEngine pk = pack_engine(*e, tb);
+        // pack a copy in the device's coordinate order (even-increment low coordinates first)
+        std::vector<int> perm;
+        const HostEngine pe = device_order(*e, build_tables(*e, di_max).DI, perm);
+        EngineTables tb = build_tables(pe, di_max);
+        PackedEngine pk = pack_engine(pe, tb);
+        for (int j = 0; j < 16; j++) pk.off.cperm[j] = (uint8_t)(j < tb.DI ? perm[(size_t)j] : j);
         auto m = std::make_unique<DevMem>();
         CU(m->alloc(pk.blob.size()));
         CU(cudaMemcpy(m->p, pk.blob.data(), pk.blob.size(), cudaMemcpyHostToDevice));
@@ -1481,13 +1485,17 @@ PQ_API int32_t pq_debug_branch_phases(pq_sim *s, int32_t branch, const uint64_t 
     cudaMemsetAsync(P.counter.p, 0, sizeof(unsigned long long), P.stream);
     enum_kernel<2><<<P.grid_enum, P.block_enum, 0, P.stream>>>(P.args);
     JobDev J;
+    std::vector<uint8_t> dev((size_t)1 << d);
     if (cudaMemcpyAsync(&J, P.jobs.p, sizeof(JobDev), cudaMemcpyDeviceToHost, P.stream) != cudaSuccess) return -2;
-    if (cudaMemcpyAsync(out, dbg.p, (size_t)1 << d, cudaMemcpyDeviceToHost, P.stream) != cudaSuccess) return -2;
+    if (cudaMemcpyAsync(dev.data(), dbg.p, (size_t)1 << d, cudaMemcpyDeviceToHost, P.stream) != cudaSuccess) return -2;
     cudaError_t e = cudaStreamSynchronize(P.stream);
     if (e != cudaSuccess) {
         g_err = cudaGetErrorString(e);
         return -2;
     }
+    // the kernel indexes branches in the device's coordinate order: back to the reference's
+    const EngineDev &E = view.dev[0];
+    for (uint64_t sr = 0; sr < (1ull << d); sr++) out[sr] = dev[(size_t)to_device_order(E, sr)];
     return J.vanish ? -1 : d;
 }
 

@@ -796,6 +796,41 @@ PackedEngine pack_engine(const HostEngine& e, const EngineTables& T) {
     return P;
 }
 
+HostEngine device_order(const HostEngine& e, int DI, std::vector<int>& perm) {
+    // Coordinates whose Z4 increment is even first (stable), then the odd ones, among the low
+    // DI coordinates: the walk's fixed-position steps are then even quarter turns (paired FMA)
+    // for almost every engine.  perm[j] = reference coordinate of device coordinate j.
+    const int d = e.d;
+    perm.resize((size_t)d);
+    int k = 0;
+    for (int j = 0; j < DI; j++)
+        if (!e.lp0[(size_t)j]) perm[(size_t)k++] = j;
+    for (int j = 0; j < DI; j++)
+        if (e.lp0[(size_t)j]) perm[(size_t)k++] = j;
+    for (int j = DI; j < d; j++) perm[(size_t)j] = j;
+    HostEngine p = e;
+    const int abo = e.L.abo();
+    std::vector<int> inv((size_t)d);
+    for (int j = 0; j < d; j++) inv[(size_t)perm[(size_t)j]] = j;
+    for (int j = 0; j < d; j++) {
+        const int r = perm[(size_t)j];
+        std::copy(e.ku.begin() + (size_t)r * abo, e.ku.begin() + (size_t)(r + 1) * abo, p.ku.begin() + (size_t)j * abo);
+        p.kernel[(size_t)j] = e.kernel[(size_t)r];
+        p.R[(size_t)j] = e.R[(size_t)r];
+        p.free_col[(size_t)j] = e.free_col[(size_t)r];
+        p.lp0[(size_t)j] = e.lp0[(size_t)r];
+    }
+    std::fill(p.Gw.begin(), p.Gw.end(), 0ull);
+    for (int i = 0; i < d; i++)
+        for (int j = 0; j < d; j++)
+            if ((e.Gw[(size_t)i * e.dw + (size_t)(j >> 6)] >> (j & 63)) & 1ull) {
+                const int a = inv[(size_t)i], b = inv[(size_t)j];
+                p.Gw[(size_t)a * p.dw + (size_t)(b >> 6)] |= 1ull << (b & 63);
+            }
+    for (int j = 0; j < d; j++) p.G[(size_t)j] = p.Gw[(size_t)j * p.dw];
+    return p;
+}
+
 EngineDev rebase_engine(const EngineDev& o, const uint8_t* base) {
     EngineDev d = o;
     d.o1 = shift(o.o1, base); d.o3 = shift(o.o3, base); d.wa = shift(o.wa, base); d.wb = shift(o.wb, base);

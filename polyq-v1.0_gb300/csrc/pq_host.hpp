@@ -193,6 +193,9 @@ struct PackedEngine {
     EngineDev off;
 };
 PackedEngine pack_engine(const HostEngine& e, const EngineTables& t);
+// Copy of e with its low DI coordinates reordered for the device (see pq_host.cpp); perm[j] is
+// the reference coordinate of device coordinate j.
+HostEngine device_order(const HostEngine& e, int DI, std::vector<int>& perm);
 EngineDev rebase_engine(const EngineDev& off, const uint8_t* base);
 
 // Boundary map: `puts` lists (variable, boundary source) in the order the reference's

@@ -703,7 +703,7 @@ __global__ void __launch_bounds__(256) mc_kernel(const EngineDev *__restrict__ E
     for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < samples;
          k += (long long)gridDim.x * blockDim.x) {
         const uint64_t ci = (uint64_t)(k >> 10), kk = (uint64_t)(k & 1023);
-        const uint64_t s = splitmix_at((seed ^ (ci * golden)) + golden + (kk + 1ull) * golden) & dmask;
+        const uint64_t s = to_device_order(E, splitmix_at((seed ^ (ci * golden)) + golden + (kk + 1ull) * golden) & dmask);
         uint32_t m;
         uint64_t yy;
         chunk_start(sLp, sG, sR, J.y0, s, m, yy);
@@ -766,6 +766,7 @@ __global__ void __launch_bounds__(256) mc_big_kernel(const EngineDev *__restrict
                 s[w] = v;
             }
         }
+        s[0] = to_device_order(E, s[0]);  // the reordered low coordinates all lie in word 0
         uint32_t m = 0, t = 0;
         uint64_t yy = J.y0;
         for (int w = 0; w < nwd; w++)
