@@ -212,10 +212,12 @@ PQ_HD void fixed_constants_partial(const EngineDev &E, const uint64_t *vals, int
 
 // u0 = xor of the boundary columns of the fixed variables set to 1, words [w0, W) step ws.
 PQ_HD void boundary_shift_partial(const EngineDev &E, const uint64_t *vals, uint64_t *u, int w0, int ws) {
+    const int nvw = (E.nf + 63) >> 6;
     for (int w = w0; w < E.W; w += ws) {
         uint64_t acc = 0;
-        for (int f = 0; f < E.nf; f++)
-            if (bit_at(vals, f)) acc ^= E.ucols[(size_t)f * E.W + w];
+        for (int vw = 0; vw < nvw; vw++)  // only the fixed variables set to 1
+            for (uint64_t r = vals[vw]; r; r &= r - 1)
+                acc ^= E.ucols[(size_t)((vw << 6) + ctz64(r)) * E.W + w];
         u[w] = acc;
     }
 }
