@@ -242,6 +242,13 @@ static pq_status build_plan(const std::vector<Segment> &segs, int nw, cudaStream
                           &P.errflag})
             m->astream = P.stream;
     }
+    {
+        // (boundary, branch engine) jobs are indexed with 32-bit integers on the device
+        double total = 0.0;
+        for (const auto &sg : segs) total += (double)sg.count * (double)sg.tg->dev.size();
+        if (total > (double)(1 << 28))
+            return fail(PQ_ERR_INVALID_ARG, "boundaries x branch engines above 2^28 in one launch; split the call");
+    }
     std::vector<EngineDev> eng;
     std::vector<IoMapDev> maps;
     std::vector<JobDev> jobs;
