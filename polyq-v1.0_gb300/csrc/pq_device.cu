@@ -187,6 +187,7 @@ struct Plan {
     int smem_words = 8;
     int grid_prep = 1, grid_enum = 1, block_enum = 256;
     int minb = 3;  // enum_kernel<0, minb> instantiation (blocks per SM its registers allow)
+    uint64_t last_use = 0;  // recency in the owning simulator's plan cache
     bool graph_ready = false;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
@@ -526,6 +527,7 @@ struct pq_sim {
     double build_s = 0.0;
     std::mutex mu;
     std::map<int64_t, std::unique_ptr<Plan>> plans;
+    uint64_t use_clock = 0;
     bool have_sw = false;
     PathSum sw;
     std::vector<int> junction;
@@ -553,6 +555,7 @@ struct pq_batch {
 };
 
 static int words_for(int nq) { return std::max(1, (nq + 63) / 64); }
+static const size_t kMaxPlans = 16;  // cached launch plans per simulator (boundary counts)
 
 // puts for <y|C|x> (src/pathsum.rs:430-450)
 static IoMapHost main_iomap(const PathSum &ps) {
@@ -714,13 +717,24 @@ static pq_status sim_plan(pq_sim *s, int64_t n, Plan **out) {
     if (s->host_only) return fail(PQ_ERR_NO_DEVICE, "simulator was created by pq_analyze (host structures only)");
     auto it = s->plans.find(n);
     if (it != s->plans.end()) {
+        it->second->last_use = ++s->use_clock;
         *out = it->second.get();
         return PQ_OK;
+    }
+    // plans are cached per boundary count; past kMaxPlans, the least recently used one goes
+    // (after the simulator's stream drains: device-pointer calls may still be running on it)
+    if (s->plans.size() >= kMaxPlans) {
+        auto victim = s->plans.begin();
+        for (auto pi = s->plans.begin(); pi != s->plans.end(); ++pi)
+            if (pi->second->last_use < victim->second->last_use) victim = pi;
+        CU(cudaStreamSynchronize(s->stream));
+        s->plans.erase(victim);
     }
     auto P = std::make_unique<Plan>();
     std::vector<Segment> segs{{&s->main, n}};
     pq_status st = build_plan(segs, s->nw, s->stream, s->tu, *P);
     if (st != PQ_OK) return st;
+    P->last_use = ++s->use_clock;
     *out = P.get();
     s->plans[n] = std::move(P);
     return PQ_OK;

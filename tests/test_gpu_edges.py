@@ -62,3 +62,14 @@ def test_batch_with_empty_member(gpu):
     assert got.shape == (5,)
     assert np.max(np.abs(got[:2] - sims[0].amplitudes([0, 0], [1, 2]))) < 1e-15
     assert np.max(np.abs(got[2:] - sims[2].amplitudes([0, 0, 0], [3, 4, 5]))) < 1e-15
+
+
+def test_plan_cache_is_bounded(gpu):
+    # 20 distinct boundary counts: older launch plans are evicted, results stay the same
+    c = random_clifford_t(6, 40, 6, False, Rng(5))
+    sim = Simulator(c)
+    ref = O.OracleSim(c)
+    ys = [(5 * i + 3) % 64 for i in range(40)]
+    for n in list(range(1, 21)) + [3, 1]:
+        got = sim.amplitudes([0] * n, ys[:n])
+        assert np.max(np.abs(got - ref.amplitudes([0] * n, ys[:n]))) < 1e-12
