@@ -337,7 +337,7 @@ def run_gb300(args):
     ref_peak = ops_step / t_peak
     ref_achieved = ops_step / (enum_avg * 1e-3)
     cpu = None
-    if rank == 0 and not args.no_cpu:
+    if rank == 0 and ws == 1 and not args.no_cpu:  # the CPU baseline is taken at N=1 only
         threads = cpu_threads()
         sample = max(4, int(args.cpu_sample))
         cbr, dt = cpu_rate(circ, ys, sample, threads)
