@@ -300,7 +300,7 @@ def run_gb300(args):
         ms = sum(step_ms) / len(step_ms)
         ms = max_over_ranks(dist, ms)
         value = replica_rate(ws, branches_step, ms)
-        # FP32-compensated results of the last step against the device FP64 mode
+        # FP32 results of the last step against the device FP64 mode
         got = dout.cpu().numpy().view(np.complex128).copy()
         errb = derr.cpu().numpy().copy()
     ref = sim.amplitudes_fp64([0] * n, ys)
@@ -713,7 +713,7 @@ def run_estimate(args):
 
 
 def run_rotations(args):
-    """Arbitrary angles: rz(theta) slots plus CCZ layers, FP32-compensated vs device FP64 per
+    """Arbitrary angles: rz(theta) slots plus CCZ layers, the FP32 path vs device FP64 per
     amplitude; a 20-qubit variant also against the dense statevector."""
     import numpy as np
 

@@ -104,7 +104,8 @@ PQ_API pq_status pq_sim_stats(const pq_sim *sim, pq_stats *out);
 
 /* Simulator::amplitude / amplitude_index for n boundaries -- sim.rs:171-182.
  * x, y: n bitstrings each (host memory).  out: 2n doubles.  errbound (optional, n doubles):
- * bound on |out - exact| from FP32 branch weights (compensated accumulation, FP64 reduction). */
+ * bound on |out - exact| from the FP32 weight arithmetic (exact-grid hi sums, FP32 lo sums,
+ * FP64 reduction). */
 PQ_API pq_status pq_amplitudes(pq_sim *sim, int64_t n, const uint64_t *x, const uint64_t *y, double *out,
                                double *errbound);
 /* Simulator::probability -- sim.rs:196-198: |amplitude|^2, n doubles. */

@@ -16,8 +16,9 @@
 //     kernel vector j).  Hence c(s) = W[y, s & lomask] * CHI(s >> DI): W is the FP64 product of
 //     the first DI coordinates' weights and the pivot weights, stored as an FP32 hi/lo pair;
 //     CHI is the FP64 product over byte slices of the coordinates >= DI (once per chunk).
-//     The hi parts are summed with TwoSum, the lo parts in plain FP32, so the only per-branch
-//     rounding left is of order u^2.
+//     hi lies on an exact power-of-two grid, so its chunk sums are exact in FP32 in any
+//     order and under quarter turns; lo = W - hi is summed in plain FP32, so the per-branch
+//     rounding left is that of the small lo parts.
 #pragma once
 #include <stdint.h>
 

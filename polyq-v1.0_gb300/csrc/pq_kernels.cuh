@@ -4,10 +4,12 @@
 //                    constants, boundary shift u0 = xor of resident boundary columns, radical
 //                    consistency + particular solution (pivot bits y0), start shift, Z8 index
 //                    k0 and the Z4 linear coefficients Lp_j        (src/engine.rs:569-610)
-//   enum_kernel      persistent: each warp pulls work items (a job's contiguous chunk range)
-//                    from an atomic counter; lane l walks chunks l, l+32, ... of the item in
-//                    Gray order: one AND+POPC Z8 update, one table weight, compensated FP32
-//                    accumulation; FP64 scaling of each chunk and an FP64 warp-shuffle reduce
+//   enum_kernel      persistent: each warp pulls work items (a job's contiguous range of
+//                    units of 1-8 chunks) from an atomic counter; lane l walks units l, l+32,
+//                    ... in Gray order in a rotating frame over the sign-folded weight table:
+//                    per step one table load and index xor shared by the unit's chunks, and a
+//                    quarter-turn-and-add of each chunk's exact-grid hi and FP32 lo sums; FP64
+//                    scaling of each chunk and an FP64 warp-shuffle reduce
 //                    (src/engine.rs:669-722, normal_form.rs:479-493)
 //   job_reduce       FP64 sum of a job's item partials in item order, times the Z8 root of k0,
 //                    e^{i phase} and 2^{(mag2 - h)/2}                  (src/engine.rs:557-565)
@@ -401,7 +403,8 @@ __device__ __forceinline__ void walk_unit(const EngineDev &E, const JobDev &J, c
     }
 }
 
-// MODE 0: FP32 weights, compensated accumulation.  MODE 1: FP64 weights and accumulation.
+// MODE 0: FP32 weights (exact-grid hi + lo) in the rotating-frame walk.  MODE 1: FP64 weights
+// and accumulation.
 // MODE 2: record the Z8 index of every branch into dbg (single-job debug launches).
 // MINB: resident blocks of 256 threads per SM the register allocation is sized for (2: 128,
 // 3: 80, 4: 64 registers per thread) -- chosen per launch by measurement.
@@ -627,11 +630,11 @@ __global__ void job_reduce_kernel(KArgs a) {
         const double mag = pow2_half(E.mag2 - E.num_h);
         v.x *= mag;
         v.y *= mag;
-        // Rigorous bound on |computed - exact| relative to sum_s |c(s)| * mag:
-        //  joint table: weights exact to 2^-46 (hi + lo of an FP64 product); TwoSum over a chunk
-        //  of n = 2^dl terms errs by <= gamma_n^2 sum|p| (gamma_n = n u / (1 - n u)); the lo sum
-        //  by <= n u * (u sum|c|); FP64 chunk scaling and reductions by a few 2^-52.
-        //  FP64 path: (n + 2 * nsl_tp + 8) 2^-53.
+        // Bound on |computed - exact| relative to sum_s |c(s)| * mag (conservative):
+        //  joint table: weights exact to 2^-46 (hi + lo of an FP64 product); hi chunk sums are
+        //  exact, the terms below keep an allowance of gamma_n^2 + 2 n u^2 (gamma_n = n u /
+        //  (1 - n u), n = 2^dl) for them; FP64 chunk scaling and reductions a few 2^-52; the lo
+        //  sums add errfac (per engine, from the grid).  FP64 path: (n + 2 nsl_tp + 8) 2^-53.
         const double u32 = 5.9604644775390625e-08, u64 = 1.1102230246251565e-16;
         const double n = (double)(1ull << (a.jdl[j] & 255));
         double rel;
