@@ -187,6 +187,7 @@ struct Plan {
     int smem_words = 8;
     int grid_prep = 1, grid_enum = 1, block_enum = 256;
     int minb = 3;  // enum_kernel<0, minb> instantiation (blocks per SM its registers allow)
+    bool any_ctab = false;  // some job can take its chunk sums from a chunk-sum table
     uint64_t last_use = 0;  // recency in the owning simulator's plan cache
     bool graph_ready = false;
     cudaStream_t stream = nullptr;
@@ -315,6 +316,7 @@ static pq_status build_plan(const std::vector<Segment> &segs, int nw, cudaStream
         }
         istart[k + 1] = istart[k] + (long long)((jnch[j] + jcpi[j] - 1) / jcpi[j]);
         P.branches += std::ldexp(1.0, E.d);
+        if (E.ctab && (jdl[j] & 255) == E.DI) P.any_ctab = true;
     }
     P.nitems = istart[P.njobs];
     CU(upload(P.engines, eng));
@@ -453,10 +455,24 @@ static pq_status run_host(Plan &P, const uint64_t *x, const uint64_t *y, double 
     if (prob) {
         // Probabilities are promised to 1e-12 absolute: when the FP32 bound cannot certify
         // that, the same launch shape is re-run with FP64 weights and FP64 accumulation.
-        bool escalate = false;
-        for (int o = 0; o < P.nout && !escalate; o++) {
-            double a = std::sqrt(ho[2 * o] * ho[2 * o] + ho[2 * o + 1] * ho[2 * o + 1]);
-            escalate = he[o] * (2.0 * a + he[o]) > 1e-12;
+        auto uncertified = [&]() {
+            for (int o = 0; o < P.nout; o++) {
+                double a = std::sqrt(ho[2 * o] * ho[2 * o] + ho[2 * o + 1] * ho[2 * o + 1]);
+                if (he[o] * (2.0 * a + he[o]) > 1e-12) return true;
+            }
+            return false;
+        };
+        bool escalate = uncertified();
+        if (escalate && P.any_ctab && !P.args.use_ctab) {
+            // first the chunk-sum tables (FP64, faster than the walk), with their own bound
+            P.args.use_ctab = 1;
+            cudaError_t e = enqueue_core(P, 0);
+            P.args.use_ctab = 0;
+            CU(e);
+            CU(cudaMemcpyAsync(P.hout.p, P.out.p, (size_t)P.nout * 16, cudaMemcpyDeviceToHost, P.stream));
+            CU(cudaMemcpyAsync(P.herr.p, P.err.p, (size_t)P.nout * 8, cudaMemcpyDeviceToHost, P.stream));
+            CU(cudaStreamSynchronize(P.stream));
+            escalate = uncertified();
         }
         if (escalate) {
             CU(enqueue_core(P, 1));

@@ -518,6 +518,26 @@ __global__ void __launch_bounds__(256, MINB) enum_kernel(KArgs a) {
                 unsigned long long ch = un;
                 for (int i = 0; i < np; i++) ch = insert_zero(ch, E.pairc[i] - dl);
                 const uint64_t s1 = (uint64_t)ch << dl;
+                if (MODE == 0 && a.use_ctab && E.ctab && dl == E.DI) {
+                    // chunk-sum tables on a plan laid out for the walk (units of several
+                    // chunks): each chunk from its own start
+                    for (int kc = 0; kc < nk; kc++) {
+                        uint64_t s = s1;
+                        for (int i = 0; i < np; i++)
+                            if ((kc >> i) & 1) s |= 1ull << E.pairc[i];
+                        uint32_t m;
+                        uint64_t yy;
+                        chunk_start(Lp, G, R, J.y0, s, m, yy);
+                        uint32_t b = 0;
+                        for (int j = 0; j < dl; j++)
+                            b |= (((uint32_t)(Lp[j] >> 1) ^ (uint32_t)popc64(G[j] & s)) & 1u) << j;
+                        const double2 v = rot4d(E.ctab[(yy << E.DI) | b], m & 3u);
+                        const double2 chi = chunk_high_weight(E, s);
+                        accx += v.x * chi.x - v.y * chi.y;
+                        accy += v.x * chi.y + v.y * chi.x;
+                    }
+                    continue;
+                }
                 if (MODE != 1 && E.joint && dl >= 3) {
                     if (np == 3) {
                         if (MINB == 2) {  // eight accumulators per lane: only with the 128-register budget
@@ -638,14 +658,20 @@ __global__ void job_reduce_kernel(KArgs a) {
         const double u32 = 5.9604644775390625e-08, u64 = 1.1102230246251565e-16;
         const double n = (double)(1ull << (a.jdl[j] & 255));
         double rel;
-        if (E.joint) {
+        const int dlj = a.jdl[j] & 255;
+        const bool ctab = a.use_ctab && E.ctab && dlj == E.DI;
+        if (ctab) {
+            // FP64 chunk-sum table (a DI-stage transform of FP64 products) and FP64 sums of at
+            // most 2^(d - DI) chunk values per job, item partials and the warp reduction
+            rel = ((double)E.DI + 2.0 * (double)(1ull << (E.d - E.DI)) + 64.0) * 2.0 * u64;
+        } else if (E.joint) {
             const double g = n * u32 / (1.0 - n * u32);
             rel = g * g + 2.0 * n * u32 * u32 + 1.5e-14 + 64.0 * u64;
         } else {
             rel = (n + 2.0 * E.nsl_tp + 8.0 + (double)E.nsl_th) * 2.0 * u64;
         }
         eb = rel * E.sum_abs_bound * mag;
-        if (E.joint) eb += E.errfac * mag;  // lo-part sums of the unrolled walk (exact hi sums)
+        if (E.joint && !ctab) eb += E.errfac * mag;  // lo-part sums of the walk (exact hi sums)
     }
     a.job_vals[j] = v;
     a.job_err[j] = eb;

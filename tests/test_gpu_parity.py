@@ -349,3 +349,17 @@ def test_chunk_tables_match_fp64(gpu):
             assert_amps(a, r, err)  # within the reported bound; FP64 rounding of cancelling sums
     finally:
         set_tuning(chunk_tables=2)
+
+
+def test_probabilities_of_large_amplitudes(gpu):
+    # 8 qubits, 40 T, one cached engine of d = 20-22: amplitudes of order 2^-4, where the FP32
+    # bound cannot certify 1e-12 on |a|^2 and the probability is re-evaluated (chunk-sum
+    # tables, then FP64 if needed); all 256 probabilities against the dense statevector
+    from polyq_gb300.rng import workload_circuit
+    for seed in (5, 7):
+        c = workload_circuit(8, 240, 40, seed)
+        s = Simulator(c, "cached")
+        p = s.probabilities([0] * 256, list(range(256)))
+        want = np.abs(O.dense_statevector(c, 0)) ** 2
+        assert np.max(np.abs(p - want)) <= 1e-12
+        assert abs(np.sum(p) - 1.0) < 1e-9
