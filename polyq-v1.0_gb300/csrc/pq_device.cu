@@ -406,16 +406,18 @@ static cudaError_t enqueue_core(Plan &P, int mode) {
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(P.counter.p, 0, sizeof(unsigned long long), P.stream);
     if (e != cudaSuccess) return e;
+    KArgs args = P.args;
+    args.fp64_mode = mode == 1 ? 1 : 0;
     if ((e = cudaEventRecordWithFlags(P.tev[0], P.stream, evflag)) != cudaSuccess) return e;
-    prepare_kernel<<<P.grid_prep, 128, (size_t)4 * P.smem_words * 8, P.stream>>>(P.args);
+    prepare_kernel<<<P.grid_prep, 128, (size_t)4 * P.smem_words * 8, P.stream>>>(args);
     if ((e = cudaEventRecordWithFlags(P.tev[1], P.stream, evflag)) != cudaSuccess) return e;
-    if (mode == 1) enum_kernel<1><<<P.grid_enum, P.block_enum, 0, P.stream>>>(P.args);
-    else if (P.minb == 4) enum_kernel<0, 4><<<P.grid_enum, P.block_enum, 0, P.stream>>>(P.args);
-    else if (P.minb == 2) enum_kernel<0, 2><<<P.grid_enum, P.block_enum, 0, P.stream>>>(P.args);
-    else enum_kernel<0, 3><<<P.grid_enum, P.block_enum, 0, P.stream>>>(P.args);
+    if (mode == 1) enum_kernel<1><<<P.grid_enum, P.block_enum, 0, P.stream>>>(args);
+    else if (P.minb == 4) enum_kernel<0, 4><<<P.grid_enum, P.block_enum, 0, P.stream>>>(args);
+    else if (P.minb == 2) enum_kernel<0, 2><<<P.grid_enum, P.block_enum, 0, P.stream>>>(args);
+    else enum_kernel<0, 3><<<P.grid_enum, P.block_enum, 0, P.stream>>>(args);
     if ((e = cudaEventRecordWithFlags(P.tev[2], P.stream, evflag)) != cudaSuccess) return e;
-    job_reduce_kernel<<<(P.njobs + 255) / 256, 256, 0, P.stream>>>(P.args);
-    out_reduce_kernel<<<(P.nout + 255) / 256, 256, 0, P.stream>>>(P.args);
+    job_reduce_kernel<<<(P.njobs + 255) / 256, 256, 0, P.stream>>>(args);
+    out_reduce_kernel<<<(P.nout + 255) / 256, 256, 0, P.stream>>>(args);
     if ((e = cudaEventRecordWithFlags(P.tev[3], P.stream, evflag)) != cudaSuccess) return e;
     return cudaGetLastError();
 }
@@ -437,7 +439,14 @@ static pq_status launch_graph(Plan &P) {
 }
 
 // Host-buffer run: H2D boundaries, graph, D2H results, wait.
-static pq_status run_host(Plan &P, const uint64_t *x, const uint64_t *y, double *out, double *err, bool prob) {
+// What a host run must certify to 1e-12 absolute: nothing (amplitudes carry their bound), the
+// probability |a|^2, or the real part (a marginal probability).
+enum Certify { CERT_NONE = 0, CERT_PROB = 1, CERT_REAL = 2 };
+
+// Host-buffer run: H2D boundaries, graph, D2H results, wait.  Under CERT_PROB / CERT_REAL, when
+// the FP32 bound cannot certify 1e-12 absolute, the same launch shape is re-run from the
+// chunk-sum tables (FP64) and then, if still needed, with FP64 weights and accumulation.
+static pq_status run_host(Plan &P, const uint64_t *x, const uint64_t *y, double *out, double *err, Certify cert) {
     const size_t bw = (size_t)P.nreq * P.nw * 8;
     std::memcpy(P.hx.p, x, bw);
     std::memcpy(P.hy.p, y, bw);
@@ -452,45 +461,48 @@ static pq_status run_host(Plan &P, const uint64_t *x, const uint64_t *y, double 
     if (*P.herrflag.as<int>()) return fail(PQ_ERR_INTERNAL, "device self-check failed (odd Z8 increment)");
     const double *ho = P.hout.as<double>();
     const double *he = P.herr.as<double>();
-    if (prob) {
-        // Probabilities are promised to 1e-12 absolute: when the FP32 bound cannot certify
-        // that, the same launch shape is re-run with FP64 weights and FP64 accumulation.
-        auto uncertified = [&]() {
-            for (int o = 0; o < P.nout; o++) {
-                double a = std::sqrt(ho[2 * o] * ho[2 * o] + ho[2 * o + 1] * ho[2 * o + 1]);
-                if (he[o] * (2.0 * a + he[o]) > 1e-12) return true;
-            }
-            return false;
-        };
-        bool escalate = uncertified();
-        if (escalate && P.any_ctab && !P.args.use_ctab) {
-            // first the chunk-sum tables (FP64, faster than the walk), with their own bound
-            P.args.use_ctab = 1;
-            cudaError_t e = enqueue_core(P, 0);
-            P.args.use_ctab = 0;
-            CU(e);
-            CU(cudaMemcpyAsync(P.hout.p, P.out.p, (size_t)P.nout * 16, cudaMemcpyDeviceToHost, P.stream));
-            CU(cudaMemcpyAsync(P.herr.p, P.err.p, (size_t)P.nout * 8, cudaMemcpyDeviceToHost, P.stream));
-            CU(cudaStreamSynchronize(P.stream));
-            escalate = uncertified();
+    auto bound_of = [&](int o) {
+        if (cert == CERT_PROB) {
+            const double a = std::sqrt(ho[2 * o] * ho[2 * o] + ho[2 * o + 1] * ho[2 * o + 1]);
+            return he[o] * (2.0 * a + he[o]);
         }
-        if (escalate) {
-            CU(enqueue_core(P, 1));
-            CU(cudaMemcpyAsync(P.hout.p, P.out.p, (size_t)P.nout * 16, cudaMemcpyDeviceToHost, P.stream));
-            CU(cudaStreamSynchronize(P.stream));
-            double *hw = P.herr.as<double>();
-            for (int o = 0; o < P.nout; o++) hw[o] = 0.0;  // FP64 path: rounding far below 1e-12
+        return he[o];
+    };
+    auto uncertified = [&]() {
+        for (int o = 0; o < P.nout; o++)
+            if (bound_of(o) > 1e-12) return true;
+        return false;
+    };
+    auto rerun = [&](int mode, int ctab) -> pq_status {
+        const int saved = P.args.use_ctab;
+        P.args.use_ctab = ctab;
+        cudaError_t e = enqueue_core(P, mode);
+        P.args.use_ctab = saved;
+        CU(e);
+        CU(cudaMemcpyAsync(P.hout.p, P.out.p, (size_t)P.nout * 16, cudaMemcpyDeviceToHost, P.stream));
+        CU(cudaMemcpyAsync(P.herr.p, P.err.p, (size_t)P.nout * 8, cudaMemcpyDeviceToHost, P.stream));
+        CU(cudaStreamSynchronize(P.stream));
+        return PQ_OK;
+    };
+    if (cert != CERT_NONE && uncertified()) {
+        if (P.any_ctab && !P.args.use_ctab) {
+            st = rerun(0, 1);
+            if (st != PQ_OK) return st;
+        }
+        if (uncertified()) {
+            st = rerun(1, 0);
+            if (st != PQ_OK) return st;
         }
     }
     for (int o = 0; o < P.nout; o++) {
-        if (prob) {
+        if (cert == CERT_PROB) {
             double re = ho[2 * o], im = ho[2 * o + 1];
             out[o] = re * re + im * im;
         } else {
             out[2 * o] = ho[2 * o];
             out[2 * o + 1] = ho[2 * o + 1];
         }
-        if (err) err[o] = prob ? he[o] * (2.0 * std::sqrt(ho[2 * o] * ho[2 * o] + ho[2 * o + 1] * ho[2 * o + 1]) + he[o]) : he[o];
+        if (err) err[o] = bound_of(o);
     }
     return PQ_OK;
 }
@@ -772,7 +784,7 @@ PQ_API pq_status pq_amplitudes(pq_sim *s, int64_t n, const uint64_t *x, const ui
     Plan *P = nullptr;
     st = sim_plan(s, n, &P);
     if (st != PQ_OK) return st;
-    return run_host(*P, x, y, out, errbound, false);
+    return run_host(*P, x, y, out, errbound, CERT_NONE);
 }
 
 PQ_API pq_status pq_probabilities(pq_sim *s, int64_t n, const uint64_t *x, const uint64_t *y, double *out) {
@@ -785,7 +797,7 @@ PQ_API pq_status pq_probabilities(pq_sim *s, int64_t n, const uint64_t *x, const
     Plan *P = nullptr;
     st = sim_plan(s, n, &P);
     if (st != PQ_OK) return st;
-    return run_host(*P, x, y, out, nullptr, true);
+    return run_host(*P, x, y, out, nullptr, CERT_PROB);
 }
 
 PQ_API pq_status pq_amplitudes_device(pq_sim *s, int64_t n, const uint64_t *x, const uint64_t *y, double *out,
@@ -813,7 +825,7 @@ PQ_API pq_status pq_amplitudes_plain(pq_sim *s, int64_t n, const uint64_t *x, co
     st = sim_plan(s, 1, &P);
     if (st != PQ_OK) return st;
     for (int64_t i = 0; i < n; i++) {
-        st = run_host(*P, x + (size_t)i * s->nw, y + (size_t)i * s->nw, out + 2 * i, nullptr, false);
+        st = run_host(*P, x + (size_t)i * s->nw, y + (size_t)i * s->nw, out + 2 * i, nullptr, CERT_NONE);
         if (st != PQ_OK) return st;
     }
     return PQ_OK;
@@ -896,7 +908,7 @@ PQ_API pq_status pq_marginal(pq_sim *s, const uint64_t *x, int32_t nmeas, const 
         if (outcomes[i]) yv[qubits[i] >> 6] |= 1ull << (qubits[i] & 63);
     // repeated measured qubits with different outcomes contradict: the map's check makes it 0
     double amp[2];
-    st = run_host(*M->plan, x, yv.data(), amp, nullptr, false);
+    st = run_host(*M->plan, x, yv.data(), amp, nullptr, CERT_REAL);
     if (st != PQ_OK) return st;
     *out = amp[0] > 0.0 ? amp[0] : 0.0;
     return PQ_OK;
@@ -993,7 +1005,7 @@ PQ_API pq_status pq_amplitude_estimate(pq_sim *s, const uint64_t *x, const uint6
             std::memcpy(&Y[k * nw], y, sizeof(uint64_t) * nw);
         }
         std::vector<double> amp(2 * segs.size());
-        st = run_host(P, X.data(), Y.data(), amp.data(), nullptr, false);
+        st = run_host(P, X.data(), Y.data(), amp.data(), nullptr, CERT_NONE);
         if (st != PQ_OK) return st;
         double sx = 0.0, sy = 0.0, sq = 0.0;
         for (size_t k = 0; k < segs.size(); k++) {
@@ -1014,7 +1026,7 @@ PQ_API pq_status pq_amplitude_estimate(pq_sim *s, const uint64_t *x, const uint6
         Plan *P = nullptr;
         pq_status st = sim_plan(s, 1, &P);
         if (st != PQ_OK) return st;
-        return run_host(*P, x, y, out, nullptr, false);
+        return run_host(*P, x, y, out, nullptr, CERT_NONE);
     }
     if (E.d > kMaxD) {
         // beyond the enumeration's limits: prepare alone, then the multi-word sampler
@@ -1106,7 +1118,7 @@ PQ_API pq_status pq_sample_many(pq_sim *s, const uint64_t *x, int64_t shots, uin
             slot = std::move(P);
         }
         Plan &P = *slot;
-        st = run_host(P, X.data(), Y.data(), amp.data(), err.data(), false);
+        st = run_host(P, X.data(), Y.data(), amp.data(), err.data(), CERT_NONE);
         if (st != PQ_OK) return st;
         bool any_tie = false;
         for (size_t i = 0; i < ns; i++) {
@@ -1181,7 +1193,7 @@ PQ_API pq_status pq_batch_run(pq_batch *b, const uint64_t *x, const uint64_t *y,
     if (!b || !x || !y || !out) return fail(PQ_ERR_INVALID_ARG, "null argument");
     std::lock_guard<std::mutex> lk(b->mu);
     if (!b->plan) return fail(PQ_ERR_INTERNAL, "batch has no launch plan (a failed autotune left none)");
-    return run_host(*b->plan, x, y, out, err, false);
+    return run_host(*b->plan, x, y, out, err, CERT_NONE);
 }
 PQ_API pq_status pq_batch_run_device(pq_batch *b, const uint64_t *x, const uint64_t *y, double *out, double *err,
                                      void *stream) {
@@ -1282,7 +1294,7 @@ static pq_status time_tuning(pq_sim *s, int64_t n, const uint64_t *x, const uint
     scratch.resize((size_t)2 * n);
     double best = 1e300;
     for (int r = 0; r <= reps; r++) {
-        st = run_host(P, x, y, scratch.data(), nullptr, false);
+        st = run_host(P, x, y, scratch.data(), nullptr, CERT_NONE);
         if (st != PQ_OK) return st;
         float ms[3];
         st = last_kernel_ms(P, ms);
@@ -1418,7 +1430,7 @@ PQ_API pq_status pq_batch_autotune(pq_batch *b, const uint64_t *x, const uint64_
         if (e != PQ_OK) return e;
         double bt = 1e300;
         for (int r = 0; r <= reps; r++) {
-            e = run_host(P, x, y, scratch.data(), nullptr, false);
+            e = run_host(P, x, y, scratch.data(), nullptr, CERT_NONE);
             if (e != PQ_OK) return e;
             float ms[3];
             e = last_kernel_ms(P, ms);
@@ -1740,14 +1752,24 @@ struct SrvReq {
     double t_submit = 0.0;
     Target *tg = nullptr;
     int64_t bytes = 0;
+    int precise = 0;  // 0 the FP32 walk; 1 chunk-sum tables; 2 FP64 walk (probability re-evaluation)
 };
 struct SrvWave {
     std::vector<SrvReq> reqs;
     std::unique_ptr<Plan> plan;
     int slot = -1;
+    int precise = 0;
     int64_t bytes = 0;
     cudaEvent_t done = nullptr;
 };
+
+// The launch shape of a request at a re-evaluation level.
+static pq_tuning srv_tuning(const pq_tuning &tu, int precise) {
+    pq_tuning t = tu;
+    if (precise == 1) t.chunk_tables = 1;
+    if (precise == 2) t.chunk_tables = 2;
+    return t;
+}
 
 // Device bytes of one request's launch state (jobs, item partials, outputs).
 static int64_t request_bytes(const Target &T, const pq_tuning &tu) {
@@ -1839,12 +1861,12 @@ static pq_status srv_launch(pq_server *S, SrvWave &w, const pq_tuning &tu) {
     }
     cudaStream_t st = S->streams[w.slot];
     w.plan = std::make_unique<Plan>();
-    pq_status ps = build_plan(segs, 2, st, tu, *w.plan, true);
+    pq_status ps = build_plan(segs, 2, st, srv_tuning(tu, w.precise), *w.plan, true);
     if (ps != PQ_OK) return ps;
     Plan &P = *w.plan;
     CU(cudaMemcpyAsync(P.x.p, xs.data(), xs.size() * 8, cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(P.y.p, ys.data(), ys.size() * 8, cudaMemcpyHostToDevice, st));
-    CU(enqueue_core(P, 0));
+    CU(enqueue_core(P, w.precise == 2 ? 1 : 0));
     double *hb = S->hbuf[w.slot];
     CU(cudaMemcpyAsync(hb, P.out.p, (size_t)n * 16, cudaMemcpyDeviceToHost, st));
     CU(cudaMemcpyAsync(hb + 2 * S->max_slots, P.err.p, (size_t)n * 8, cudaMemcpyDeviceToHost, st));
@@ -1872,6 +1894,22 @@ static void srv_loop(pq_server *S) {
                 const SrvReq &rq = w->reqs[k];
                 pq_result r = srv_result(rq, q == cudaSuccess ? PQ_OK : PQ_ERR_DEVICE, t);
                 const double re = hb[2 * k], im = hb[2 * k + 1], eb = hb[2 * S->max_slots + k];
+                if (q == cudaSuccess && rq.r.kind != PQ_REQ_AMPLITUDE && rq.precise < 2) {
+                    // probabilities (and marginals) are promised to 1e-12 absolute: when the
+                    // bound cannot show it, the request is re-evaluated at the next level
+                    const double pb = rq.r.kind == PQ_REQ_PROBABILITY
+                                          ? eb * (2.0 * std::sqrt(re * re + im * im) + eb)
+                                          : eb;
+                    if (pb > 1e-12) {
+                        SrvReq again = rq;
+                        // level 1 only where it differs from level 0: some engine of the target
+                        // has chunk-sum tables and the wave did not use them already
+                        const bool tables = w->plan && w->plan->any_ctab && !w->plan->args.use_ctab;
+                        again.precise = rq.precise == 0 && !tables ? 2 : rq.precise + 1;
+                        S->pending.push_front(again);
+                        continue;
+                    }
+                }
                 if (rq.r.kind == PQ_REQ_AMPLITUDE) {
                     r.re = re;
                     r.im = im;
@@ -1921,8 +1959,9 @@ static void srv_loop(pq_server *S) {
             std::vector<pq_result> refused;
             auto w = std::make_unique<SrvWave>();
             std::vector<SrvReq> back;
+            w->precise = cand.empty() ? 0 : cand.front().precise;
             for (auto &q : cand) {
-                if (!back.empty()) {
+                if (!back.empty() || q.precise != w->precise) {  // one re-evaluation level per wave
                     back.push_back(q);
                     continue;
                 }
@@ -1932,7 +1971,7 @@ static void srv_loop(pq_server *S) {
                     continue;
                 }
                 // work of the request: branches over all of its branch engines
-                q.bytes = request_bytes(*q.tg, tu);
+                q.bytes = request_bytes(*q.tg, srv_tuning(tu, q.precise));
                 if (q.tg->branches_per_amp > std::ldexp(1.0, S->max_d) || q.bytes > S->budget) {
                     refused.push_back(srv_result(q, PQ_ERR_ADMISSION_REFUSED, srv_now(S)));
                     continue;

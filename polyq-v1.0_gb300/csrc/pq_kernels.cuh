@@ -58,6 +58,7 @@ struct KArgs {
     uint8_t *lpx;               // optional: Lp of every coordinate, lpx_stride bytes per job (any d)
     int lpx_stride;
     int use_ctab;               // chunk sums from the engines' chunk-sum tables where they apply
+    int fp64_mode;              // the enumeration ran with FP64 weights (error bound of that path)
 };
 
 __device__ __forceinline__ int warp_sum_i(int v) {
@@ -664,14 +665,14 @@ __global__ void job_reduce_kernel(KArgs a) {
             // FP64 chunk-sum table (a DI-stage transform of FP64 products) and FP64 sums of at
             // most 2^(d - DI) chunk values per job, item partials and the warp reduction
             rel = ((double)E.DI + 2.0 * (double)(1ull << (E.d - E.DI)) + 64.0) * 2.0 * u64;
-        } else if (E.joint) {
+        } else if (E.joint && !a.fp64_mode) {
             const double g = n * u32 / (1.0 - n * u32);
             rel = g * g + 2.0 * n * u32 * u32 + 1.5e-14 + 64.0 * u64;
         } else {
             rel = (n + 2.0 * E.nsl_tp + 8.0 + (double)E.nsl_th) * 2.0 * u64;
         }
         eb = rel * E.sum_abs_bound * mag;
-        if (E.joint && !ctab) eb += E.errfac * mag;  // lo-part sums of the walk (exact hi sums)
+        if (E.joint && !ctab && !a.fp64_mode) eb += E.errfac * mag;  // lo-part sums of the walk
     }
     a.job_vals[j] = v;
     a.job_err[j] = eb;

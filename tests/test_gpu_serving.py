@@ -39,9 +39,8 @@ def _expected(sims, r):
     s = sims[r["sim"]]
     if r["kind"] == AMPLITUDE:
         return complex(s.amplitudes([0], [r["y"]])[0])
-    if r["kind"] == PROBABILITY:
-        a = complex(s.amplitudes([0], [r["y"]])[0])
-        return a.real * a.real + a.imag * a.imag
+    if r["kind"] == PROBABILITY:  # same re-evaluation rule as the server (1e-12 certification)
+        return float(s.probabilities([0], [r["y"]])[0])
     return s.marginal(0, [(r["qubit"], r["outcome"])])
 
 
@@ -153,3 +152,28 @@ def test_overlapping_arrivals_are_admitted_while_waves_run(pool):
     lat = sorted(r["done_s"] - r["submit_s"] for r in res)
     assert lat[len(lat) // 2] < 10.0
     srv.close()
+
+
+def test_served_probabilities_within_1e12_absolute(gpu):
+    # 8 qubits, 40 T, one cached engine of d = 20-22: amplitudes of order 2^-4, where the FP32
+    # bound cannot show 1e-12 on |a|^2; the server re-evaluates those requests (chunk-sum
+    # tables, then the FP64 walk) in later waves, mixed with amplitude requests of the same
+    # circuit that stay at the FP32 level
+    from polyq_gb300.rng import workload_circuit
+    c = workload_circuit(8, 240, 40, 5)
+    s = Simulator(c, "cached")
+    want = np.abs(O.dense_statevector(c, 0)) ** 2
+    srv = Server([s], max_slots=32, mem_budget_bytes=1 << 28, max_branch_dim=40)
+    reqs = []
+    for y in range(256):
+        reqs.append({"sim": 0, "kind": PROBABILITY, "x": 0, "y": y, "tag": y})
+        if y % 8 == 0:
+            reqs.append({"sim": 0, "kind": AMPLITUDE, "x": 0, "y": y, "tag": 1000 + y})
+    srv.submit(reqs)
+    res = {r["tag"]: r for r in srv.collect(len(reqs), 300)}
+    srv.close()
+    p = np.array([res[y]["re"] for y in range(256)])
+    assert all(res[y]["status"] == 0 and res[y]["errbound"] <= 1e-12 for y in range(256))
+    assert np.max(np.abs(p - want)) <= 1e-12
+    amps = s.amplitudes([0] * 32, list(range(0, 256, 8)))
+    assert np.array_equal(np.array([complex(res[1000 + y]["re"], res[1000 + y]["im"]) for y in range(0, 256, 8)]), amps)
