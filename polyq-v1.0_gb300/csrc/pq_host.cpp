@@ -234,78 +234,188 @@ void PathSum::trace_closure() {  // pathsum.rs:399-425
 // Symmetric LDL^T over F2 with the MinWeight pivot rule: the lightest alive row with a
 // diagonal bit is a 1x1 pivot; otherwise the lightest row with an off-diagonal bit is a
 // 2x2 pivot with its lowest alive neighbour.  Ties break on the row index.
+// Rows are kept with the span of words that may hold set bits, so that the row operations
+// of a step cost the span of the vectors involved, not the full width m/64 (the quadratic
+// forms of circuits are local: a variable meets few others, and those were created near it).
+// The pivot queues are binary heaps with lazy deletion; a popped entry is used only if it
+// still equals its variable's current key, so the choice is the minimum (weight, index)
+// exactly as with an ordered set.
+namespace {
+struct SpanRows {
+    int W = 0;
+    std::vector<uint64_t> w;
+    std::vector<int> lo, hi;  // [lo, hi) words that may be nonzero
+    SpanRows(int m, int words) : W(words), w((size_t)m * words, 0ull), lo((size_t)m, 0), hi((size_t)m, 0) {}
+    uint64_t* row(int i) { return &w[(size_t)i * W]; }
+    const uint64_t* row(int i) const { return &w[(size_t)i * W]; }
+    void set(int i, int bit) {
+        row(i)[bit >> 6] |= 1ull << (bit & 63);
+        widen(i, bit >> 6, (bit >> 6) + 1);
+    }
+    void widen(int i, int a, int b) {
+        if (lo[i] == hi[i]) { lo[i] = a; hi[i] = b; return; }
+        lo[i] = std::min(lo[i], a);
+        hi[i] = std::max(hi[i], b);
+    }
+    void xor_in(int i, const uint64_t* v, int a, int b) {
+        if (a >= b) return;
+        uint64_t* r = row(i);
+        for (int k = a; k < b; k++) r[k] ^= v[k];
+        widen(i, a, b);
+    }
+    Bits bits(int i, int len) const {
+        Bits o(len);
+        std::copy(row(i) + lo[i], row(i) + hi[i], o.w.begin() + lo[i]);
+        return o;
+    }
+};
+// A scratch vector with its word span; cleared over that span.
+struct SpanVec {
+    std::vector<uint64_t> w;
+    int lo = 0, hi = 0;
+    explicit SpanVec(int words) : w((size_t)words, 0ull) {}
+    void clear() {
+        for (int k = lo; k < hi; k++) w[k] = 0;
+        lo = hi = 0;
+    }
+    void trim() {
+        while (lo < hi && w[lo] == 0) lo++;
+        while (hi > lo && w[hi - 1] == 0) hi--;
+    }
+    bool get(int i) const { return (w[(size_t)i >> 6] >> (i & 63)) & 1ull; }
+    void unset(int i) { w[(size_t)i >> 6] &= ~(1ull << (i & 63)); }
+    template <class F> void for_each_one(F&& f) const {
+        for (int k = lo; k < hi; k++) {
+            uint64_t x = w[k];
+            while (x) { f(k * 64 + __builtin_ctzll(x)); x &= x - 1; }
+        }
+    }
+};
+}  // namespace
+
 Structure eliminate(const std::vector<Bits>& bmat, const Bits& parity) {
     const int m = (int)bmat.size();
-    std::vector<Bits> gram(bmat);
-    std::vector<Bits> basis((size_t)m, Bits(m));
-    for (int i = 0; i < m; i++) { gram[i].set(i, parity.get(i)); basis[i].set(i, true); }
-    Bits alive(m);
-    for (int i = 0; i < m; i++) alive.set(i, true);
+    const int W = std::max(1, (m + 63) / 64);
+    SpanRows gram(m, W), basis(m, W);
+    for (int i = 0; i < m; i++) {
+        bmat[i].for_each_one([&](int j) { gram.set(i, j); });
+        if (parity.get(i)) gram.set(i, i);
+        basis.set(i, i);
+    }
+    std::vector<uint64_t> alive((size_t)W, 0ull);
+    for (int i = 0; i < m; i++) alive[(size_t)i >> 6] |= 1ull << (i & 63);
+    auto is_alive = [&](int i) { return (alive[(size_t)i >> 6] >> (i & 63)) & 1ull; };
     Structure st;
     st.m = m;
     // key[a] = (class, weight): class 1 = diagonal set, 2 = off-diagonal only, 0 = neither
     std::vector<std::pair<uint8_t, uint32_t>> key((size_t)m, {0, 0});
-    std::set<std::pair<uint32_t, int>> dset, oset;
+    using Entry = std::pair<uint32_t, int>;
+    std::vector<Entry> dheap, oheap;
+    auto push = [](std::vector<Entry>& h, Entry e) {
+        h.push_back(e);
+        std::push_heap(h.begin(), h.end(), std::greater<Entry>());
+    };
+    auto top = [&](std::vector<Entry>& h, uint8_t cls) -> int {
+        while (!h.empty()) {
+            const Entry e = h.front();
+            if (key[e.second].first == cls && key[e.second].second == e.first) return e.second;
+            std::pop_heap(h.begin(), h.end(), std::greater<Entry>());
+            h.pop_back();
+        }
+        return -1;
+    };
     auto reclass = [&](int a) {
-        if (key[a].first == 1) dset.erase({key[a].second, a});
-        else if (key[a].first == 2) oset.erase({key[a].second, a});
-        if (!alive.get(a)) { key[a] = {0, 0}; return; }
-        uint32_t w = gram[a].and_count(alive);
-        if (gram[a].get(a)) { key[a] = {1, w}; dset.insert({w, a}); }
-        else if (w > 0) { key[a] = {2, w}; oset.insert({w, a}); }
-        else key[a] = {0, 0};
+        std::pair<uint8_t, uint32_t> k{0, 0};
+        if (is_alive(a)) {
+            const uint64_t* r = gram.row(a);
+            uint32_t w = 0;
+            for (int q = gram.lo[a]; q < gram.hi[a]; q++) w += (uint32_t)__builtin_popcountll(r[q] & alive[q]);
+            if ((r[a >> 6] >> (a & 63)) & 1ull) k = {1, w};
+            else if (w > 0) k = {2, w};
+        }
+        if (k == key[a]) return;
+        key[a] = k;
+        if (k.first == 1) push(dheap, {k.second, a});
+        else if (k.first == 2) push(oheap, {k.second, a});
     };
     for (int a = 0; a < m; a++) reclass(a);
+    SpanVec s(W), sb(W), touched(W);
+    auto masked = [&](SpanVec& v, int r) {  // v = gram[r] & alive
+        const uint64_t* g = gram.row(r);
+        v.lo = gram.lo[r];
+        v.hi = gram.hi[r];
+        for (int q = v.lo; q < v.hi; q++) v.w[q] = g[q] & alive[q];
+    };
+    auto kill = [&](int a) { alive[(size_t)a >> 6] &= ~(1ull << (a & 63)); };
     while (true) {
-        if (!dset.empty()) {  // single_step (normal_form.rs:61-82)
-            int a = dset.begin()->second;
-            Bits s = gram[a];
-            s.and_with(alive);
-            s.set(a, false);
-            const Bits pa = basis[a];
-            s.for_each_one([&](int bi) { gram[bi].xor_with(s); basis[bi].xor_with(pa); });
-            alive.set(a, false);
+        int a = top(dheap, 1);
+        if (a >= 0) {  // single_step (normal_form.rs:61-82)
+            masked(s, a);
+            s.unset(a);
+            s.trim();
+            const Bits pa = basis.bits(a, m);
+            const int plo = basis.lo[a], phi = basis.hi[a];
+            s.for_each_one([&](int bi) {
+                gram.xor_in(bi, s.w.data(), s.lo, s.hi);
+                basis.xor_in(bi, pa.w.data(), plo, phi);
+            });
+            kill(a);
             st.odd.push_back(pa);
             reclass(a);
             s.for_each_one([&](int bi) { reclass(bi); });
+            s.clear();
             continue;
         }
-        if (!oset.empty()) {  // hyper_step (normal_form.rs:87-129)
-            int a = oset.begin()->second;
-            Bits sa = gram[a];
-            sa.and_with(alive);
-            int b = sa.first_one();
-            sa.set(b, false);
-            Bits sb = gram[b];
-            sb.and_with(alive);
-            sb.set(a, false);
-            const Bits pa = basis[a], pb = basis[b];
-            Bits touched = sa;
-            for (int i = 0; i < touched.nw(); i++) touched.w[i] |= sb.w[i];
+        a = top(oheap, 2);
+        if (a >= 0) {  // hyper_step (normal_form.rs:87-129)
+            masked(s, a);
+            s.trim();
+            int b = -1;
+            for (int q = s.lo; q < s.hi && b < 0; q++)
+                if (s.w[q]) b = q * 64 + __builtin_ctzll(s.w[q]);
+            s.unset(b);
+            s.trim();
+            masked(sb, b);
+            sb.unset(a);
+            sb.trim();
+            const Bits pa = basis.bits(a, m), pb = basis.bits(b, m);
+            const int alo = basis.lo[a], ahi = basis.hi[a], blo = basis.lo[b], bhi = basis.hi[b];
+            touched.lo = std::min(s.lo < s.hi ? s.lo : W, sb.lo < sb.hi ? sb.lo : W);
+            touched.hi = std::max(s.hi, sb.hi);
+            if (touched.lo > touched.hi) touched.lo = touched.hi;
+            for (int q = touched.lo; q < touched.hi; q++) touched.w[q] = s.w[q] | sb.w[q];
             touched.for_each_one([&](int k) {
-                if (sa.get(k)) { gram[k].xor_with(sb); basis[k].xor_with(pb); }
-                if (sb.get(k)) { gram[k].xor_with(sa); basis[k].xor_with(pa); }
+                if (s.get(k)) { gram.xor_in(k, sb.w.data(), sb.lo, sb.hi); basis.xor_in(k, pb.w.data(), blo, bhi); }
+                if (sb.get(k)) { gram.xor_in(k, s.w.data(), s.lo, s.hi); basis.xor_in(k, pa.w.data(), alo, ahi); }
             });
-            alive.set(a, false);
-            alive.set(b, false);
+            kill(a);
+            kill(b);
             st.pa.push_back(pa);
             st.pb.push_back(pb);
             reclass(a);
             reclass(b);
             touched.for_each_one([&](int k) { reclass(k); });
+            s.clear();
+            sb.clear();
+            touched.clear();
             continue;
         }
         break;
     }
-    alive.for_each_one([&](int r) { st.even.push_back(basis[r]); });
+    for (int r = 0; r < m; r++)
+        if (is_alive(r)) st.even.push_back(basis.bits(r, m));
     return st;
 }
 
-// z4 value of a basis vector (normal_form.rs:339-348)
-static unsigned z4_value(const std::vector<Bits>& b, const Bits& v0, const Bits& v1, const Bits& p) {
+// z4 value of a basis vector (normal_form.rs:339-348).  The bilinear part p^T B p (B symmetric,
+// zero diagonal, a few entries per row) is summed over B's adjacency lists: O(|p| deg) bit
+// tests instead of |p| row-wide popcounts.
+static unsigned z4_value(const std::vector<std::vector<int>>& adj, const Bits& v0, const Bits& v1, const Bits& p) {
     unsigned lin = p.and_count(v0) + 2 * p.and_count(v1);
     unsigned t = 0;
-    p.for_each_one([&](int j) { t += b[j].and_count(p); });
+    p.for_each_one([&](int j) {
+        for (int k : adj[(size_t)j]) t += p.get(k) ? 1u : 0u;
+    });
     return (lin + 2 * ((t / 2) & 1)) & 3u;
 }
 
@@ -445,18 +555,20 @@ std::unique_ptr<HostEngine> build_engine(const PathSum& ps, const std::vector<in
     // Z4 diagonal (normal_form.rs:354-391)
     Bits v0(m), v1(m);
     for (int i = 0; i < m; i++) { uint8_t x = ps.v[E->freev[i]]; v0.set(i, x & 1); v1.set(i, (x & 2) != 0); }
+    std::vector<std::vector<int>> adj((size_t)m);
+    for (int i = 0; i < m; i++) adj[(size_t)i] = bff[(size_t)i].ones();
     Diag& dg = E->dg;
     dg.wa = Bits(Lo.g); dg.wb = Bits(Lo.g); dg.o1 = Bits(Lo.nodd); dg.o3 = Bits(Lo.nodd); dg.we = Bits(Lo.neven);
     for (int j = 0; j < Lo.g; j++) {
-        dg.wa.set(j, z4_value(bff, v0, v1, st.pa[j]) == 2);
-        dg.wb.set(j, z4_value(bff, v0, v1, st.pb[j]) == 2);
+        dg.wa.set(j, z4_value(adj, v0, v1, st.pa[j]) == 2);
+        dg.wb.set(j, z4_value(adj, v0, v1, st.pb[j]) == 2);
     }
     dg.sigma = 0;
     for (int l = 0; l < Lo.nodd; l++) {
-        if (z4_value(bff, v0, v1, st.odd[l]) == 1) { dg.o1.set(l, true); dg.sigma++; }
+        if (z4_value(adj, v0, v1, st.odd[l]) == 1) { dg.o1.set(l, true); dg.sigma++; }
         else { dg.o3.set(l, true); dg.sigma--; }
     }
-    for (int l = 0; l < Lo.neven; l++) dg.we.set(l, z4_value(bff, v0, v1, st.even[l]) == 2);
+    for (int l = 0; l < Lo.neven; l++) dg.we.set(l, z4_value(adj, v0, v1, st.even[l]) == 2);
     E->sigma = dg.sigma;
     E->mag2 = 2 * Lo.g + 2 * Lo.neven + Lo.nodd;
     // terms (engine.rs:232-238), FP64

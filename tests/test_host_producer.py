@@ -108,3 +108,12 @@ def test_host_only_simulator_refuses_evaluation():
     with pytest.raises(N.PqError) as e:
         s.amplitudes([0], [3])
     assert e.value.status == 7
+
+
+def test_large_engines_bit_exact():
+    # thousands of free variables (the elimination's row spans and pivot heaps at scale)
+    from polyq_gb300.rng import workload_circuit
+    st = _same_engines(workload_circuit(100, 6000, 30, 1), "cached")
+    assert st["free_vars"] > 5000
+    _same_engines(workload_circuit(100, 10000, 40, 1), "cached")
+    _same_engines(workload_circuit(80, 4000, 24, 2), pairs=2)
