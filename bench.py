@@ -563,6 +563,8 @@ def run_serve(args):
         return {"offered_per_s": rate, "requests": nreq, "completed": len(ok),
                 "refused": sum(1 for r in res if r["status"] == 3), "other_errors": sum(1 for r in res if r["status"] not in (0, 3)),
                 "throughput_per_s": len(ok) / span if span > 0 else None,
+                "evaluated_at_level": {name: sum(1 for r in ok if r["level"] == lv)
+                                       for lv, name in enumerate(("fp32_walk", "chunk_tables", "fp64_walk"))},
                 "p50_ms": 1e3 * _pct(lat, 0.5) if lat else None,
                 "p99_ms": 1e3 * _pct(lat, 0.99) if lat else None}, [q for q in reqs if q["tag"] in okt]
 

@@ -181,6 +181,10 @@ typedef struct pq_result {
     double re, im;        /* amplitude, or probability in re */
     double errbound;
     double submit_s, done_s;  /* seconds on the server's monotonic clock */
+    int32_t level;        /* evaluation that produced it: 0 the FP32 walk, 1 chunk-sum tables,
+                             2 the FP64 walk (probabilities and marginals whose bound could not
+                             show 1e-12 absolute are re-evaluated at the next level) */
+    int32_t reserved;
 } pq_result;
 /* max_slots: requests per launched wave; mem_budget_bytes: device memory the in-flight waves
  * may hold; max_branch_dim: a request whose work -- branches summed over its branch engines --

@@ -187,7 +187,9 @@ struct Plan {
     int smem_words = 8;
     int grid_prep = 1, grid_enum = 1, block_enum = 256;
     int minb = 3;  // enum_kernel<0, minb> instantiation (blocks per SM its registers allow)
-    bool any_ctab = false;  // some job can take its chunk sums from a chunk-sum table
+    bool any_ctab = false;   // some job can take its chunk sums from a chunk-sum table
+    bool fp32_any = false;   // some job walks in FP32 (joint table) without tables
+    bool fp32_rest = false;  // some job walks in FP32 even with tables (none for its engine)
     uint64_t last_use = 0;  // recency in the owning simulator's plan cache
     bool graph_ready = false;
     cudaStream_t stream = nullptr;
@@ -316,7 +318,10 @@ static pq_status build_plan(const std::vector<Segment> &segs, int nw, cudaStream
         }
         istart[k + 1] = istart[k] + (long long)((jnch[j] + jcpi[j] - 1) / jcpi[j]);
         P.branches += std::ldexp(1.0, E.d);
-        if (E.ctab && (jdl[j] & 255) == E.DI) P.any_ctab = true;
+        const bool covered = E.ctab && (jdl[j] & 255) == E.DI;
+        P.any_ctab = P.any_ctab || covered;
+        P.fp32_any = P.fp32_any || E.joint;
+        P.fp32_rest = P.fp32_rest || (E.joint && !covered);
     }
     P.nitems = istart[P.njobs];
     CU(upload(P.engines, eng));
@@ -395,8 +400,9 @@ static pq_status build_plan(const std::vector<Segment> &segs, int nw, cudaStream
     return PQ_OK;
 }
 
-// Enqueue the core launch sequence on P.stream (capturable).
-static cudaError_t enqueue_core(Plan &P, int mode) {
+// Enqueue the core launch sequence on P.stream (capturable).  mode 1 walks in FP64; ctab >= 0
+// overrides the plan's use of chunk-sum tables (which, where they apply, are FP64 in either mode).
+static cudaError_t enqueue_core(Plan &P, int mode, int ctab = -1) {
     cudaError_t e;
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     if ((e = cudaStreamIsCapturing(P.stream, &cs)) != cudaSuccess) return e;
@@ -408,6 +414,7 @@ static cudaError_t enqueue_core(Plan &P, int mode) {
     if (e != cudaSuccess) return e;
     KArgs args = P.args;
     args.fp64_mode = mode == 1 ? 1 : 0;
+    if (ctab >= 0) args.use_ctab = ctab;
     if ((e = cudaEventRecordWithFlags(P.tev[0], P.stream, evflag)) != cudaSuccess) return e;
     prepare_kernel<<<P.grid_prep, 128, (size_t)4 * P.smem_words * 8, P.stream>>>(args);
     if ((e = cudaEventRecordWithFlags(P.tev[1], P.stream, evflag)) != cudaSuccess) return e;
@@ -474,23 +481,24 @@ static pq_status run_host(Plan &P, const uint64_t *x, const uint64_t *y, double 
         return false;
     };
     auto rerun = [&](int mode, int ctab) -> pq_status {
-        const int saved = P.args.use_ctab;
-        P.args.use_ctab = ctab;
-        cudaError_t e = enqueue_core(P, mode);
-        P.args.use_ctab = saved;
-        CU(e);
+        CU(enqueue_core(P, mode, ctab));
         CU(cudaMemcpyAsync(P.hout.p, P.out.p, (size_t)P.nout * 16, cudaMemcpyDeviceToHost, P.stream));
         CU(cudaMemcpyAsync(P.herr.p, P.err.p, (size_t)P.nout * 8, cudaMemcpyDeviceToHost, P.stream));
         CU(cudaStreamSynchronize(P.stream));
         return PQ_OK;
     };
     if (cert != CERT_NONE && uncertified()) {
-        if (P.any_ctab && !P.args.use_ctab) {
+        bool tables = P.args.use_ctab != 0;
+        if (P.any_ctab && !tables) {
             st = rerun(0, 1);
             if (st != PQ_OK) return st;
+            tables = true;
         }
-        if (uncertified()) {
-            st = rerun(1, 0);
+        // then the FP64 walk for the jobs that walked in FP32 (the tables stay where they
+        // apply; jobs without a joint table already used FP64 weights, so a rerun would repeat
+        // them)
+        if (uncertified() && (tables ? P.fp32_rest : P.fp32_any)) {
+            st = rerun(1, tables ? 1 : 0);
             if (st != PQ_OK) return st;
         }
     }
@@ -844,7 +852,7 @@ PQ_API pq_status pq_amplitudes_fp64(pq_sim *s, int64_t n, const uint64_t *x, con
     const size_t bw = (size_t)n * s->nw * 8;
     CU(cudaMemcpyAsync(P->x.p, x, bw, cudaMemcpyHostToDevice, P->stream));
     CU(cudaMemcpyAsync(P->y.p, y, bw, cudaMemcpyHostToDevice, P->stream));
-    CU(enqueue_core(*P, 1));
+    CU(enqueue_core(*P, 1, 0));  // the FP64 walk alone (the precision reference)
     CU(cudaMemcpyAsync(out, P->out.p, (size_t)n * 16, cudaMemcpyDeviceToHost, P->stream));
     CU(cudaStreamSynchronize(P->stream));
     return PQ_OK;
@@ -1757,18 +1765,36 @@ struct SrvReq {
 struct SrvWave {
     std::vector<SrvReq> reqs;
     std::unique_ptr<Plan> plan;
+    pq_tuning tu{};  // launch shape of the wave
     int slot = -1;
     int precise = 0;
     int64_t bytes = 0;
     cudaEvent_t done = nullptr;
 };
 
-// The launch shape of a request at a re-evaluation level.
+// The launch shape of a request at a re-evaluation level (1: chunk-sum tables where they apply,
+// the FP32 walk elsewhere; 2: the tables, the FP64 walk elsewhere).
 static pq_tuning srv_tuning(const pq_tuning &tu, int precise) {
     pq_tuning t = tu;
-    if (precise == 1) t.chunk_tables = 1;
-    if (precise == 2) t.chunk_tables = 2;
+    if (precise >= 1) t.chunk_tables = 1;
     return t;
+}
+
+// Which evaluations a target's branch engines take under a launch shape: some sum their chunks
+// from chunk-sum tables (any_ctab), some walk in FP32 without tables (fp32_any), some walk in
+// FP32 even with tables (fp32_rest).  Engines without a joint table use FP64 weights always.
+static void eval_cover(const Target &T, const pq_tuning &tu, bool &any_ctab, bool &fp32_any, bool &fp32_rest) {
+    any_ctab = fp32_any = fp32_rest = false;
+    for (const auto &E : T.dev) {
+        int dl;
+        unsigned long long nch;
+        unsigned cpi;
+        job_shape(E, tu.chunks_per_lane, unit_max_for(E, tu), dl, nch, cpi);
+        const bool covered = E.ctab != nullptr && (dl & 255) == E.DI;
+        any_ctab = any_ctab || covered;
+        fp32_any = fp32_any || E.joint;
+        fp32_rest = fp32_rest || (E.joint && !covered);
+    }
 }
 
 // Device bytes of one request's launch state (jobs, item partials, outputs).
@@ -1820,6 +1846,7 @@ static pq_result srv_result(const SrvReq &q, int32_t status, double t) {
     r.kind = q.r.kind;
     r.submit_s = q.t_submit;
     r.done_s = t;
+    r.level = q.precise;
     return r;
 }
 
@@ -1861,7 +1888,8 @@ static pq_status srv_launch(pq_server *S, SrvWave &w, const pq_tuning &tu) {
     }
     cudaStream_t st = S->streams[w.slot];
     w.plan = std::make_unique<Plan>();
-    pq_status ps = build_plan(segs, 2, st, srv_tuning(tu, w.precise), *w.plan, true);
+    w.tu = srv_tuning(tu, w.precise);
+    pq_status ps = build_plan(segs, 2, st, w.tu, *w.plan, true);
     if (ps != PQ_OK) return ps;
     Plan &P = *w.plan;
     CU(cudaMemcpyAsync(P.x.p, xs.data(), xs.size() * 8, cudaMemcpyHostToDevice, st));
@@ -1896,18 +1924,24 @@ static void srv_loop(pq_server *S) {
                 const double re = hb[2 * k], im = hb[2 * k + 1], eb = hb[2 * S->max_slots + k];
                 if (q == cudaSuccess && rq.r.kind != PQ_REQ_AMPLITUDE && rq.precise < 2) {
                     // probabilities (and marginals) are promised to 1e-12 absolute: when the
-                    // bound cannot show it, the request is re-evaluated at the next level
+                    // bound cannot show it, the request is re-evaluated at the next level that
+                    // can tighten it -- the chunk-sum tables where some engine has them and
+                    // this wave did not use them, else the FP64 walk where some engine walked
+                    // in FP32 (engines without a joint table already used FP64 weights)
                     const double pb = rq.r.kind == PQ_REQ_PROBABILITY
                                           ? eb * (2.0 * std::sqrt(re * re + im * im) + eb)
                                           : eb;
                     if (pb > 1e-12) {
-                        SrvReq again = rq;
-                        // level 1 only where it differs from level 0: some engine of the target
-                        // has chunk-sum tables and the wave did not use them already
-                        const bool tables = w->plan && w->plan->any_ctab && !w->plan->args.use_ctab;
-                        again.precise = rq.precise == 0 && !tables ? 2 : rq.precise + 1;
-                        S->pending.push_front(again);
-                        continue;
+                        bool any_ctab = false, fp32_any = false, fp32_rest = false;
+                        eval_cover(*rq.tg, w->tu, any_ctab, fp32_any, fp32_rest);
+                        const bool used = w->plan && w->plan->args.use_ctab;
+                        const int next = !used && any_ctab ? 1 : ((used ? fp32_rest : fp32_any) ? 2 : -1);
+                        if (next > 0) {
+                            SrvReq again = rq;
+                            again.precise = next;
+                            S->pending.push_front(again);
+                            continue;
+                        }
                     }
                 }
                 if (rq.r.kind == PQ_REQ_AMPLITUDE) {

@@ -405,7 +405,8 @@ __device__ __forceinline__ void walk_unit(const EngineDev &E, const JobDev &J, c
 }
 
 // MODE 0: FP32 weights (exact-grid hi + lo) in the rotating-frame walk.  MODE 1: FP64 weights
-// and accumulation.
+// and accumulation.  In both, jobs with chunk-sum tables take their chunk sums from them when
+// the launch asks for tables (use_ctab).
 // MODE 2: record the Z8 index of every branch into dbg (single-job debug launches).
 // MINB: resident blocks of 256 threads per SM the register allocation is sized for (2: 128,
 // 3: 80, 4: 64 registers per thread) -- chosen per launch by measurement.
@@ -468,7 +469,7 @@ __global__ void __launch_bounds__(256, MINB) enum_kernel(KArgs a) {
             if (cend > nun) cend = nun;
             const uint64_t lomask = (E.DI >= 64) ? ~0ull : ((1ull << E.DI) - 1ull);
             const uint32_t steps = 1u << dl;
-            if (MODE == 0 && a.use_ctab && E.ctab && dl == E.DI && np == 0 && (cpi & (cpi - 1)) == 0) {
+            if (MODE != 2 && a.use_ctab && E.ctab && dl == E.DI && np == 0 && (cpi & (cpi - 1)) == 0) {
                 // Chunk-sum tables: lane l sums the item's chunks base .. base + q - 1 (base =
                 // c0 + l q, q = cpi / 32 a power of two) in Gray order, one FP64 table lookup per
                 // chunk.  A step flips one high coordinate j: the folded index gains
@@ -519,7 +520,7 @@ __global__ void __launch_bounds__(256, MINB) enum_kernel(KArgs a) {
                 unsigned long long ch = un;
                 for (int i = 0; i < np; i++) ch = insert_zero(ch, E.pairc[i] - dl);
                 const uint64_t s1 = (uint64_t)ch << dl;
-                if (MODE == 0 && a.use_ctab && E.ctab && dl == E.DI) {
+                if (MODE != 2 && a.use_ctab && E.ctab && dl == E.DI) {
                     // chunk-sum tables on a plan laid out for the walk (units of several
                     // chunks): each chunk from its own start
                     for (int kc = 0; kc < nk; kc++) {
@@ -655,22 +656,32 @@ __global__ void job_reduce_kernel(KArgs a) {
         //  joint table: weights exact to 2^-46 (hi + lo of an FP64 product); hi chunk sums are
         //  exact, the terms below keep an allowance of gamma_n^2 + 2 n u^2 (gamma_n = n u /
         //  (1 - n u), n = 2^dl) for them; FP64 chunk scaling and reductions a few 2^-52; the lo
-        //  sums add errfac (per engine, from the grid).  FP64 path: (n + 2 nsl_tp + 8) 2^-53.
+        //  sums add errfac (per engine, from the grid).  FP64 path: (n + 2 nsl_tp + 8 + nsl_th)
+        //  2^-52.  Every path adds the FP64 running sums over a lane's chunks and a job's items.
         const double u32 = 5.9604644775390625e-08, u64 = 1.1102230246251565e-16;
         const double n = (double)(1ull << (a.jdl[j] & 255));
         double rel;
         const int dlj = a.jdl[j] & 255;
         const bool ctab = a.use_ctab && E.ctab && dlj == E.DI;
+        // FP64 running sums shared by every path: a lane's chunks (at most nk ceil(cpi / 32)),
+        // the job's items (recursive summation: n terms, n u relative to sum |c|)
+        const unsigned long long cpi = a.jcpi[j];
+        const double lane_chunks = (double)(1 << ((a.jdl[j] >> 8) & 3)) * (double)((cpi + 31) / 32);
+        const double items = (double)(a.istart[k + 1] - a.istart[k]);
+        const double sums = (lane_chunks + items) * 2.0 * u64;
         if (ctab) {
-            // FP64 chunk-sum table (a DI-stage transform of FP64 products) and FP64 sums of at
-            // most 2^(d - DI) chunk values per job, item partials and the warp reduction
-            rel = ((double)E.DI + 2.0 * (double)(1ull << (E.d - E.DI)) + 64.0) * 2.0 * u64;
+            // FP64 throughout, in units of 2u: the table entry (complex products of at most
+            // DI + 13 factors, sqrt(5) u each, then a DI-stage transform), each chunk's
+            // high-coordinate factor (nsl_th products of 8-factor slice products) and its
+            // product with the entry, the 5-level warp reduction, the final scalings
+            rel = (2.0 * (double)E.DI + 16.0 + 10.0 * (double)E.nsl_th + 5.0 + 64.0) * 2.0 * u64;
         } else if (E.joint && !a.fp64_mode) {
             const double g = n * u32 / (1.0 - n * u32);
             rel = g * g + 2.0 * n * u32 * u32 + 1.5e-14 + 64.0 * u64;
         } else {
             rel = (n + 2.0 * E.nsl_tp + 8.0 + (double)E.nsl_th) * 2.0 * u64;
         }
+        rel += sums;
         eb = rel * E.sum_abs_bound * mag;
         if (E.joint && !ctab && !a.fp64_mode) eb += E.errfac * mag;  // lo-part sums of the walk
     }

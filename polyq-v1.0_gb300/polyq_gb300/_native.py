@@ -51,7 +51,8 @@ class Request(ct.Structure):
 
 class Result(ct.Structure):
     _fields_ = [("tag", ct.c_int64), ("status", ct.c_int32), ("kind", ct.c_int32), ("re", ct.c_double),
-                ("im", ct.c_double), ("errbound", ct.c_double), ("submit_s", ct.c_double), ("done_s", ct.c_double)]
+                ("im", ct.c_double), ("errbound", ct.c_double), ("submit_s", ct.c_double), ("done_s", ct.c_double),
+                ("level", ct.c_int32), ("reserved", ct.c_int32)]
 
 
 # name -> (restype, argtypes)

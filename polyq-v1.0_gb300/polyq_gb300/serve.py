@@ -48,7 +48,7 @@ class Server:
         for i in range(k):
             r = buf[i]
             out.append({"tag": r.tag, "status": r.status, "kind": r.kind, "re": r.re, "im": r.im,
-                        "errbound": r.errbound, "submit_s": r.submit_s, "done_s": r.done_s})
+                        "errbound": r.errbound, "submit_s": r.submit_s, "done_s": r.done_s, "level": r.level})
         return out
 
     def drain(self, timeout_s=60.0):
