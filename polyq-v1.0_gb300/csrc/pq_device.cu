@@ -143,10 +143,22 @@ static pq_status upload_target(Target &T, int di_max) {
         EngineTables tb = build_tables(pe, di_max);
         PackedEngine pk = pack_engine(pe, tb);
         for (int j = 0; j < 16; j++) pk.off.cperm[j] = (uint8_t)(j < tb.DI ? perm[(size_t)j] : j);
+        // the weight table sits at an address aligned to its size (a power of two), so that the
+        // walk forms entry addresses by XOR with the flipped coordinates' byte strides
+        const size_t woff = (size_t)pk.off.wtab;
+        const size_t wbytes = pk.off.wtab ? ((size_t)16 << (tb.DI + pe.rank)) : 0;
         auto m = std::make_unique<DevMem>();
-        CU(m->alloc(pk.blob.size()));
-        CU(cudaMemcpy(m->p, pk.blob.data(), pk.blob.size(), cudaMemcpyHostToDevice));
-        T.dev.push_back(rebase_engine(pk.off, reinterpret_cast<const uint8_t *>(m->p)));
+        CU(m->alloc(pk.blob.size() + (wbytes > 16 ? wbytes : 0)));
+        size_t shift = 0;
+        if (wbytes > 16) {
+            const size_t at = ((uintptr_t)m->p + woff) & (wbytes - 1);
+            shift = at ? wbytes - at : 0;
+        }
+        uint8_t *base = reinterpret_cast<uint8_t *>(m->p) + shift;
+        CU(cudaMemcpy(base, pk.blob.data(), pk.blob.size(), cudaMemcpyHostToDevice));
+        T.dev.push_back(rebase_engine(pk.off, base));
+        if (wbytes && ((uintptr_t)T.dev.back().wtab & (wbytes - 1)) != 0)
+            return fail(PQ_ERR_INTERNAL, "weight table not aligned to its size");
         T.bytes += (int64_t)m->n;
         T.mem.push_back(std::move(m));
         T.branches_per_amp += std::ldexp(1.0, e->d);

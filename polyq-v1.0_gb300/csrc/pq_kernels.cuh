@@ -178,9 +178,10 @@ __device__ __forceinline__ uint32_t quad_parity(const uint64_t *G, uint64_t x) {
 // Unrolled by 8: coordinates 0 and 1 flip at fixed positions with fixed directions (0+, 1+, 0-,
 // 0+, 1-, 0-), coordinate 2 once per group with the group's direction, and the group boundary
 // flips coordinate 3 + ctz(g+1) (its parity is warp-uniform: a uniform branch).
-//   sidx   (pivot bits << DI) | low DI coordinates: the table index
+//   sidx   (pivot bits << DI) | low DI coordinates: the table index; the table is aligned to
+//          its size, so the walk keeps the entry's address and XORs byte strides into it
 //   Pc[k]  bit j = c_j of chunk k for the walked coordinates
-//   T_j    (1 << j) | (R_j << DI): the change of sidx when coordinate j flips
+//   T_j    ((1 << j) | (R_j << DI)) * 16: the change of the entry's address when coordinate j flips
 // On return acc[k] = (hi.re, hi.im, lo.re, lo.im) of chunk k's A at the last branch, whose
 // folded index is m[k] + L'_{dl-1} (the walk ends on the unit vector of coordinate dl-1).
 // Accumulators and table entries travel as pairs of FP32 in one 64-bit register, (re, im): an
@@ -192,11 +193,6 @@ __device__ __forceinline__ uint64_t pk2(float a, float b) {
     return r;
 }
 __device__ __forceinline__ void up2(uint64_t p, float &a, float &b) { asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(p)); }
-__device__ __forceinline__ float lo2(uint64_t p) {
-    float a, b;
-    up2(p, a, b);
-    return a;
-}
 __device__ __forceinline__ uint64_t ffma2(uint64_t a, uint64_t b, uint64_t c) {
     uint64_t d;
     asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
@@ -218,7 +214,6 @@ __device__ __forceinline__ void qturn_odd(uint64_t &H, uint64_t &L, float rho, c
     L = pk2(fmaf(rho, li, wz), fmaf(-rho, lr, ww));
 }
 
-__device__ __forceinline__ float rho_of(uint32_t L) { return (L & 2u) ? -1.0f : 1.0f; }
 
 template <int MODE, int K, int PAR>
 __device__ __forceinline__ void gray_chunk_rot(const float4 *__restrict__ W4, uint32_t sidx, const uint32_t (&Pc)[K],
@@ -226,19 +221,15 @@ __device__ __forceinline__ void gray_chunk_rot(const float4 *__restrict__ W4, ui
                                                uint8_t *dbg, const uint64_t (&sbase)[K], uint32_t k0,
                                                uint32_t (&m)[K], const uint64_t *G, uint32_t lomask) {
     constexpr int O0 = PAR & 1, O1 = (PAR >> 1) & 1, O2 = (PAR >> 2) & 1;
-    const ulonglong2 *__restrict__ W = reinterpret_cast<const ulonglong2 *>(W4);
+    // the table is aligned to its size: an entry's address is the base OR its byte offset, and
+    // a flip XORs the coordinate's byte stride into it
+    uint64_t wad = reinterpret_cast<uint64_t>(W4) | ((uint64_t)sidx << 4);
     const uint32_t T0 = Tg[0], T1 = Tg[1], T2 = Tg[2];
     const uint32_t Lp0 = Lp[0], Lp1 = Lp[1], Lp2 = Lp[2];
-    uint64_t p0[K], p1[K], p2[K];  // (rho, rho) of coordinates 0..2 per chunk
     uint64_t H[K], L[K];
-    const ulonglong2 w0 = __ldg(&W[sidx]);
+    const ulonglong2 w0 = __ldg(reinterpret_cast<const ulonglong2 *>(wad));
 #pragma unroll
     for (int k = 0; k < K; k++) {
-        const float r0 = rho_of(Lp0 + ((Pc[k] & 1u) << 1)), r1 = rho_of(Lp1 + (Pc[k] & 2u)),
-                    r2 = rho_of(Lp2 + ((Pc[k] >> 1) & 2u));
-        p0[k] = pk2(r0, r0);
-        p1[k] = pk2(r1, r1);
-        p2[k] = pk2(r2, r2);
         H[k] = w0.x;
         L[k] = w0.y;
     }
@@ -247,13 +238,14 @@ __device__ __forceinline__ void gray_chunk_rot(const float4 *__restrict__ W4, ui
     // MODE 2 records the true Z8 index: folded index + 2 q(s_lo) (the sign held by the table)
 #define PQ_REC(k)                                                                                        \
     if (MODE == 2)                                                                                       \
-        dbg[sbase[k] | (sidx & inner)] = (uint8_t)((k0 + 2u * (m[k] + 2u * quad_parity(G, sidx & lomask))) & 7u);
+        dbg[sbase[k] | (((uint32_t)wad >> 4) & inner)] =                                               \
+            (uint8_t)((k0 + 2u * (m[k] + 2u * quad_parity(G, ((uint32_t)wad >> 4) & lomask))) & 7u);
     // flip by T, then A <- quarter-turn(A) + w for every chunk of the unit.  RHO2: the (rho, rho)
     // pair of an even step; RHO: the signed rho of an odd step.
 #define PQ_Q(ODD, T, RHO2, RHO, DM)                                                \
     {                                                                              \
-        sidx ^= (T);                                                               \
-        const ulonglong2 w = __ldg(&W[sidx]);                                      \
+        wad ^= (uint64_t)(T);                                                      \
+        const ulonglong2 w = __ldg(reinterpret_cast<const ulonglong2 *>(wad));     \
         _Pragma("unroll") for (int k = 0; k < K; k++) {                            \
             if (ODD) qturn_odd(H[k], L[k], (RHO), w);                              \
             else qturn_even(H[k], L[k], (RHO2), w);                                \
@@ -268,20 +260,31 @@ __device__ __forceinline__ void gray_chunk_rot(const float4 *__restrict__ W4, ui
 #define PQ_L0 (Lp0 + ((Pc[k] & 1u) << 1))
 #define PQ_L1 (Lp1 + (Pc[k] & 2u))
 #define PQ_L2 (Lp2 + ((Pc[k] >> 1) & 2u))
+    // rho of coordinates 0..2 per chunk, formed at each use from c_j (bit j of Pc[k]) rather than
+    // held in registers: +-1.0f with sign bit (Lp_j >> 1) ^ c_j, negated on an odd down-flip
+    const uint32_t u0 = (((Lp0 >> 1) & 1u) << 31) | 0x3F800000u, u0n = u0 ^ (O0 ? 0x80000000u : 0u);
+    const uint32_t u1 = (((Lp1 >> 1) & 1u) << 31) | 0x3F800000u, u1n = u1 ^ (O1 ? 0x80000000u : 0u);
+#define PQ_R0 __uint_as_float(((Pc[k] & 1u) << 31) ^ u0)
+#define PQ_R0N __uint_as_float(((Pc[k] & 1u) << 31) ^ u0n)
+#define PQ_R1 __uint_as_float((((Pc[k] >> 1) & 1u) << 31) ^ u1)
+#define PQ_R1N __uint_as_float((((Pc[k] >> 1) & 1u) << 31) ^ u1n)
     for (uint32_t g = 0;; ++g) {
-        PQ_Q(O0, T0, p0[k], lo2(p0[k]), PQ_L0);
-        PQ_Q(O1, T1, p1[k], lo2(p1[k]), PQ_L1);
-        PQ_Q(O0, T0, p0[k], -lo2(p0[k]), 0u - PQ_L0);
+        PQ_Q(O0, T0, pk2(PQ_R0, PQ_R0), PQ_R0, PQ_L0);
+        PQ_Q(O1, T1, pk2(PQ_R1, PQ_R1), PQ_R1, PQ_L1);
+        PQ_Q(O0, T0, pk2(PQ_R0, PQ_R0), PQ_R0N, 0u - PQ_L0);
         {
-            const bool up = (sidx ^ T2) & 4u;
-            PQ_Q(O2, T2, p2[k], up ? lo2(p2[k]) : -lo2(p2[k]), up ? PQ_L2 : 0u - PQ_L2);
+            const bool up = ((uint32_t)wad ^ T2) & 64u;  // coordinate 2's bit after the flip
+            const uint32_t u2 = ((((Lp2 >> 1) ^ (O2 && !up ? 1u : 0u)) & 1u) << 31) | 0x3F800000u;
+#define PQ_R2 __uint_as_float((((Pc[k] >> 2) & 1u) << 31) ^ u2)
+            PQ_Q(O2, T2, pk2(PQ_R2, PQ_R2), PQ_R2, up ? PQ_L2 : 0u - PQ_L2);
+#undef PQ_R2
         }
-        PQ_Q(O0, T0, p0[k], lo2(p0[k]), PQ_L0);
-        PQ_Q(O1, T1, p1[k], -lo2(p1[k]), 0u - PQ_L1);
-        PQ_Q(O0, T0, p0[k], -lo2(p0[k]), 0u - PQ_L0);
+        PQ_Q(O0, T0, pk2(PQ_R0, PQ_R0), PQ_R0, PQ_L0);
+        PQ_Q(O1, T1, pk2(PQ_R1, PQ_R1), PQ_R1N, 0u - PQ_L1);
+        PQ_Q(O0, T0, pk2(PQ_R0, PQ_R0), PQ_R0N, 0u - PQ_L0);
         if (g + 1 == ngroups) break;
         const int j = 3 + ctz32(g + 1);
-        const uint32_t down = (sidx >> j) & 1u;  // bit j is set before a down flip
+        const uint32_t down = ((uint32_t)wad >> (j + 4)) & 1u;  // bit j is set before a down flip
         const uint32_t Lpj = Lp[j];
         // rho = -1 iff bit 1 of L'_j = Lp_j + 2 c_j is set, negated on an odd down-flip: its sign
         // bit is c_j xor a warp-uniform bit, placed at bit 31 of +1.0f
@@ -296,6 +299,10 @@ __device__ __forceinline__ void gray_chunk_rot(const float4 *__restrict__ W4, ui
 #undef PQ_RHO_J
 #undef PQ_DM_J
     }
+#undef PQ_R0
+#undef PQ_R0N
+#undef PQ_R1
+#undef PQ_R1N
 #undef PQ_L0
 #undef PQ_L1
 #undef PQ_L2
@@ -416,7 +423,7 @@ __global__ void __launch_bounds__(256, MINB) enum_kernel(KArgs a) {
     __shared__ uint64_t sR[8][64];
     __shared__ uint8_t sLp[8][64];
     __shared__ uint8_t sLm[8][64];
-    __shared__ uint32_t sTg[8][32];  // (1 << j) | (R_j << DI)
+    __shared__ uint32_t sTg[8][32];  // byte stride of coordinate j in the table: ((1 << j) | (R_j << DI)) * 16
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     uint64_t *G = sG[wib];
     uint64_t *R = sR[wib];
@@ -449,7 +456,7 @@ __global__ void __launch_bounds__(256, MINB) enum_kernel(KArgs a) {
                 R[j] = E.R[j];
                 Lp[j] = J.Lp[j];
                 Lm[j] = (uint8_t)((4u - J.Lp[j]) & 3u);
-                if (j < dlj) Tg[j] = (1u << j) | ((uint32_t)E.R[j] << E.DI);
+                if (j < dlj) Tg[j] = ((1u << j) | ((uint32_t)E.R[j] << E.DI)) << 4;
             }
             __syncwarp();
         }
