@@ -72,6 +72,9 @@ struct EngineDev {
     const float2 *tlo;       // 2^DI
     const float2 *tp;        // nsl_tp x 256
     const double2 *th;       // nsl_th x 256
+    const double2 *thr;      // nsl_th x 256: th with the pair coordinates' factors left out
+    const float4 *pf;        // 2^npairc: the pair coordinates' weight for each pattern of their
+                             // bits, as FP32 pairs (re hi, im hi, re lo, im lo), hi + lo = FP64
     const double2 *tlo64;    // 2^DI   (FP64 path)
     const double2 *tp64;     // nsl_tp x 256
     const float4 *wtab;      // 2^(DI + rank): (hi.re, hi.im, lo.re, lo.im) of tlo[s] * TP(y)
@@ -307,6 +310,17 @@ PQ_HD double2 chunk_high_weight(const EngineDev &E, uint64_t s) {
     c.x = 1.0;
     c.y = 0.0;
     for (int sl = 0; sl < E.nsl_th; sl++) c = cmul_d(c, E.th[sl * 256 + (int)((s >> (E.DI + 8 * sl)) & 255ull)]);
+    return c;
+}
+
+// FP64 weight of the coordinates above DI other than the pair coordinates.
+PQ_HD double2 chunk_rest_weight(const EngineDev &E, uint64_t s) {
+    double2 c;
+    c.x = 1.0;
+    c.y = 0.0;
+    if (E.nsl_th == 0) return c;
+    c = E.thr[(int)((s >> E.DI) & 255ull)];
+    for (int sl = 1; sl < E.nsl_th; sl++) c = cmul_d(c, E.thr[sl * 256 + (int)((s >> (E.DI + 8 * sl)) & 255ull)]);
     return c;
 }
 

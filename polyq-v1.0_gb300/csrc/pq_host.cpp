@@ -821,6 +821,33 @@ PackedEngine pack_engine(const HostEngine& e, const EngineTables& T) {
     if (T.joint)
         for (int j = T.DI; j < e.d && d.npairc < 3; j++)
             if (e.R[(size_t)j] == 0) d.pairc[d.npairc++] = j;
+    // The high-coordinate weight factors as chi(s) = chi_rest(s) P(bits of s at the pair
+    // coordinates): thr is th without the pair coordinates' factors, pf the 2^npairc values of P
+    // split into FP32 hi + lo (the walk combines the chunks of a unit with them in FP32 pairs).
+    {
+        auto xw = [&](int j, int bit) { int kk = e.free_col[(size_t)j]; return bit ? e.beta[kk] : e.alpha[kk]; };
+        auto is_pair = [&](int j) { return j == d.pairc[0] || j == d.pairc[1] || j == d.pairc[2]; };
+        std::vector<Cplx> thr((size_t)T.nsl_th * 256);
+        for (int sl = 0; sl < T.nsl_th; sl++)
+            for (int b = 0; b < 256; b++) {
+                Cplx c{1.0, 0.0};
+                for (int q = 0; q < 8 && T.DI + 8 * sl + q < e.d; q++)
+                    if (!is_pair(T.DI + 8 * sl + q)) c = cmul(c, xw(T.DI + 8 * sl + q, (b >> q) & 1));
+                thr[(size_t)sl * 256 + b] = c;
+            }
+        d.thr = as_off<double2>(k.vec(thr));
+        std::vector<float> pf;
+        for (int pat = 0; pat < (1 << d.npairc); pat++) {
+            Cplx c{1.0, 0.0};
+            for (int i = 0; i < d.npairc; i++) c = cmul(c, xw(d.pairc[i], (pat >> i) & 1));
+            const float hr = (float)c.re, hi = (float)c.im;
+            pf.push_back(hr);
+            pf.push_back(hi);
+            pf.push_back((float)(c.re - (double)hr));
+            pf.push_back((float)(c.im - (double)hi));
+        }
+        d.pf = as_off<float4>(k.vec(pf));
+    }
     // hi.re, hi.im, lo.re, lo.im with hi + lo = the FP64 weight.  hi lies on the grid g, a power
     // of two with 2^DI * max|w| <= 2^23 g: any sum of at most 2^DI hi parts (a chunk) is then an
     // integer multiple of g below 2^24 g, i.e. exact in FP32; lo = w - hi (|lo| <= g/2) carries
@@ -951,6 +978,7 @@ EngineDev rebase_engine(const EngineDev& o, const uint8_t* base) {
     d.fixed_th = shift(o.fixed_th, base); d.pivrow = shift(o.pivrow, base); d.cons = shift(o.cons, base);
     d.pivcol = shift(o.pivcol, base); d.G = shift(o.G, base); d.Gw = shift(o.Gw, base); d.R = shift(o.R, base);
     d.tlo = shift(o.tlo, base); d.tp = shift(o.tp, base); d.th = shift(o.th, base);
+    d.thr = shift(o.thr, base); d.pf = shift(o.pf, base);
     d.tlo64 = shift(o.tlo64, base); d.tp64 = shift(o.tp64, base); d.wtab = shift(o.wtab, base);
     d.ctab = o.ctab ? shift(o.ctab, base) : nullptr;
     return d;

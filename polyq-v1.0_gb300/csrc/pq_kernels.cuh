@@ -143,13 +143,6 @@ __global__ void __launch_bounds__(128) prepare_kernel(KArgs a) {
 }
 
 // ------------------------------------------------------------------------------ enumerate
-// (cos, sin)(m pi/2) from the bits of m: +-1.0f carries the sign in bit 31 ((m & 2) << 30), and
-// exactly one of the two is non-zero (chosen by m & 1).
-__device__ __forceinline__ float2 quarter_turn(uint32_t m) {
-    const uint32_t one = 0x3F800000u | ((m & 2u) << 30);
-    const uint32_t odd = m & 1u;
-    return make_float2(__uint_as_float(odd ? 0u : one), __uint_as_float(odd ? one : 0u));
-}
 
 // Parity of the quadratic part sum_{i<j} G_ij x_i x_j restricted to the bits of x (G symmetric,
 // zero diagonal): every pair is counted twice by sum_{j in x} popc(G_j & x).
@@ -157,6 +150,47 @@ __device__ __forceinline__ uint32_t quad_parity(const uint64_t *G, uint64_t x) {
     uint32_t t = 0;
     for (uint64_t r = x; r; r &= r - 1) t += (uint32_t)popc64(G[ctz64(r)] & x);
     return (t >> 1) & 1u;
+}
+
+// a + b = s + e exactly (two-sum, no ordering of |a|, |b| assumed).
+__device__ __forceinline__ float two_sum_f(float a, float b, float &e) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return s;
+}
+
+// (ur, ui) += P S in FP32 pairs (value = hi + lo): P = (P.x + P.z) + i (P.y + P.w), S = (hx + lx)
+// + i (hy + ly) with hx, hy exact.  The products of the hi parts are exact (FMA residuals), the
+// accumulation of their hi words is exact (two-sums); cross terms with a lo part go into the lo
+// word in FP32 (lo x lo dropped).
+__device__ __forceinline__ void ff_cmul_acc(const float4 &P, float hx, float hy, float lx, float ly, float &urh,
+                                            float &url, float &uih, float &uil) {
+    float e1, e2;
+    {
+        const float a = __fmul_rn(P.x, hx), ae = __fmaf_rn(P.x, hx, -a);
+        const float b = __fmul_rn(P.y, hy), be = __fmaf_rn(P.y, hy, -b);
+        urh = two_sum_f(urh, a, e1);
+        urh = two_sum_f(urh, -b, e2);
+        float t = __fadd_rn(__fsub_rn(ae, be), __fadd_rn(e1, e2));
+        t = __fmaf_rn(P.x, lx, t);
+        t = __fmaf_rn(P.z, hx, t);
+        t = __fmaf_rn(-P.y, ly, t);
+        t = __fmaf_rn(-P.w, hy, t);
+        url = __fadd_rn(url, t);
+    }
+    {
+        const float a = __fmul_rn(P.x, hy), ae = __fmaf_rn(P.x, hy, -a);
+        const float b = __fmul_rn(P.y, hx), be = __fmaf_rn(P.y, hx, -b);
+        uih = two_sum_f(uih, a, e1);
+        uih = two_sum_f(uih, b, e2);
+        float t = __fadd_rn(__fadd_rn(ae, be), __fadd_rn(e1, e2));
+        t = __fmaf_rn(P.x, ly, t);
+        t = __fmaf_rn(P.z, hy, t);
+        t = __fmaf_rn(P.y, lx, t);
+        t = __fmaf_rn(P.w, hx, t);
+        uil = __fadd_rn(uil, t);
+    }
 }
 
 // Gray walk over the 2^dl inner coordinates of K chunks (dl >= 3) in a rotating frame.
@@ -396,19 +430,32 @@ __device__ __forceinline__ void walk_unit(const EngineDev &E, const JobDev &J, c
     }
     float acc[K][4];
     gray_chunk_rot_any<MODE, K>(E.wtab, sidx, Pc, Tg, Lp, dl, acc, dbg, sb, J.k0, mm, G, (uint32_t)lomask);
+    // The unit's chunks differ only in pair coordinates: their high-coordinate weights are
+    // chi_rest(s1) P(pattern), so the unit sum is chi_rest(s1) sum_k P(k | pat) S_k.  The inner
+    // sum runs in FP32 pairs (exact products by FMA, two-sums), the outer product in FP64 once
+    // per unit.
+    constexpr int npk = K == 8 ? 3 : (K == 4 ? 2 : (K == 2 ? 1 : 0));
+    uint32_t pat = 0;  // bits of s1 at the pair coordinates the unit does not vary
+    for (int i = npk; i < E.npairc; i++) pat |= (uint32_t)((s1 >> E.pairc[i]) & 1ull) << i;
+    float urh = 0.f, url = 0.f, uih = 0.f, uil = 0.f;
     const int jl = dl - 1;
 #pragma unroll
     for (int k = 0; k < K; k++) {
-        // S = i^{m_end} A, m_end = m + L'_{dl-1}
-        const float2 r = quarter_turn(chunk_m(k) + (uint32_t)Lp[jl] + (((Pc[k] >> jl) & 1u) << 1));
-        const double ax = (double)acc[k][0] + (double)acc[k][2];
-        const double ay = (double)acc[k][1] + (double)acc[k][3];
-        const double vx = (double)r.x * ax - (double)r.y * ay;
-        const double vy = (double)r.y * ax + (double)r.x * ay;
-        const double2 chi = chunk_high_weight(E, chunk_s(k));
-        accx += vx * chi.x - vy * chi.y;
-        accy += vx * chi.y + vy * chi.x;
+        // S = i^{m_end} A, m_end = m + L'_{dl-1}: an exact quarter turn of the FP32 pairs
+        const uint32_t q = (chunk_m(k) + (uint32_t)Lp[jl] + (((Pc[k] >> jl) & 1u) << 1)) & 3u;
+        float hx = acc[k][0], hy = acc[k][1], lx = acc[k][2], ly = acc[k][3];
+        if (q & 1u) {
+            const float t = hx; hx = -hy; hy = t;
+            const float t2 = lx; lx = -ly; ly = t2;
+        }
+        if (q & 2u) { hx = -hx; hy = -hy; lx = -lx; ly = -ly; }
+        const float4 P = E.pf[(uint32_t)k | pat];
+        ff_cmul_acc(P, hx, hy, lx, ly, urh, url, uih, uil);
     }
+    const double ux = (double)urh + (double)url, uy = (double)uih + (double)uil;
+    const double2 chi = chunk_rest_weight(E, s1);
+    accx += ux * chi.x - uy * chi.y;
+    accy += ux * chi.y + uy * chi.x;
 }
 
 // MODE 0: FP32 weights (exact-grid hi + lo) in the rotating-frame walk.  MODE 1: FP64 weights
@@ -683,14 +730,19 @@ __global__ void job_reduce_kernel(KArgs a) {
             // product with the entry, the 5-level warp reduction, the final scalings
             rel = (2.0 * (double)E.DI + 16.0 + 10.0 * (double)E.nsl_th + 5.0 + 64.0) * 2.0 * u64;
         } else if (E.joint && !a.fp64_mode) {
+            // + 1e-12: the FP32-pair combination of a unit's chunks (at most 8 terms, each with
+            // error a few 2^-48 of its magnitude)
             const double g = n * u32 / (1.0 - n * u32);
-            rel = g * g + 2.0 * n * u32 * u32 + 1.5e-14 + 64.0 * u64;
+            rel = g * g + 2.0 * n * u32 * u32 + 1.5e-14 + 64.0 * u64 + 1e-12;
         } else {
             rel = (n + 2.0 * E.nsl_tp + 8.0 + (double)E.nsl_th) * 2.0 * u64;
         }
         rel += sums;
         eb = rel * E.sum_abs_bound * mag;
-        if (E.joint && !ctab && !a.fp64_mode) eb += E.errfac * mag;  // lo-part sums of the walk
+        // lo-part sums of the walk, and the FP32 rounding of their products with the pair
+        // weights when a unit's chunks are combined (at most 16 u |P| |lo sum| per chunk: 4 / n
+        // of the sums' own bound)
+        if (E.joint && !ctab && !a.fp64_mode) eb += E.errfac * (1.0 + 4.0 / n) * mag;
     }
     a.job_vals[j] = v;
     a.job_err[j] = eb;
