@@ -66,7 +66,8 @@ typedef struct pq_stats {
     int64_t pairs;          /* decomposed T-pairs p */
     int64_t num_branches;   /* 2^p branch engines */
     double branches_per_amplitude;  /* sum over branch engines of 2^d */
-    int64_t device_bytes;   /* HBM held by the simulator's resident structures */
+    int64_t device_bytes;   /* HBM held by the simulator's resident structures (main and
+                               cached marginal engines) */
     double build_seconds;   /* host compile + elimination + upload time */
 } pq_stats;
 

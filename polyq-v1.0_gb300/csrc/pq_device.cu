@@ -124,7 +124,7 @@ template <class T> static cudaError_t upload(DevMem &m, const std::vector<T> &v)
 struct Target {
     RankSet rs;
     IoMapHost iom;
-    std::vector<std::unique_ptr<DevMem>> mem;  // one blob per branch engine
+    std::vector<std::unique_ptr<DevMem>> mem;  // the engines' tables and blobs (one allocation)
     std::vector<EngineDev> dev;                // rebased onto device addresses
     DevMem iom_mem;
     IoMapDev iom_dev{};
@@ -136,36 +136,61 @@ struct Target {
 static pq_status upload_target(Target &T, int di_max) {
     T.bytes = 0;
     T.branches_per_amp = 0.0;
-    for (auto &e : T.rs.branches) {
+    const size_t ne = T.rs.branches.size();
+    std::vector<PackedEngine> pks(ne);
+    for (size_t i = 0; i < ne; i++) {
+        const auto &e = T.rs.branches[i];
         // pack a copy in the device's coordinate order (even-increment low coordinates first)
         std::vector<int> perm;
         const HostEngine pe = device_order(*e, build_tables(*e, di_max).DI, perm);
         EngineTables tb = build_tables(pe, di_max);
-        PackedEngine pk = pack_engine(pe, tb);
-        for (int j = 0; j < 16; j++) pk.off.cperm[j] = (uint8_t)(j < tb.DI ? perm[(size_t)j] : j);
-        // the weight table sits at an address aligned to its size (a power of two), so that the
-        // walk forms entry addresses by XOR with the flipped coordinates' byte strides
-        const size_t woff = (size_t)pk.off.wtab;
-        const size_t wbytes = pk.off.wtab ? ((size_t)16 << (tb.DI + pe.rank)) : 0;
-        auto m = std::make_unique<DevMem>();
-        CU(m->alloc(pk.blob.size() + (wbytes > 16 ? wbytes : 0)));
-        size_t shift = 0;
-        if (wbytes > 16) {
-            const size_t at = ((uintptr_t)m->p + woff) & (wbytes - 1);
-            shift = at ? wbytes - at : 0;
+        pks[i] = pack_engine(pe, tb);
+        for (int j = 0; j < 16; j++) pks[i].off.cperm[j] = (uint8_t)(j < tb.DI ? perm[(size_t)j] : j);
+    }
+    // One allocation per target: the weight tables first, each at an offset aligned to its size
+    // (a power of two; placed largest first, every offset is a sum of larger powers of two), so
+    // that the walk forms entry addresses by XOR with byte strides; then the engine blobs.
+    std::vector<size_t> order(ne), toff(ne, 0), doff(ne, 0);
+    for (size_t i = 0; i < ne; i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](size_t a, size_t b) { return pks[a].wtab.size() > pks[b].wtab.size(); });
+    size_t tab = 0, maxw = 16;
+    for (size_t i : order) {
+        const size_t wb = pks[i].wtab.size() * sizeof(float);
+        if (!wb) continue;
+        if ((wb & (wb - 1)) != 0 || wb < 16) return fail(PQ_ERR_INTERNAL, "weight table size not a power of two");
+        toff[i] = tab;
+        tab += wb;
+        maxw = std::max(maxw, wb);
+    }
+    size_t data = 0;
+    for (size_t i = 0; i < ne; i++) {
+        doff[i] = data;
+        data += (pks[i].blob.size() + 15) & ~(size_t)15;
+    }
+    auto m = std::make_unique<DevMem>();
+    CU(m->alloc(maxw + tab + data));
+    uint8_t *tbase = reinterpret_cast<uint8_t *>(((uintptr_t)m->p + maxw - 1) & ~(uintptr_t)(maxw - 1));
+    uint8_t *dbase = tbase + tab;
+    for (size_t i = 0; i < ne; i++) {
+        const PackedEngine &pk = pks[i];
+        CU(cudaMemcpy(dbase + doff[i], pk.blob.data(), pk.blob.size(), cudaMemcpyHostToDevice));
+        EngineDev dev = rebase_engine(pk.off, dbase + doff[i]);
+        if (!pk.wtab.empty()) {
+            const size_t wb = pk.wtab.size() * sizeof(float);
+            CU(cudaMemcpy(tbase + toff[i], pk.wtab.data(), wb, cudaMemcpyHostToDevice));
+            dev.wtab = reinterpret_cast<const float4 *>(tbase + toff[i]);
+            if (((uintptr_t)dev.wtab & (wb - 1)) != 0) return fail(PQ_ERR_INTERNAL, "weight table not aligned to its size");
         }
-        uint8_t *base = reinterpret_cast<uint8_t *>(m->p) + shift;
-        CU(cudaMemcpy(base, pk.blob.data(), pk.blob.size(), cudaMemcpyHostToDevice));
-        T.dev.push_back(rebase_engine(pk.off, base));
-        if (wbytes && ((uintptr_t)T.dev.back().wtab & (wbytes - 1)) != 0)
-            return fail(PQ_ERR_INTERNAL, "weight table not aligned to its size");
-        T.bytes += (int64_t)m->n;
-        T.mem.push_back(std::move(m));
+        T.dev.push_back(dev);
+        const auto &e = T.rs.branches[i];
         T.branches_per_amp += std::ldexp(1.0, e->d);
         T.max_d = std::max(T.max_d, e->d);
         T.max_rank = std::max(T.max_rank, e->rank);
         T.max_words = std::max(T.max_words, e->L.full() + e->wf + 2);
     }
+    T.bytes += (int64_t)m->n;
+    T.mem.push_back(std::move(m));
     // boundary map: src | cf_pos | cf_src in one allocation
     std::vector<int32_t> blob;
     blob.insert(blob.end(), T.iom.src.begin(), T.iom.src.end());
@@ -756,7 +781,11 @@ PQ_API pq_status pq_sim_stats(const pq_sim *s, pq_stats *o) {
     o->pairs = s->main.rs.pairs;
     o->num_branches = (int64_t)s->main.rs.branches.size();
     o->branches_per_amplitude = s->main.branches_per_amp;
-    o->device_bytes = s->main.bytes;
+    {
+        std::lock_guard<std::mutex> lk(const_cast<pq_sim *>(s)->mu);
+        o->device_bytes = s->main.bytes;
+        for (const auto &kv : s->marg) o->device_bytes += kv.second->tg.bytes;
+    }
     o->build_seconds = s->build_s;
     return PQ_OK;
 }

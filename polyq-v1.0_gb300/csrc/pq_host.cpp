@@ -892,7 +892,8 @@ PackedEngine pack_engine(const HostEngine& e, const EngineTables& T) {
         w32.push_back((float)(c.re - hr));
         w32.push_back((float)(c.im - hi));
     }
-    d.wtab = as_off<float4>(k.vec(w32));
+    d.wtab = nullptr;  // uploaded apart, at an address aligned to its size
+    P.wtab = std::move(w32);
     // Chunk-sum table: a chunk walks all DI low coordinates, along which the folded Z4 index is
     // linear, i^{m} = i^{m_start} prod_j i^{Lp0_j s_j} (-1)^{b_j s_j}, b_j = (Lp_j >> 1) ^ c_j; so
     // its sum is i^{m_start} T[y_start][b] with
@@ -979,7 +980,7 @@ EngineDev rebase_engine(const EngineDev& o, const uint8_t* base) {
     d.pivcol = shift(o.pivcol, base); d.G = shift(o.G, base); d.Gw = shift(o.Gw, base); d.R = shift(o.R, base);
     d.tlo = shift(o.tlo, base); d.tp = shift(o.tp, base); d.th = shift(o.th, base);
     d.thr = shift(o.thr, base); d.pf = shift(o.pf, base);
-    d.tlo64 = shift(o.tlo64, base); d.tp64 = shift(o.tp64, base); d.wtab = shift(o.wtab, base);
+    d.tlo64 = shift(o.tlo64, base); d.tp64 = shift(o.tp64, base); d.wtab = nullptr;
     d.ctab = o.ctab ? shift(o.ctab, base) : nullptr;
     return d;
 }

@@ -190,7 +190,8 @@ EngineTables build_tables(const HostEngine& e, int di_max);
 namespace pq {
 struct PackedEngine {
     std::vector<uint8_t> blob;
-    EngineDev off;
+    EngineDev off;              // pointers are offsets into blob, except wtab (null: placed apart)
+    std::vector<float> wtab;    // the joint weight table (4 floats per entry), uploaded apart
 };
 PackedEngine pack_engine(const HostEngine& e, const EngineTables& t);
 // Copy of e with its low DI coordinates reordered for the device (see pq_host.cpp); perm[j] is
