@@ -37,7 +37,10 @@ namespace pq {
 thread_local std::string g_err;
 static std::mutex g_mu;
 static int g_device = 0;
-static pq_tuning g_tuning = {10, 4, 8, 48, 3, 4, 0};
+// Library default launch shape (2^10-step chunks, one unit per lane per work item, 8 warps, two
+// blocks per SM with 128 registers, units of 8 chunks): measured best across the plain
+// per-circuit, per-boundary and served workloads; large single launches are autotuned.
+static pq_tuning g_tuning = {10, 1, 8, 48, 2, 8, 0};
 
 // Chunks per unit a tuning allows: eight accumulating chunks per lane only fit the 128-register
 // (two blocks per SM) build of the enumeration kernel.

@@ -37,20 +37,22 @@ def test_noalloc_matches_regular_entry_point_twice(gpu):
     # many-boundaries workload: 16 branch engines, 64 boundaries -> 1024 jobs
     c = workload_many_boundaries(0)
     sim = Simulator(c)
+    # (the entry point walks units of at most 4 chunks: results move by the grouping of chunks
+    # into units, combined in FP32 pairs, far inside the stated bounds)
     for seed in (5, 6):  # two calls in a row, different boundaries
         ys = random_outputs(50, 64, seed)
-        want = sim.amplitudes([0] * 64, ys)
+        want, err = sim.amplitudes([0] * 64, ys, with_error=True)
         got = _noalloc(sim, [0] * 64, ys, torch)
         assert np.all(np.isfinite(got))
-        assert np.max(np.abs(got - want)) <= 1e-12 * np.max(np.abs(want))
+        assert np.all(np.abs(got - want) <= 1e-3 * err + 1e-15 * np.max(np.abs(want)))
     # a small circuit with vanishing boundaries in the mix
     c = workload_small(1)
     sim = Simulator(c)
     ys = [0] + random_outputs(c.num_qubits, 31, 3)
     for _ in range(2):
-        want = sim.amplitudes([0] * 32, ys)
+        want, err = sim.amplitudes([0] * 32, ys, with_error=True)
         got = _noalloc(sim, [0] * 32, ys, torch)
-        assert np.max(np.abs(got - want)) <= 1e-12 * max(1e-300, np.max(np.abs(want)))
+        assert np.all(np.abs(got - want) <= 1e-3 * err + 1e-15 * max(1e-300, np.max(np.abs(want))))
 
 
 def test_noalloc_rejects_sizes_beyond_the_scratch(gpu):
