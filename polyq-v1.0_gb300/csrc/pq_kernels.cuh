@@ -366,8 +366,9 @@ __device__ __forceinline__ void gray_chunk_rot_any(const float4 *__restrict__ W,
 
 // One unit of K chunks (K = 2^np: the chunk at s1 and those that differ from it in the first np
 // pair coordinates) on the FP32 joint-table path: folded start indices, c_j of the walked
-// coordinates, the rotating-frame walk, and each chunk's sum rotated to its last index, scaled
-// by its high-coordinate weight and added into (accx, accy).
+// coordinates, the rotating-frame walk, each chunk's sum rotated to its last index, the chunks
+// combined with their pair-coordinate weights, and the unit's sum scaled by the weight of its
+// other high coordinates and added into (accx, accy).
 template <int MODE, int K>
 __device__ __forceinline__ void walk_unit(const EngineDev &E, const JobDev &J, const uint64_t *G, const uint64_t *R,
                                           const uint8_t *Lp, const uint32_t *Tg, int dl, uint64_t s1, uint64_t lomask,
@@ -709,7 +710,7 @@ __global__ void job_reduce_kernel(KArgs a) {
         // Bound on |computed - exact| relative to sum_s |c(s)| * mag (conservative):
         //  joint table: weights exact to 2^-46 (hi + lo of an FP64 product); hi chunk sums are
         //  exact, the terms below keep an allowance of gamma_n^2 + 2 n u^2 (gamma_n = n u /
-        //  (1 - n u), n = 2^dl) for them; FP64 chunk scaling and reductions a few 2^-52; the lo
+        //  (1 - n u), n = 2^dl) for them; FP64 unit scaling and reductions a few 2^-52; the lo
         //  sums add errfac (per engine, from the grid).  FP64 path: (n + 2 nsl_tp + 8 + nsl_th)
         //  2^-52.  Every path adds the FP64 running sums over a lane's chunks and a job's items.
         const double u32 = 5.9604644775390625e-08, u64 = 1.1102230246251565e-16;
