@@ -365,3 +365,23 @@ def test_probabilities_of_large_amplitudes(gpu):
         want = np.abs(O.dense_statevector(c, 0)) ** 2
         assert np.max(np.abs(p - want)) <= 1e-12
         assert abs(np.sum(p) - 1.0) < 1e-9
+
+
+def test_unit_sizes_agree_within_bounds(gpu):
+    # units of 1, 2, 4 and 8 chunks (the pair coordinates a unit does not vary come from its
+    # first chunk's bits): every unit size within its bound of the device FP64 walk, on the
+    # many-boundaries workload (branch engines with 0..3 pair coordinates)
+    c = workload_many_boundaries(0)
+    ys = random_outputs(50, 64, 77)
+    ref = None
+    old = get_tuning()
+    try:
+        for uc, bps in ((1, 3), (2, 3), (4, 3), (8, 2)):
+            set_tuning(unit_chunks=uc, blocks_per_sm=bps)
+            s = Simulator(c)
+            got, err = s.amplitudes([0] * 64, ys, with_error=True)
+            if ref is None:
+                ref = s.amplitudes_fp64([0] * 64, ys)
+            assert_amps(got, ref, err)
+    finally:
+        set_tuning(unit_chunks=old["unit_chunks"], blocks_per_sm=old["blocks_per_sm"])
