@@ -269,6 +269,9 @@ __device__ __forceinline__ void gray_chunk_rot(const float4 *__restrict__ W4, ui
     }
     const uint32_t inner = (1u << dl) - 1u;
     const uint32_t ngroups = 1u << (dl - 3);
+    // the next step's entry is loaded one step ahead (the last prefetch of the walk reads an
+    // entry of the table that is not used)
+    ulonglong2 wn = __ldg(reinterpret_cast<const ulonglong2 *>(wad ^ (uint64_t)T0));
     // MODE 2 records the true Z8 index: folded index + 2 q(s_lo) (the sign held by the table)
 #define PQ_REC(k)                                                                                        \
     if (MODE == 2)                                                                                       \
@@ -276,10 +279,11 @@ __device__ __forceinline__ void gray_chunk_rot(const float4 *__restrict__ W4, ui
             (uint8_t)((k0 + 2u * (m[k] + 2u * quad_parity(G, ((uint32_t)wad >> 4) & lomask))) & 7u);
     // flip by T, then A <- quarter-turn(A) + w for every chunk of the unit.  RHO2: the (rho, rho)
     // pair of an even step; RHO: the signed rho of an odd step.
-#define PQ_Q(ODD, T, RHO2, RHO, DM)                                                \
+#define PQ_Q(ODD, T, TN, RHO2, RHO, DM)                                            \
     {                                                                              \
+        const ulonglong2 w = wn;                                                   \
         wad ^= (uint64_t)(T);                                                      \
-        const ulonglong2 w = __ldg(reinterpret_cast<const ulonglong2 *>(wad));     \
+        wn = __ldg(reinterpret_cast<const ulonglong2 *>(wad ^ (uint64_t)(TN)));    \
         _Pragma("unroll") for (int k = 0; k < K; k++) {                            \
             if (ODD) qturn_odd(H[k], L[k], (RHO), w);                              \
             else qturn_even(H[k], L[k], (RHO2), w);                                \
@@ -303,21 +307,23 @@ __device__ __forceinline__ void gray_chunk_rot(const float4 *__restrict__ W4, ui
 #define PQ_R1 __uint_as_float((((Pc[k] >> 1) & 1u) << 31) ^ u1)
 #define PQ_R1N __uint_as_float((((Pc[k] >> 1) & 1u) << 31) ^ u1n)
     for (uint32_t g = 0;; ++g) {
-        PQ_Q(O0, T0, pk2(PQ_R0, PQ_R0), PQ_R0, PQ_L0);
-        PQ_Q(O1, T1, pk2(PQ_R1, PQ_R1), PQ_R1, PQ_L1);
-        PQ_Q(O0, T0, pk2(PQ_R0, PQ_R0), PQ_R0N, 0u - PQ_L0);
+        PQ_Q(O0, T0, T1, pk2(PQ_R0, PQ_R0), PQ_R0, PQ_L0);
+        PQ_Q(O1, T1, T0, pk2(PQ_R1, PQ_R1), PQ_R1, PQ_L1);
+        PQ_Q(O0, T0, T2, pk2(PQ_R0, PQ_R0), PQ_R0N, 0u - PQ_L0);
         {
             const bool up = ((uint32_t)wad ^ T2) & 64u;  // coordinate 2's bit after the flip
             const uint32_t u2 = ((((Lp2 >> 1) ^ (O2 && !up ? 1u : 0u)) & 1u) << 31) | 0x3F800000u;
 #define PQ_R2 __uint_as_float((((Pc[k] >> 2) & 1u) << 31) ^ u2)
-            PQ_Q(O2, T2, pk2(PQ_R2, PQ_R2), PQ_R2, up ? PQ_L2 : 0u - PQ_L2);
+            PQ_Q(O2, T2, T0, pk2(PQ_R2, PQ_R2), PQ_R2, up ? PQ_L2 : 0u - PQ_L2);
 #undef PQ_R2
         }
-        PQ_Q(O0, T0, pk2(PQ_R0, PQ_R0), PQ_R0, PQ_L0);
-        PQ_Q(O1, T1, pk2(PQ_R1, PQ_R1), PQ_R1N, 0u - PQ_L1);
-        PQ_Q(O0, T0, pk2(PQ_R0, PQ_R0), PQ_R0N, 0u - PQ_L0);
-        if (g + 1 == ngroups) break;
-        const int j = 3 + ctz32(g + 1);
+        PQ_Q(O0, T0, T1, pk2(PQ_R0, PQ_R0), PQ_R0, PQ_L0);
+        PQ_Q(O1, T1, T0, pk2(PQ_R1, PQ_R1), PQ_R1N, 0u - PQ_L1);
+        const bool last = g + 1 == ngroups;
+        const int j = last ? 0 : 3 + ctz32(g + 1);
+        const uint32_t Tj = Tg[j];
+        PQ_Q(O0, T0, Tj, pk2(PQ_R0, PQ_R0), PQ_R0N, 0u - PQ_L0);
+        if (last) break;
         const uint32_t down = ((uint32_t)wad >> (j + 4)) & 1u;  // bit j is set before a down flip
         const uint32_t Lpj = Lp[j];
         // rho = -1 iff bit 1 of L'_j = Lp_j + 2 c_j is set, negated on an odd down-flip: its sign
@@ -326,9 +332,9 @@ __device__ __forceinline__ void gray_chunk_rot(const float4 *__restrict__ W4, ui
 #define PQ_RHO_J __uint_as_float(((Pc[k] >> j) << 31) ^ u31)
 #define PQ_DM_J (down ? 0u - (Lpj + (((Pc[k] >> j) & 1u) << 1)) : Lpj + (((Pc[k] >> j) & 1u) << 1))
         if (Lpj & 1u) {
-            PQ_Q(1, Tg[j], 0ull, PQ_RHO_J, PQ_DM_J);
+            PQ_Q(1, Tj, T0, 0ull, PQ_RHO_J, PQ_DM_J);
         } else {
-            PQ_Q(0, Tg[j], pk2(PQ_RHO_J, PQ_RHO_J), 0.f, PQ_DM_J);
+            PQ_Q(0, Tj, T0, pk2(PQ_RHO_J, PQ_RHO_J), 0.f, PQ_DM_J);
         }
 #undef PQ_RHO_J
 #undef PQ_DM_J
