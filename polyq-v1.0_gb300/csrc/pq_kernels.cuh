@@ -277,8 +277,9 @@ __device__ __forceinline__ void gray_chunk_rot(const float4 *__restrict__ W4, ui
     if (MODE == 2)                                                                                       \
         dbg[sbase[k] | (((uint32_t)wad >> 4) & inner)] =                                               \
             (uint8_t)((k0 + 2u * (m[k] + 2u * quad_parity(G, ((uint32_t)wad >> 4) & lomask))) & 7u);
-    // flip by T, then A <- quarter-turn(A) + w for every chunk of the unit.  RHO2: the (rho, rho)
-    // pair of an even step; RHO: the signed rho of an odd step.
+    // flip by T, then A <- quarter-turn(A) + w for every chunk of the unit, w the entry loaded
+    // one step earlier; the entry of the following step (stride TN) is loaded here.  RHO2: the
+    // (rho, rho) pair of an even step; RHO: the signed rho of an odd step.
 #define PQ_Q(ODD, T, TN, RHO2, RHO, DM)                                            \
     {                                                                              \
         const ulonglong2 w = wn;                                                   \
