@@ -1401,7 +1401,7 @@ static pq_status tune_search(pq_tuning start, bool tune_inner, TimeOf time_of, p
                 double ms = 0.0;
                 st = eval(t, &ms);
                 if (st != PQ_OK) break;
-                if (ms < best_t * 0.98) {
+                if (ms < best_t * 0.995) {  // event-timed launches repeat to ~0.1%
                     best = t;
                     best_t = ms;
                     changed = true;
