@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <array>
 #include <chrono>
 #include <cmath>
@@ -141,14 +142,34 @@ static pq_status upload_target(Target &T, int di_max) {
     T.branches_per_amp = 0.0;
     const size_t ne = T.rs.branches.size();
     std::vector<PackedEngine> pks(ne);
-    for (size_t i = 0; i < ne; i++) {
-        const auto &e = T.rs.branches[i];
-        // pack a copy in the device's coordinate order (even-increment low coordinates first)
-        std::vector<int> perm;
-        const HostEngine pe = device_order(*e, build_tables(*e, di_max).DI, perm);
-        EngineTables tb = build_tables(pe, di_max);
-        pks[i] = pack_engine(pe, tb);
-        for (int j = 0; j < 16; j++) pks[i].off.cperm[j] = (uint8_t)(j < tb.DI ? perm[(size_t)j] : j);
+    // pack each engine (a copy in the device's coordinate order: even-increment low coordinates
+    // first) on host threads: targets of 2^14 engines take seconds on one core
+    {
+        std::atomic<size_t> next{0};
+        std::vector<std::string> errs(ne);
+        auto work = [&]() {
+            for (size_t i = next++; i < ne; i = next++) {
+                try {
+                    const auto &e = T.rs.branches[i];
+                    std::vector<int> perm;
+                    const HostEngine pe = device_order(*e, build_tables(*e, di_max).DI, perm);
+                    EngineTables tb = build_tables(pe, di_max);
+                    pks[i] = pack_engine(pe, tb);
+                    for (int j = 0; j < 16; j++) pks[i].off.cperm[j] = (uint8_t)(j < tb.DI ? perm[(size_t)j] : j);
+                } catch (const std::exception &ex) {
+                    errs[i] = ex.what();
+                }
+            }
+        };
+        const size_t nth = std::min<size_t>(std::max(1u, std::thread::hardware_concurrency()), ne);
+        if (nth <= 1) work();
+        else {
+            std::vector<std::thread> th;
+            for (size_t t = 0; t < nth; t++) th.emplace_back(work);
+            for (auto &x : th) x.join();
+        }
+        for (auto &e : errs)
+            if (!e.empty()) return fail(PQ_ERR_INTERNAL, "engine packing: " + e);
     }
     // One allocation per target: the weight tables first, each at an offset aligned to its size
     // (a power of two; placed largest first, every offset is a sum of larger powers of two), so
