@@ -39,7 +39,7 @@ WORKLOAD = {"n_qubits": 50, "gates": 2000, "t_count": 32, "circuit_seed": 0, "bo
 # FP32 FMA-pipe operations per enumerated branch in the enumeration kernel's walk
 FMA_OPS_PER_BRANCH = 4
 # DRAM bytes of one full-size enumeration launch (ncu, dram__bytes_read.sum + dram__bytes_write.sum)
-TRAFFIC_BYTES_PER_LAUNCH = 8964864
+TRAFFIC_BYTES_PER_LAUNCH = 8934656
 
 METRIC = "branches/s and amplitudes/s at <=1e-6 rel err vs FP64; served p50/p99 latency"
 
