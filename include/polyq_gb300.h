@@ -122,6 +122,15 @@ PQ_API pq_status pq_marginal(pq_sim *sim, const uint64_t *x, int32_t nmeas, cons
  * stderr (optional): the standard error. */
 PQ_API pq_status pq_amplitude_estimate(pq_sim *sim, const uint64_t *x, const uint64_t *y, int64_t samples,
                                        uint64_t seed, double *out, double *stderr_out);
+/* approx::estimate_amplitude -- approx.rs:96-135: lazy pair sampling.  Sample i seeds
+ * Rng::new(seed ^ i * golden), draws one bit per pair for the first min(pairs, candidates, 62)
+ * pair candidates of the circuit's path sum, builds that branch engine (equal patterns share
+ * one) and evaluates it exactly when its dimension is <= exact_dim_limit, else with
+ * Engine::estimate (2^14 points, the sample's next draw as seed).  out: 2^p * mean (re, im);
+ * stderr (optional): 2^p * sqrt(var / samples).  samples <= 2^24. */
+PQ_API pq_status pq_amplitude_estimate_pairs(pq_sim *sim, const uint64_t *x, const uint64_t *y, int32_t pairs,
+                                             int64_t samples, uint64_t seed, int32_t exact_dim_limit, double *out,
+                                             double *stderr_out);
 /* Simulator::sample_many -- sim.rs:253-284: `shots` computational-basis samples of C|x>, drawn
  * by the chain rule over qubit prefixes with the reference's SplitMix64 streams (one seed per
  * shot from seed), so the same seed gives the reference's samples.  out: shots bitstrings.

@@ -59,6 +59,8 @@ def lib():
             L.pqo_marginal.argtypes = [P, u64p, ct.c_int, i32p, u8p]
             L.pqo_sample_many.argtypes = [P, u64p, ct.c_int64, ct.c_uint64, u64p]
             L.pqo_amplitude_estimate.argtypes = [P, u64p, u64p, ct.c_int64, ct.c_uint64, f64p]
+            L.pqo_amplitude_estimate_pairs.argtypes = [P, u64p, u64p, ct.c_int, ct.c_int64, ct.c_uint64, ct.c_int, f64p]
+            L.pqo_path_info.argtypes = [P, i64p]
             L.pqo_brute_force.restype = ct.c_int
             L.pqo_brute_force.argtypes = [P, u64p, u64p, f64p]
             L.pqo_dense_statevector.argtypes = [ct.c_int, ct.c_int, u8p, i32p, i32p, u32p, u64p, f64p]
@@ -164,6 +166,21 @@ class OracleSim:
         out = np.zeros(3, dtype=np.float64)
         self.L.pqo_amplitude_estimate(self.h, _ptr(xs, ct.c_uint64), _ptr(ys, ct.c_uint64), samples,
                                       ct.c_uint64(seed & (2**64 - 1)), _ptr(out, ct.c_double))
+        return float(out[0]), float(out[1]), float(out[2])
+
+    def path_info(self):
+        """(pair candidates with the io variables fixed, live variables) of the path sum."""
+        out = np.zeros(2, dtype=np.int64)
+        self.L.pqo_path_info(self.h, _ptr(out, ct.c_int64))
+        return int(out[0]), int(out[1])
+
+    def amplitude_estimate_pairs(self, x, y, pairs, samples, seed, exact_dim_limit=20):
+        """approx::estimate_amplitude (src/approx.rs:96-135): (re, im, standard error)."""
+        xs = pack_bits([x], self.nq)
+        ys = pack_bits([y], self.nq)
+        out = np.zeros(3, dtype=np.float64)
+        self.L.pqo_amplitude_estimate_pairs(self.h, _ptr(xs, ct.c_uint64), _ptr(ys, ct.c_uint64), pairs, samples,
+                                            ct.c_uint64(seed & (2**64 - 1)), exact_dim_limit, _ptr(out, ct.c_double))
         return float(out[0]), float(out[1]), float(out[2])
 
     def sample_many(self, x, shots, seed):

@@ -1311,6 +1311,71 @@ void pqo_amplitude_estimate(pqo_sim *s, const uint64_t *x, const uint64_t *y, in
     free(vb); free(a);
 }
 
+/* Pair candidates of the circuit's path sum with its io variables fixed (rank.rs:62-84) and
+ * its live variables (pathsum.rs live_vars): out = {candidates, live variables}. */
+void pqo_path_info(const pqo_sim *s, int64_t out[2]) {
+    int *f = (int *)malloc(sizeof(int) * (size_t)(2 * s->ps.nq + 1));
+    int nf = ps_io_vars(&s->ps, f);
+    pair_t *cands = (pair_t *)malloc(sizeof(pair_t) * (size_t)(s->ps.nv + 1));
+    int nt;
+    out[0] = pair_candidates(&s->ps, f, nf, cands, &nt);
+    int live = 0;
+    for (int v = 0; v < s->ps.nv; v++) live += !s->ps.dead[v];
+    out[1] = live;
+    free(cands); free(f);
+}
+
+/* approx::estimate_amplitude (src/approx.rs:96-135): lazy pair sampling.  Sample i seeds
+ * Rng::new(seed ^ i * golden), draws one bit per pair for the first min(pairs, candidates, 62)
+ * pair candidates, builds that branch engine from a copy of the path sum and evaluates it
+ * exactly when its dimension is <= exact_dim_limit, else by Engine::estimate with 2^14 points
+ * and the sample's next draw as seed.  out: 2^p mean (re, im), 2^p sqrt(var / n). */
+void pqo_amplitude_estimate_pairs(pqo_sim *s, const uint64_t *x, const uint64_t *y, int pairs, int64_t samples,
+                                  uint64_t seed, int exact_dim_limit, double out[3]) {
+    const uint64_t golden = 0x9E3779B97F4A7C15ull;
+    out[0] = out[1] = out[2] = 0.0;
+    asg_t *a = (asg_t *)malloc(sizeof(asg_t) * (size_t)(2 * s->ps.nq + 1));
+    int na = ps_boundary(&s->ps, x, y, a);
+    if (na < 0) { free(a); return; }
+    int *f = (int *)malloc(sizeof(int) * (size_t)(2 * s->ps.nq + 1));
+    int nf = ps_io_vars(&s->ps, f);
+    pair_t *cands = (pair_t *)malloc(sizeof(pair_t) * (size_t)(s->ps.nv + 1));
+    int nt, nc = pair_candidates(&s->ps, f, nf, cands, &nt);
+    int p = pairs < nc ? pairs : nc;
+    if (p > 62) p = 62;
+    cx sum = C(0, 0);
+    double sq = 0.0;
+    asg_t *al[1] = {a};
+    int an[1] = {na};
+    for (int64_t i = 0; i < samples; i++) {
+        srng r = srng_new(seed ^ ((uint64_t)i * golden));
+        pathsum b = ps_clone(&s->ps);
+        for (int j = 0; j < p; j++) ps_substitute(&b, cands[j].a, cands[j].b, (int)(srng_u64(&r) & 1ull));
+        engine *E = engine_new(&b, f, nf);
+        cx v;
+        if (E->el.d <= exact_dim_limit) {
+            rank_engine one; one.nbr = 1; one.pairs = 0; one.br = &E;
+            eval_many(&one, 1, al, an, &v, 1);
+        } else {
+            uint8_t *vals = (uint8_t *)malloc((size_t)E->nf + 1);
+            values_from_asg(E, a, na, vals);
+            double se;
+            engine_estimate(E, vals, (int64_t)1 << 14, srng_u64(&r), &v, &se);
+            free(vals);
+        }
+        sum = cadd(sum, v);
+        sq += v.re * v.re + v.im * v.im;
+        engine_free(E);
+        ps_free(&b);
+    }
+    const double n = (double)samples, scale = ldexp(1.0, p);
+    const cx mean = C(sum.re / n, sum.im / n);
+    double var = sq / n - (mean.re * mean.re + mean.im * mean.im);
+    if (var < 0.0) var = 0.0;
+    out[0] = mean.re * scale; out[1] = mean.im * scale; out[2] = scale * sqrt(var / n);
+    free(cands); free(f); free(a);
+}
+
 /* Simulator::sample / sample_many (src/sim.rs:253-284): one seed per shot from Rng::new(seed);
  * per shot, qubit by qubit, p0 = min(prefix marginal with the new bit 0, p_prev) and the bit is 1
  * iff next_f64() * p_prev >= p0.  The prefix marginal of qubits 0..l is the sandwich engine with

@@ -47,6 +47,11 @@ int pqo_brute_force(pqo_sim *s, const uint64_t *x, const uint64_t *y, double out
 void pqo_sample_many(pqo_sim *s, const uint64_t *x, int64_t shots, uint64_t seed, uint64_t *out);
 void pqo_amplitude_estimate(pqo_sim *s, const uint64_t *x, const uint64_t *y, int64_t samples, uint64_t seed,
                             double out[3]);
+/* {pair candidates with the io variables fixed, live variables} of the circuit's path sum. */
+void pqo_path_info(const pqo_sim *s, int64_t out[2]);
+/* approx::estimate_amplitude (approx.rs:96-135): out = (re, im, stderr). */
+void pqo_amplitude_estimate_pairs(pqo_sim *s, const uint64_t *x, const uint64_t *y, int pairs, int64_t samples,
+                                  uint64_t seed, int exact_dim_limit, double out[3]);
 
 /* Dense statevector (src/dense.rs:12-27); out has 2*2^nq doubles. */
 void pqo_dense_statevector(int nq, int ngates, const uint8_t *op, const int32_t *q0, const int32_t *q1,

@@ -1152,6 +1152,175 @@ PQ_API pq_status pq_amplitude_estimate(pq_sim *s, const uint64_t *x, const uint6
     return mc_finish(E, J, hp, grid, samples, out, stderr_out);
 }
 
+// Lazy pair sampling (src/approx.rs:96-135, estimate_amplitude): sample i draws
+// Rng::new(seed ^ i * golden), takes one bit per pair for the first p pair candidates, builds
+// that branch engine (substitutions + one elimination, on host threads; equal patterns share
+// one engine) and evaluates it exactly when its dimension is at most exact_dim_limit, else by
+// Engine::estimate with 2^14 points and the sample's next draw as seed.  The estimate is
+// 2^p mean and its standard error 2^p sqrt(var / n).
+PQ_API pq_status pq_amplitude_estimate_pairs(pq_sim *s, const uint64_t *x, const uint64_t *y, int32_t pairs,
+                                             int64_t samples, uint64_t seed, int32_t exact_dim_limit, double *out,
+                                             double *stderr_out) {
+    if (!s || !x || !y || !out) return fail(PQ_ERR_INVALID_ARG, "null argument");
+    if (pairs < 0) return fail(PQ_ERR_INVALID_ARG, "negative pair count");
+    if (samples <= 0 || samples > (1LL << 24)) return fail(PQ_ERR_INVALID_ARG, "samples must be in 1..2^24");
+    if (exact_dim_limit < 0) return fail(PQ_ERR_INVALID_ARG, "negative exact dimension limit");
+    if (s->host_only) return fail(PQ_ERR_NO_DEVICE, "simulator was created by pq_analyze (host structures only)");
+    std::lock_guard<std::mutex> lk(s->mu);
+    CU(cudaSetDevice(s->device));
+    const uint64_t golden = 0x9E3779B97F4A7C15ull;
+    const int nw = s->nw;
+    out[0] = out[1] = 0.0;
+    if (stderr_out) *stderr_out = 0.0;
+    int ntc = 0;
+    const std::vector<int> &fixed = s->main.iom.fixed;
+    const auto cands = pair_candidates(s->ps, fixed, ntc);
+    const int p = std::min(std::min((int)pairs, (int)cands.size()), 62);
+    const size_t ns = (size_t)samples;
+    std::vector<uint64_t> pat(ns), mseed(ns);
+    std::map<uint64_t, int> index;  // pattern -> distinct engine
+    std::vector<uint64_t> distinct;
+    std::vector<int> eng_of(ns);
+    for (size_t i = 0; i < ns; i++) {
+        SplitMix r(seed ^ ((uint64_t)i * golden));
+        uint64_t b = 0;
+        for (int j = 0; j < p; j++) b |= (r.u64() & 1ull) << j;
+        pat[i] = b;
+        mseed[i] = r.u64();
+        auto it = index.find(b);
+        if (it == index.end()) {
+            it = index.emplace(b, (int)distinct.size()).first;
+            distinct.push_back(b);
+        }
+        eng_of[i] = it->second;
+    }
+    // one engine per distinct pattern, on host threads
+    Target T;
+    T.iom = s->main.iom;
+    T.rs.pairs = p;
+    T.rs.branches.resize(distinct.size());
+    {
+        std::atomic<size_t> next{0};
+        std::vector<std::string> errs(distinct.size());
+        auto work = [&]() {
+            for (size_t k = next++; k < distinct.size(); k = next++) {
+                try {
+                    T.rs.branches[k] = pattern_engine(s->ps, fixed, cands, p, distinct[k]);
+                } catch (const std::exception &e) {
+                    errs[k] = e.what();
+                }
+            }
+        };
+        const size_t nth = std::min<size_t>(std::max(1u, std::thread::hardware_concurrency()), distinct.size());
+        if (nth <= 1) work();
+        else {
+            std::vector<std::thread> th;
+            for (size_t t = 0; t < nth; t++) th.emplace_back(work);
+            for (auto &t : th) t.join();
+        }
+        for (auto &e : errs)
+            if (!e.empty()) return fail(PQ_ERR_INTERNAL, "engine build: " + e);
+    }
+    pq_status st = upload_target(T, s->di_max);
+    if (st != PQ_OK) return st;
+    const int64_t kMcPoints = 1 << 14;
+    std::vector<std::complex<double>> val(distinct.size());  // exact values
+    std::vector<char> exact(distinct.size(), 0);
+    std::vector<Target> views(distinct.size());
+    std::vector<Segment> segs;
+    std::vector<size_t> seg_engine;
+    for (size_t k = 0; k < distinct.size(); k++) {
+        views[k].dev.push_back(T.dev[k]);
+        views[k].iom_dev = T.iom_dev;
+        views[k].max_words = T.max_words;
+        const EngineDev &E = T.dev[k];
+        // the reference's own rule, and Engine::estimate's exact sum for subspaces of at most
+        // as many points as it would sample
+        const bool ex = E.d <= exact_dim_limit || (E.d < 63 && (1LL << E.d) <= kMcPoints);
+        if (ex && (E.d > s->tu.max_branch_dim || E.rank > kMaxPivots))
+            return fail(PQ_ERR_ADMISSION_REFUSED, "sampled branch engine above the enumeration's limits");
+        if (ex) {
+            exact[k] = 1;
+            segs.push_back({&views[k], 1});
+            seg_engine.push_back(k);
+        }
+    }
+    if (!segs.empty()) {
+        Plan P;
+        st = build_plan(segs, nw, s->stream, s->tu, P);
+        if (st != PQ_OK) return st;
+        std::vector<uint64_t> X(segs.size() * nw), Y(segs.size() * nw);
+        for (size_t k = 0; k < segs.size(); k++) {
+            std::memcpy(&X[k * nw], x, sizeof(uint64_t) * nw);
+            std::memcpy(&Y[k * nw], y, sizeof(uint64_t) * nw);
+        }
+        std::vector<double> amp(2 * segs.size());
+        st = run_host(P, X.data(), Y.data(), amp.data(), nullptr, CERT_NONE);
+        if (st != PQ_OK) return st;
+        for (size_t k = 0; k < segs.size(); k++) val[seg_engine[k]] = {amp[2 * k], amp[2 * k + 1]};
+    }
+    // Monte-Carlo samples: per distinct engine, prepare once, then one sampler launch per sample
+    std::vector<std::complex<double>> mcval(ns);
+    for (size_t k = 0; k < distinct.size(); k++) {
+        if (exact[k]) continue;
+        const EngineDev &E = T.dev[k];
+        if (E.d > 64 * MC_WORDS) return fail(PQ_ERR_UNSUPPORTED, "Monte-Carlo estimate supports branch dimensions up to 512");
+        Plan Q;
+        std::vector<Segment> one{{&views[k], 1}};
+        st = build_plan(one, nw, s->stream, s->tu, Q, false, true);
+        if (st != PQ_OK) return st;
+        DevMem lpx;
+        if (E.d > kMaxD) {
+            CU(lpx.alloc((size_t)E.d));
+            Q.args.lpx = lpx.as<uint8_t>();
+            Q.args.lpx_stride = E.d;
+        }
+        const size_t bwb = (size_t)nw * 8;
+        CU(cudaMemcpyAsync(Q.x.p, x, bwb, cudaMemcpyHostToDevice, Q.stream));
+        CU(cudaMemcpyAsync(Q.y.p, y, bwb, cudaMemcpyHostToDevice, Q.stream));
+        prepare_kernel<<<Q.grid_prep, 128, (size_t)4 * Q.smem_words * 8, Q.stream>>>(Q.args);
+        CU(cudaGetLastError());
+        const int grid = (int)std::max<long long>(1, std::min<long long>((kMcPoints + 255) / 256, (long long)sm_count() * 8));
+        DevMem part;
+        CU(part.alloc((size_t)grid * 3 * sizeof(double)));
+        JobDev J;
+        CU(cudaMemcpyAsync(&J, Q.jobs.p, sizeof(JobDev), cudaMemcpyDeviceToHost, Q.stream));
+        std::vector<double> hp((size_t)grid * 3);
+        for (size_t i = 0; i < ns; i++) {
+            if (eng_of[i] != (int)k) continue;
+            if (E.d > kMaxD)
+                mc_big_kernel<<<grid, 256, 0, Q.stream>>>(Q.engines.as<EngineDev>(), Q.jobs.as<JobDev>(),
+                                                          lpx.as<uint8_t>(), mseed[i], (long long)kMcPoints,
+                                                          part.as<double>());
+            else
+                mc_kernel<<<grid, 256, 0, Q.stream>>>(Q.engines.as<EngineDev>(), Q.jobs.as<JobDev>(), mseed[i],
+                                                      (long long)kMcPoints, part.as<double>());
+            CU(cudaGetLastError());
+            CU(cudaMemcpyAsync(hp.data(), part.p, hp.size() * sizeof(double), cudaMemcpyDeviceToHost, Q.stream));
+            CU(cudaStreamSynchronize(Q.stream));
+            double v[2] = {0.0, 0.0};
+            st = mc_finish(E, J, hp, grid, kMcPoints, v, nullptr);
+            if (st != PQ_OK) return st;
+            mcval[i] = {v[0], v[1]};
+        }
+    }
+    std::complex<double> sum(0.0, 0.0);
+    double sq = 0.0;
+    for (size_t i = 0; i < ns; i++) {
+        const std::complex<double> a = exact[(size_t)eng_of[i]] ? val[(size_t)eng_of[i]] : mcval[i];
+        sum += a;
+        sq += std::norm(a);
+    }
+    const double n = (double)samples;
+    const std::complex<double> mean = sum / n;
+    const double var = std::max(sq / n - std::norm(mean), 0.0);
+    const double scale = std::ldexp(1.0, p);
+    out[0] = mean.real() * scale;
+    out[1] = mean.imag() * scale;
+    if (stderr_out) *stderr_out = scale * std::sqrt(var / n);
+    return PQ_OK;
+}
+
 // ---------------------------------------------------------------- sampling
 // Simulator::sample_many (src/sim.rs:253-284) with the shots batched per qubit: level l
 // evaluates, for every shot at once, the marginal of qubits 0..l with the shot's decided prefix

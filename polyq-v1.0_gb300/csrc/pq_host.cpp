@@ -626,7 +626,7 @@ std::unique_ptr<HostEngine> build_engine(const PathSum& ps, const std::vector<in
 static const int kMaxPairs = 14;
 static const uint32_t kMask30 = (1u << 30) - 1;
 
-static std::vector<std::pair<int, int>> pair_candidates(const PathSum& ps, const std::vector<int>& fixed, int& ntclass) {
+std::vector<std::pair<int, int>> pair_candidates(const PathSum& ps, const std::vector<int>& fixed, int& ntclass) {
     std::map<uint32_t, std::vector<int>> groups;  // rank.rs:62-84
     for (int k = 0; k < ps.nv; k++) {
         if (ps.dead[k] || ps.theta[k] == 0) continue;
@@ -659,6 +659,13 @@ int best_pairs(const HostEngine& base, int available, int tclass) {  // rank.rs:
         if (cost < bestc) { best = p; bestc = cost; }
     }
     return best;
+}
+
+std::unique_ptr<HostEngine> pattern_engine(const PathSum& ps, const std::vector<int>& fixed,
+                                           const std::vector<std::pair<int, int>>& cands, int p, uint64_t pattern) {
+    PathSum b = ps;
+    for (int i = 0; i < p; i++) b.substitute(cands[(size_t)i].first, cands[(size_t)i].second, (pattern >> i) & 1ull);
+    return build_engine(b, fixed);
 }
 
 // 2^p branch engines built on host threads (rank.rs:88-103 builds them with rayon)

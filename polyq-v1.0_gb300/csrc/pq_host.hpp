@@ -167,6 +167,12 @@ struct RankSet {
 };
 RankSet build_rank(const PathSum& ps, const std::vector<int>& fixed, int strategy, int pairs);
 int best_pairs(const HostEngine& base, int available, int tclass);
+// Substitution pairs (src/rank.rs:62-84): T-class pairs first; ntclass = their count.
+std::vector<std::pair<int, int>> pair_candidates(const PathSum& ps, const std::vector<int>& fixed, int& ntclass);
+// The branch engine of one pattern of the first p pairs (bit i: the value substituted for pair
+// i), built from a copy of ps (src/approx.rs:112-117).
+std::unique_ptr<HostEngine> pattern_engine(const PathSum& ps, const std::vector<int>& fixed,
+                                           const std::vector<std::pair<int, int>>& cands, int p, uint64_t pattern);
 
 // Weight tables of one branch engine (FP64; the device also keeps FP32 roundings):
 //   tlo[s]  = prod_{j < DI} a_{free(j)}[s_j]                 s < 2^DI, DI = min(d, di_max)

@@ -73,6 +73,8 @@ SIGNATURES = {
     "pq_marginal": (ct.c_int, [P, u64p, ct.c_int32, i32p, u8p, f64p]),
     "pq_sample_many": (ct.c_int, [P, u64p, ct.c_int64, ct.c_uint64, u64p]),
     "pq_amplitude_estimate": (ct.c_int, [P, u64p, u64p, ct.c_int64, ct.c_uint64, f64p, f64p]),
+    "pq_amplitude_estimate_pairs": (ct.c_int, [P, u64p, u64p, ct.c_int32, ct.c_int64, ct.c_uint64, ct.c_int32, f64p,
+                                               f64p]),
     "pq_amplitudes_device": (ct.c_int, [P, ct.c_int64, P, P, P, P, P]),
     "pq_amplitudes_plain": (ct.c_int, [P, ct.c_int64, u64p, u64p, f64p]),
     "pq_amplitudes_fp64": (ct.c_int, [P, ct.c_int64, u64p, u64p, f64p]),

@@ -190,6 +190,21 @@ class Simulator:
                                               _p(se, ct.c_double)))
         return float(out[0]), float(out[1]), float(se[0])
 
+    def amplitude_estimate_pairs(self, input: int, output: int, pairs: int, samples: int, seed: int,
+                                 exact_dim_limit: int = 20):
+        """src/approx.rs:96-135 (estimate_amplitude): (re, im, standard_error) of the lazy
+        pair-sampling estimate of <output|C|input> -- `samples` random patterns of the first
+        `pairs` pair candidates, each branch engine built on the fly and evaluated exactly (or by
+        Monte Carlo above `exact_dim_limit`)."""
+        xs = pack_bits([input], self.num_qubits)
+        ys = pack_bits([output], self.num_qubits)
+        out = np.zeros(2, dtype=np.float64)
+        se = np.zeros(1, dtype=np.float64)
+        N.check(self._L.pq_amplitude_estimate_pairs(self._h, _p(xs, ct.c_uint64), _p(ys, ct.c_uint64), int(pairs),
+                                                    int(samples), ct.c_uint64(seed & (2**64 - 1)),
+                                                    int(exact_dim_limit), _p(out, ct.c_double), _p(se, ct.c_double)))
+        return float(out[0]), float(out[1]), float(se[0])
+
     def sample_many(self, input: int, shots: int, seed: int):
         """src/sim.rs:272-284 / src/pybind.rs sample_many: `shots` measurement outcomes of C|input>
         as basis-state indices (the reference's SplitMix64 streams: same seed, same samples)."""

@@ -73,3 +73,39 @@ def test_sampled_large_subspace_matches_oracle(gpu, per_layer):
         scale = max(abs(complex(want[0], want[1])), want[2], 1e-300)
         assert abs(complex(got[0], got[1]) - complex(want[0], want[1])) <= 1e-9 * scale
         assert got[2] == pytest.approx(want[2], rel=1e-9)
+
+
+def test_lazy_pair_sampling_matches_oracle(gpu):
+    # src/approx.rs:96-135 on the device: the same draws as the oracle's restatement.  Exact
+    # branches (the circuits of src/approx.rs:210-229): FP32 walk vs FP64, and unbiased within
+    # 6 standard errors + 5e-3 of the dense amplitude
+    rng = Rng(62)
+    tested = 0
+    for _ in range(30):
+        c = random_layered(3, 3, rng)
+        ref = O.OracleSim(c, "cached")
+        cands, live = ref.path_info()
+        if cands < 3 or live > 20:
+            continue
+        tested += 1
+        y = rng.below(8)
+        sim = Simulator(c, "cached")
+        re, im, se = sim.amplitude_estimate_pairs(0, y, 3, 4000, 5, 20)
+        ore, oim, ose = ref.amplitude_estimate_pairs(0, y, 3, 4000, 5, 20)
+        assert abs(complex(re, im) - complex(ore, oim)) <= 1e-9
+        assert se == pytest.approx(ose, rel=1e-6, abs=1e-9)
+        want = O.dense_statevector(c, 0)[y]
+        assert abs(complex(re, im) - want) < 6.0 * se + 5e-3
+    assert tested >= 3
+    # Monte-Carlo branches: 2 pairs of the many-boundaries circuit leave branch engines of
+    # d ~ 25 > the limit 10, estimated with 2^14 points each from the sample's own seed
+    from polyq_gb300.rng import random_outputs
+    c = workload_many_boundaries(0)
+    y = random_outputs(50, 1, 3)[0]
+    sim = Simulator(c, "cached")
+    ref = O.OracleSim(c, "cached")
+    got = sim.amplitude_estimate_pairs(0, y, 2, 12, 7, 10)
+    want = ref.amplitude_estimate_pairs(0, y, 2, 12, 7, 10)
+    scale = max(abs(complex(want[0], want[1])), want[2], 1e-300)
+    assert abs(complex(got[0], got[1]) - complex(want[0], want[1])) <= 1e-9 * scale
+    assert got[2] == pytest.approx(want[2], rel=1e-6)

@@ -307,3 +307,40 @@ def test_subspace_monte_carlo_sampled():
         assert se > 0.0
         assert abs(complex(re, im) - want) < 6.0 * se + 5e-3
     assert tested >= 3
+
+
+def _lazy_pair_cases(seed, trials):
+    # the circuits of src/approx.rs:210-229: random_layered(3, 3) with at least 3 pair
+    # candidates and at most 20 live path-sum variables; y drawn after the filter
+    rng = Rng(seed)
+    for _ in range(trials):
+        c = random_layered(3, 3, rng)
+        sim = O.OracleSim(c, "cached")
+        cands, live = sim.path_info()
+        if cands < 3 or live > 20:
+            continue
+        yield c, sim, rng.below(1 << 3)
+
+
+def test_lazy_pair_sampling_is_unbiased():
+    # src/approx.rs:210-229: estimate_amplitude(ps, io vars, boundary, 3 pairs, 4000 samples,
+    # seed 5, exact dimension limit 20) within 6 standard errors + 5e-3 of the dense amplitude
+    tested = 0
+    for c, sim, y in _lazy_pair_cases(62, 30):
+        tested += 1
+        want = O.dense_statevector(c, 0)[y]
+        re, im, se = sim.amplitude_estimate_pairs(0, y, 3, 4000, 5, 20)
+        assert abs(complex(re, im) - want) < 6.0 * se + 5e-3, (re, im, se, want)
+    assert tested >= 3
+
+
+def test_lazy_pair_sampling_monte_carlo_branches():
+    # exact dimension limit 0: every sampled branch engine goes through Engine::estimate (here
+    # with its exact fallback, 2^d <= 2^14); same tolerance
+    tested = 0
+    for c, sim, y in _lazy_pair_cases(62, 30):
+        tested += 1
+        want = O.dense_statevector(c, 0)[y]
+        re, im, se = sim.amplitude_estimate_pairs(0, y, 3, 400, 9, 0)
+        assert abs(complex(re, im) - want) < 6.0 * se + 5e-3
+    assert tested >= 3
