@@ -571,6 +571,9 @@ def run_serve(args):
     full, served = load(args.rate, args.duration)
     cap = full["throughput_per_s"] or args.rate
     sub, _ = load(0.5 * min(cap, args.rate), args.duration)
+    # capacity: four times the offered rate for a quarter of the time (the served rate there is
+    # what the server sustains when arrivals outrun it)
+    sat, _ = load(4.0 * args.rate, 0.25 * args.duration)
     # plain per-request launches (one synchronous call per request, no batching) on a sample of
     # the requests the server admitted
     reqs = served[:300]
@@ -597,7 +600,8 @@ def run_serve(args):
              "p50_ms": 1e3 * _pct(lat, 0.5), "p99_ms": 1e3 * _pct(lat, 0.99)}
     srv.close()
     line = {"metric": METRIC, "workload": "serve", "value": full["throughput_per_s"], "unit": "requests/s",
-            "at_offered_load": full, "sub_saturation": sub, "plain_per_request": plain, "n_gpus": 1,
+            "at_offered_load": full, "sub_saturation": sub, "saturated": sat, "plain_per_request": plain,
+            "n_gpus": 1,
             "data": "synthetic",
             "config": {"workload": "64 resident circuits n~U[16,64], 40n gates, T~U[8,40] (seed 5); Poisson arrivals; "
                                    "amplitude/probability/marginal 1:1:1; marginals on one of the first 4 qubits",
