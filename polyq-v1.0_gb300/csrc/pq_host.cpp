@@ -408,15 +408,16 @@ Structure eliminate(const std::vector<Bits>& bmat, const Bits& parity) {
 }
 
 // z4 value of a basis vector (normal_form.rs:339-348).  The bilinear part p^T B p (B symmetric,
-// zero diagonal, a few entries per row) is summed over B's adjacency lists: O(|p| deg) bit
-// tests instead of |p| row-wide popcounts.
-static unsigned z4_value(const std::vector<std::vector<int>>& adj, const Bits& v0, const Bits& v1, const Bits& p) {
+// zero diagonal, a few entries per row) counts every pair {j, k} of p's bits with B_jk = 1
+// twice; its half is summed over the upper adjacency lists (neighbours k > j): O(|p| deg / 2)
+// bit tests instead of |p| row-wide popcounts.
+static unsigned z4_value(const std::vector<std::vector<int>>& upper, const Bits& v0, const Bits& v1, const Bits& p) {
     unsigned lin = p.and_count(v0) + 2 * p.and_count(v1);
-    unsigned t = 0;
+    unsigned half = 0;
     p.for_each_one([&](int j) {
-        for (int k : adj[(size_t)j]) t += p.get(k) ? 1u : 0u;
+        for (int k : upper[(size_t)j]) half += p.get(k) ? 1u : 0u;
     });
-    return (lin + 2 * ((t / 2) & 1)) & 3u;
+    return (lin + 2 * (half & 1)) & 3u;
 }
 
 int HostEngine::phase8(const uint64_t* u) const {  // normal_form.rs:479-493
@@ -555,8 +556,11 @@ std::unique_ptr<HostEngine> build_engine(const PathSum& ps, const std::vector<in
     // Z4 diagonal (normal_form.rs:354-391)
     Bits v0(m), v1(m);
     for (int i = 0; i < m; i++) { uint8_t x = ps.v[E->freev[i]]; v0.set(i, x & 1); v1.set(i, (x & 2) != 0); }
-    std::vector<std::vector<int>> adj((size_t)m);
-    for (int i = 0; i < m; i++) adj[(size_t)i] = bff[(size_t)i].ones();
+    std::vector<std::vector<int>> adj((size_t)m);  // upper adjacency: neighbours k > i
+    for (int i = 0; i < m; i++)
+        bff[(size_t)i].for_each_one([&](int k) {
+            if (k > i) adj[(size_t)i].push_back(k);
+        });
     Diag& dg = E->dg;
     dg.wa = Bits(Lo.g); dg.wb = Bits(Lo.g); dg.o1 = Bits(Lo.nodd); dg.o3 = Bits(Lo.nodd); dg.we = Bits(Lo.neven);
     for (int j = 0; j < Lo.g; j++) {
