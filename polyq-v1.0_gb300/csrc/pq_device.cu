@@ -1177,7 +1177,7 @@ PQ_API pq_status pq_amplitude_estimate_pairs(pq_sim *s, const uint64_t *x, const
     const auto cands = pair_candidates(s->ps, fixed, ntc);
     const int p = std::min(std::min((int)pairs, (int)cands.size()), 62);
     const size_t ns = (size_t)samples;
-    std::vector<uint64_t> pat(ns), mseed(ns);
+    std::vector<uint64_t> mseed(ns);
     std::map<uint64_t, int> index;  // pattern -> distinct engine
     std::vector<uint64_t> distinct;
     std::vector<int> eng_of(ns);
@@ -1185,7 +1185,6 @@ PQ_API pq_status pq_amplitude_estimate_pairs(pq_sim *s, const uint64_t *x, const
         SplitMix r(seed ^ ((uint64_t)i * golden));
         uint64_t b = 0;
         for (int j = 0; j < p; j++) b |= (r.u64() & 1ull) << j;
-        pat[i] = b;
         mseed[i] = r.u64();
         auto it = index.find(b);
         if (it == index.end()) {
@@ -1259,8 +1258,16 @@ PQ_API pq_status pq_amplitude_estimate_pairs(pq_sim *s, const uint64_t *x, const
         if (st != PQ_OK) return st;
         for (size_t k = 0; k < segs.size(); k++) val[seg_engine[k]] = {amp[2 * k], amp[2 * k + 1]};
     }
-    // Monte-Carlo samples: per distinct engine, prepare once, then one sampler launch per sample
-    std::vector<std::complex<double>> mcval(ns);
+    // exact samples: their engine's value; Monte-Carlo samples: per distinct engine, prepare
+    // once, then one sampler launch per sample
+    std::complex<double> sum(0.0, 0.0);
+    double sq = 0.0;
+    for (size_t i = 0; i < ns; i++)
+        if (exact[(size_t)eng_of[i]]) {
+            const std::complex<double> a = val[(size_t)eng_of[i]];
+            sum += a;
+            sq += std::norm(a);
+        }
     for (size_t k = 0; k < distinct.size(); k++) {
         if (exact[k]) continue;
         const EngineDev &E = T.dev[k];
@@ -1301,15 +1308,10 @@ PQ_API pq_status pq_amplitude_estimate_pairs(pq_sim *s, const uint64_t *x, const
             double v[2] = {0.0, 0.0};
             st = mc_finish(E, J, hp, grid, kMcPoints, v, nullptr);
             if (st != PQ_OK) return st;
-            mcval[i] = {v[0], v[1]};
+            const std::complex<double> a(v[0], v[1]);
+            sum += a;
+            sq += std::norm(a);
         }
-    }
-    std::complex<double> sum(0.0, 0.0);
-    double sq = 0.0;
-    for (size_t i = 0; i < ns; i++) {
-        const std::complex<double> a = exact[(size_t)eng_of[i]] ? val[(size_t)eng_of[i]] : mcval[i];
-        sum += a;
-        sq += std::norm(a);
     }
     const double n = (double)samples;
     const std::complex<double> mean = sum / n;
