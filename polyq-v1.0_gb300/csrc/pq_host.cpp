@@ -237,9 +237,8 @@ void PathSum::trace_closure() {  // pathsum.rs:399-425
 // Rows are kept with the span of words that may hold set bits, so that the row operations
 // of a step cost the span of the vectors involved, not the full width m/64 (the quadratic
 // forms of circuits are local: a variable meets few others, and those were created near it).
-// The pivot queues are binary heaps with lazy deletion; a popped entry is used only if it
-// still equals its variable's current key, so the choice is the minimum (weight, index)
-// exactly as with an ordered set.
+// The pivot queues hold each variable once under its current key and yield the minimum
+// (weight, index), the MinWeight rule's choice.
 namespace {
 struct SpanRows {
     int W = 0;
@@ -267,6 +266,40 @@ struct SpanRows {
         Bits o(len);
         std::copy(row(i) + lo[i], row(i) + hi[i], o.w.begin() + lo[i]);
         return o;
+    }
+};
+// Pivot queue of one class: the variables keyed by (weight, index), minimum first.  Weights
+// below 64 live in per-weight bitsets (with a count and a lowest-word hint), the rest in an
+// ordered set; the minimum is the lowest index of the lightest non-empty weight.
+struct PivotQueue {
+    static const int kB = 64;
+    int W;
+    std::vector<uint64_t> bits;  // kB x W
+    int cnt[kB];
+    int hint[kB];                // no bit below this word
+    std::set<std::pair<uint32_t, int>> big;
+    explicit PivotQueue(int words) : W(words), bits((size_t)kB * words, 0ull) {
+        for (int w = 0; w < kB; w++) { cnt[w] = 0; hint[w] = words; }
+    }
+    void add(uint32_t w, int a) {
+        if (w >= (uint32_t)kB) { big.insert({w, a}); return; }
+        bits[(size_t)w * W + (a >> 6)] |= 1ull << (a & 63);
+        cnt[w]++;
+        hint[w] = std::min(hint[w], a >> 6);
+    }
+    void del(uint32_t w, int a) {
+        if (w >= (uint32_t)kB) { big.erase({w, a}); return; }
+        bits[(size_t)w * W + (a >> 6)] &= ~(1ull << (a & 63));
+        cnt[w]--;
+    }
+    int min() {
+        for (int w = 0; w < kB; w++) {
+            if (!cnt[w]) continue;
+            const uint64_t* b = &bits[(size_t)w * W];
+            for (int q = hint[w]; q < W; q++)
+                if (b[q]) { hint[w] = q; return q * 64 + __builtin_ctzll(b[q]); }
+        }
+        return big.empty() ? -1 : big.begin()->second;
     }
 };
 // A scratch vector with its word span; cleared over that span.
@@ -309,21 +342,7 @@ Structure eliminate(const std::vector<Bits>& bmat, const Bits& parity) {
     st.m = m;
     // key[a] = (class, weight): class 1 = diagonal set, 2 = off-diagonal only, 0 = neither
     std::vector<std::pair<uint8_t, uint32_t>> key((size_t)m, {0, 0});
-    using Entry = std::pair<uint32_t, int>;
-    std::vector<Entry> dheap, oheap;
-    auto push = [](std::vector<Entry>& h, Entry e) {
-        h.push_back(e);
-        std::push_heap(h.begin(), h.end(), std::greater<Entry>());
-    };
-    auto top = [&](std::vector<Entry>& h, uint8_t cls) -> int {
-        while (!h.empty()) {
-            const Entry e = h.front();
-            if (key[e.second].first == cls && key[e.second].second == e.first) return e.second;
-            std::pop_heap(h.begin(), h.end(), std::greater<Entry>());
-            h.pop_back();
-        }
-        return -1;
-    };
+    PivotQueue dq(W), oq(W);
     auto reclass = [&](int a) {
         std::pair<uint8_t, uint32_t> k{0, 0};
         if (is_alive(a)) {
@@ -334,9 +353,11 @@ Structure eliminate(const std::vector<Bits>& bmat, const Bits& parity) {
             else if (w > 0) k = {2, w};
         }
         if (k == key[a]) return;
+        if (key[a].first == 1) dq.del(key[a].second, a);
+        else if (key[a].first == 2) oq.del(key[a].second, a);
         key[a] = k;
-        if (k.first == 1) push(dheap, {k.second, a});
-        else if (k.first == 2) push(oheap, {k.second, a});
+        if (k.first == 1) dq.add(k.second, a);
+        else if (k.first == 2) oq.add(k.second, a);
     };
     for (int a = 0; a < m; a++) reclass(a);
     SpanVec s(W), sb(W), touched(W);
@@ -348,7 +369,7 @@ Structure eliminate(const std::vector<Bits>& bmat, const Bits& parity) {
     };
     auto kill = [&](int a) { alive[(size_t)a >> 6] &= ~(1ull << (a & 63)); };
     while (true) {
-        int a = top(dheap, 1);
+        int a = dq.min();
         if (a >= 0) {  // single_step (normal_form.rs:61-82)
             masked(s, a);
             s.unset(a);
@@ -366,7 +387,7 @@ Structure eliminate(const std::vector<Bits>& bmat, const Bits& parity) {
             s.clear();
             continue;
         }
-        a = top(oheap, 2);
+        a = oq.min();
         if (a >= 0) {  // hyper_step (normal_form.rs:87-129)
             masked(s, a);
             s.trim();
