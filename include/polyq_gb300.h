@@ -127,7 +127,8 @@ PQ_API pq_status pq_amplitude_estimate(pq_sim *sim, const uint64_t *x, const uin
  * pair candidates of the circuit's path sum, builds that branch engine (equal patterns share
  * one) and evaluates it exactly when its dimension is <= exact_dim_limit, else with
  * Engine::estimate (2^14 points, the sample's next draw as seed).  out: 2^p * mean (re, im);
- * stderr (optional): 2^p * sqrt(var / samples).  samples <= 2^24. */
+ * stderr (optional): 2^p * sqrt(var / samples).  samples <= 2^24, at most 2^14 distinct
+ * sampled patterns per call (their engines are held for the call). */
 PQ_API pq_status pq_amplitude_estimate_pairs(pq_sim *sim, const uint64_t *x, const uint64_t *y, int32_t pairs,
                                              int64_t samples, uint64_t seed, int32_t exact_dim_limit, double *out,
                                              double *stderr_out);

@@ -1193,6 +1193,10 @@ PQ_API pq_status pq_amplitude_estimate_pairs(pq_sim *s, const uint64_t *x, const
         }
         eng_of[i] = it->second;
     }
+    // every distinct pattern's engine is held (host and device) for the call, as the 2^p
+    // engines of a rank strategy are: the same cap, 2^14
+    if (distinct.size() > ((size_t)1 << 14))
+        return fail(PQ_ERR_INVALID_ARG, "more than 2^14 distinct sampled branch engines in one call; split the samples");
     // one engine per distinct pattern, on host threads
     Target T;
     T.iom = s->main.iom;
