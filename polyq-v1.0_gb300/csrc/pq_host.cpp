@@ -382,6 +382,7 @@ Structure eliminate(const std::vector<Bits>& bmat, const Bits& parity) {
             });
             kill(a);
             st.odd.push_back(pa);
+            st.sodd.push_back({plo, phi});
             reclass(a);
             s.for_each_one([&](int bi) { reclass(bi); });
             s.clear();
@@ -413,6 +414,8 @@ Structure eliminate(const std::vector<Bits>& bmat, const Bits& parity) {
             kill(b);
             st.pa.push_back(pa);
             st.pb.push_back(pb);
+            st.spa.push_back({alo, ahi});
+            st.spb.push_back({blo, bhi});
             reclass(a);
             reclass(b);
             touched.for_each_one([&](int k) { reclass(k); });
@@ -424,7 +427,10 @@ Structure eliminate(const std::vector<Bits>& bmat, const Bits& parity) {
         break;
     }
     for (int r = 0; r < m; r++)
-        if (is_alive(r)) st.even.push_back(basis.bits(r, m));
+        if (is_alive(r)) {
+            st.even.push_back(basis.bits(r, m));
+            st.seven.push_back({basis.lo[r], basis.hi[r]});
+        }
     return st;
 }
 
@@ -432,12 +438,15 @@ Structure eliminate(const std::vector<Bits>& bmat, const Bits& parity) {
 // zero diagonal, a few entries per row) counts every pair {j, k} of p's bits with B_jk = 1
 // twice; its half is summed over the upper adjacency lists (neighbours k > j): O(|p| deg / 2)
 // bit tests instead of |p| row-wide popcounts.
-static unsigned z4_value(const std::vector<std::vector<int>>& upper, const Bits& v0, const Bits& v1, const Bits& p) {
-    unsigned lin = p.and_count(v0) + 2 * p.and_count(v1);
-    unsigned half = 0;
-    p.for_each_one([&](int j) {
-        for (int k : upper[(size_t)j]) half += p.get(k) ? 1u : 0u;
-    });
+static unsigned z4_value(const std::vector<std::vector<int>>& upper, const Bits& v0, const Bits& v1, const Bits& p,
+                         std::pair<int, int> span) {
+    unsigned lin = 0, half = 0;
+    for (int q = span.first; q < span.second; q++) {
+        const uint64_t x = p.w[(size_t)q];
+        lin += (unsigned)__builtin_popcountll(x & v0.w[(size_t)q]) + 2u * (unsigned)__builtin_popcountll(x & v1.w[(size_t)q]);
+        for (uint64_t r = x; r; r &= r - 1)
+            for (int k : upper[(size_t)(q * 64 + __builtin_ctzll(r))]) half += p.get(k) ? 1u : 0u;
+    }
     return (lin + 2 * (half & 1)) & 3u;
 }
 
@@ -503,16 +512,18 @@ std::unique_ptr<HostEngine> build_engine(const PathSum& ps, const std::vector<in
     int ncol = 0;
     for (int i = 0; i < m; i++) if (needed[i]) colpos[i] = ncol++;
     std::vector<uint64_t> cols((size_t)ncol * std::max(1, W), 0ull);
-    auto scan = [&](const std::vector<Bits>& vecs, int off) {
+    auto scan = [&](const std::vector<Bits>& vecs, const std::vector<std::pair<int, int>>& span, int off) {
         for (size_t l = 0; l < vecs.size(); l++)
-            vecs[l].for_each_one([&](int j) {
-                if (colpos[j] >= 0) cols[(size_t)colpos[j] * W + off + (l >> 6)] |= 1ull << (l & 63);
-            });
+            for (int q = span[l].first; q < span[l].second; q++)
+                for (uint64_t x = vecs[l].w[(size_t)q]; x; x &= x - 1) {
+                    const int j = q * 64 + __builtin_ctzll(x);
+                    if (colpos[j] >= 0) cols[(size_t)colpos[j] * W + off + (l >> 6)] |= 1ull << (l & 63);
+                }
     };
-    scan(st.pa, Lo.off_a());
-    scan(st.pb, Lo.off_b());
-    scan(st.odd, Lo.off_o());
-    scan(st.even, Lo.off_e());
+    scan(st.pa, st.spa, Lo.off_a());
+    scan(st.pb, st.spb, Lo.off_b());
+    scan(st.odd, st.sodd, Lo.off_o());
+    scan(st.even, st.seven, Lo.off_e());
     E->ucols.assign((size_t)nf * std::max(1, W), 0ull);
     for (int i = 0; i < nf; i++)
         ps.b[fixed[i]].for_each_one([&](int j) {
@@ -585,15 +596,15 @@ std::unique_ptr<HostEngine> build_engine(const PathSum& ps, const std::vector<in
     Diag& dg = E->dg;
     dg.wa = Bits(Lo.g); dg.wb = Bits(Lo.g); dg.o1 = Bits(Lo.nodd); dg.o3 = Bits(Lo.nodd); dg.we = Bits(Lo.neven);
     for (int j = 0; j < Lo.g; j++) {
-        dg.wa.set(j, z4_value(adj, v0, v1, st.pa[j]) == 2);
-        dg.wb.set(j, z4_value(adj, v0, v1, st.pb[j]) == 2);
+        dg.wa.set(j, z4_value(adj, v0, v1, st.pa[j], st.spa[(size_t)j]) == 2);
+        dg.wb.set(j, z4_value(adj, v0, v1, st.pb[j], st.spb[(size_t)j]) == 2);
     }
     dg.sigma = 0;
     for (int l = 0; l < Lo.nodd; l++) {
-        if (z4_value(adj, v0, v1, st.odd[l]) == 1) { dg.o1.set(l, true); dg.sigma++; }
+        if (z4_value(adj, v0, v1, st.odd[l], st.sodd[(size_t)l]) == 1) { dg.o1.set(l, true); dg.sigma++; }
         else { dg.o3.set(l, true); dg.sigma--; }
     }
-    for (int l = 0; l < Lo.neven; l++) dg.we.set(l, z4_value(adj, v0, v1, st.even[l]) == 2);
+    for (int l = 0; l < Lo.neven; l++) dg.we.set(l, z4_value(adj, v0, v1, st.even[l], st.seven[(size_t)l]) == 2);
     E->sigma = dg.sigma;
     E->mag2 = 2 * Lo.g + 2 * Lo.neven + Lo.nodd;
     // terms (engine.rs:232-238), FP64

@@ -94,6 +94,8 @@ struct PathSum {
 struct Structure {
     int m = 0;
     std::vector<Bits> pa, pb, odd, even;  // basis vectors over the m free variables
+    // words [first, second) outside which each basis vector is zero (same order as above)
+    std::vector<std::pair<int, int>> spa, spb, sodd, seven;
     int g() const { return (int)pa.size(); }
 };
 Structure eliminate(const std::vector<Bits>& b, const Bits& parity);  // MinWeight rule
