@@ -61,7 +61,7 @@ def config(extra=None):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+    """nvidia-smi clocks and throttle reasons sampled every 50 ms while running."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -74,7 +74,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", self.gpu, "--query-gpu=" + self.FIELDS,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -105,7 +105,7 @@ class ClockSampler:
         samples when no window is given or none fell inside it)."""
         sm, mx, reasons = [], [], set()
         names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
-        lines = [ln for t, ln in self.lines if t0 is None or (t0 <= t <= t1 + 0.25)]
+        lines = [ln for t, ln in self.lines if t0 is None or (t0 <= t <= t1 + 0.06)]
         if not lines:
             lines = [ln for _, ln in self.lines]
         for ln in lines:
@@ -267,6 +267,8 @@ def run_gb300(args):
                                        ct.c_void_p(stream.cuda_stream)))
 
     kms = (ct.c_float * 3)()
+    clk = ClockSampler(local).__enter__()
+    clk.wait_first()
     with torch.cuda.stream(stream):
         for _ in range(max(3, args.warmup)):
             step_device()
@@ -274,28 +276,28 @@ def run_gb300(args):
         # work of one step: branches enumerated (vanishing pairs excluded) and reference-form ops
         branches_step, ops_step, popc_step, logic_step, per_boundary = enumerated(L, N, sim, n)
         peaks = (ct.c_double * 4)()
+        tp0 = time.perf_counter()
         N.check(L.pq_measure_peaks(peaks))
+        peak_clocks = clk.summary(tp0, time.perf_counter())
         if dist:
             dist.barrier()
         torch.cuda.synchronize()
         step_ms, enum_ms = [], []
-        with ClockSampler(local) as clk:
-            clk.wait_first()
-            t_wall0 = time.perf_counter()
-            for _ in range(args.steps):
-                flush.zero_()
-                e0 = torch.cuda.Event(enable_timing=True)
-                e1 = torch.cuda.Event(enable_timing=True)
-                e0.record(stream)
-                step_device()
-                e1.record(stream)
-                e1.synchronize()
-                step_ms.append(e0.elapsed_time(e1))
-                N.check(L.pq_sim_kernel_ms(sim.handle, n, kms))
-                enum_ms.append(kms[1])
-            torch.cuda.synchronize()
-            t_wall1 = time.perf_counter()
-            t_wall = t_wall1 - t_wall0
+        t_wall0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step_device()
+            e1.record(stream)
+            e1.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+            N.check(L.pq_sim_kernel_ms(sim.handle, n, kms))
+            enum_ms.append(kms[1])
+        torch.cuda.synchronize()
+        t_wall1 = time.perf_counter()
+        t_wall = t_wall1 - t_wall0
         clocks = clk.summary(t_wall0, t_wall1)
         ms = sum(step_ms) / len(step_ms)
         ms = max_over_ranks(dist, ms)
@@ -313,6 +315,7 @@ def run_gb300(args):
     err_h = np.zeros(n)
     import ctypes
     P = lambda a, t: a.ctypes.data_as(ctypes.POINTER(t))  # noqa: E731
+    t_e2e0 = time.perf_counter()
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
@@ -320,6 +323,7 @@ def run_gb300(args):
         N.check(L.pq_amplitudes(sim.handle, n, P(xs_h, ct.c_uint64), P(ys_h, ct.c_uint64), P(out_h, ct.c_double),
                                 P(err_h, ct.c_double)))
         e2e_s.append(time.perf_counter() - t0)
+    e2e_clocks = clk.summary(t_e2e0, time.perf_counter())
     e2e_ms = 1e3 * sum(e2e_s) / len(e2e_s)
     e2e_ms = max_over_ranks(dist, e2e_ms)
     e2e_value = replica_rate(ws, branches_step, e2e_ms)
@@ -328,6 +332,8 @@ def run_gb300(args):
     # shared by the chunks of a unit.  Peak: the measured fma.f32 rate of this device.
     enum_avg = sum(enum_ms) / len(enum_ms)
     lop3, popcr, fmar = peaks[0], peaks[1], peaks[2]
+    # nominal FP32 FMA rate: 128 FP32 lanes per SM at the maximum SM clock (2070 MHz)
+    fma_nominal = peaks[3] * 128 * 2.07e9
     fma_step = FMA_OPS_PER_BRANCH * branches_step
     achieved = fma_step / (enum_avg * 1e-3)
     # the reference engine's form of the same work: 5 W_o + 6 W_g int64 ops per branch, 2 popc.b32
@@ -359,7 +365,7 @@ def run_gb300(args):
                           "tuning_source": "fixed" if args.no_autotune else "pq_sim_autotune (%.1f s)" % tune_s}),
         "precision": {"max_rel_err_vs_fp64": float(np.max(rel)), "median_rel_err_vs_fp64": float(np.median(rel)),
                       "max_errbound_rel": float(np.max(errb / np.abs(ref)))},
-        "e2e": {"value": e2e_value, "unit": "branches/s", "ms_per_step": e2e_ms,
+        "e2e": {"value": e2e_value, "unit": "branches/s", "ms_per_step": e2e_ms, "clocks": e2e_clocks,
                 "h2d_bytes_per_step": int(xs_h.nbytes + ys_h.nbytes),
                 "d2h_bytes_per_step": int(out_h.nbytes + err_h.nbytes + 4)},
         "gpu_launches": 4 * args.steps,
@@ -368,6 +374,9 @@ def run_gb300(args):
                      "kernel": "enum_kernel", "kernel_ms": enum_avg,
                      "ops": "%d FP32 FMA-pipe ops per enumerated branch" % FMA_OPS_PER_BRANCH,
                      "peak_source": "measured fma.f32 rate on this device (pq_measure_peaks), not a vendor figure",
+                     "peak_sm_mhz": peak_clocks.get("sm_mhz"),
+                     "peak_nominal": fma_nominal / 1e12, "frac_of_nominal": achieved / fma_nominal,
+                     "peak_nominal_source": "%d SMs x 128 FP32 lanes x 2070 MHz" % int(peaks[3]),
                      "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one full-size launch, "
                                        "ncu capture in profiles/enum_kernel_many_boundaries.md",
                      "reference_form": {
@@ -384,6 +393,13 @@ def run_gb300(args):
                                     "figures describe the enumeration and do not apply to this line")
     if cpu:
         line["cpu_baseline"] = cpu
+    if rank == 0 and ws == 1 and not args.headline_only:
+        # the other configurations, measured in the same run: the small single amplitude, the
+        # uneven batch against its plain paths, the served Poisson stream
+        line["cfg1_small"] = leg_small(args, clk)
+        line["cfg3_batched"] = leg_batched(args, clk, cpu=not args.no_cpu)
+        line["cfg5_serve"] = leg_serve(args, clk)
+    clk.__exit__(None, None, None)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
@@ -406,7 +422,48 @@ def _gpu_setup():
     return pq, N
 
 
-def run_batched(args):
+def _bucket(d):
+    return "d<=12" if d <= 12 else ("d13-18" if d <= 18 else "d>=19")
+
+
+def cpu_batched_buckets(circs, outs, enum_per_circuit, threads, budget_s=4.0):
+    """CPU restatement on the uneven batch, per branch-dimension bucket: each bucket's
+    circuits are evaluated in order (all 64 boundaries for d <= 18, 2 boundaries above) until
+    `budget_s` of CPU time is spent; the bucket's remaining circuits are charged their
+    enumerated branches (the same (boundary, engine) pairs the device enumerates) at the
+    bucket's measured branch rate.  Returns {bucket: {...}}."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    by = {}
+    for i, ((c, d), o) in enumerate(zip(circs, outs)):
+        by.setdefault(_bucket(d), []).append(i)
+    res = {}
+    for key, idx in sorted(by.items()):
+        spent, measured, br_meas = 0.0, {}, 0.0
+        for i in idx:
+            if spent >= budget_s:
+                break
+            c, d = circs[i]
+            k = 64 if d <= 18 else 2
+            r = oracle.OracleSim(c, "auto")
+            t0 = time.perf_counter()
+            r.amplitudes([0] * k, outs[i][:k], nthreads=threads)
+            dt = time.perf_counter() - t0
+            spent += dt
+            measured[i] = dt * 64.0 / k
+            br_meas += r.last_branches() * 64.0 / k
+        rate = br_meas / sum(measured.values()) if measured and sum(measured.values()) > 0 else None
+        total = sum(measured.values())
+        for i in idx:
+            if i not in measured and rate:
+                total += enum_per_circuit[i] / rate
+        res[key] = {"circuits": len(idx), "measured_circuits": len(measured),
+                    "cpu_amps_per_s": 64.0 * len(idx) / total if total > 0 else None,
+                    "cpu_branches_per_s": rate, "cpu_seconds_for_bucket": total}
+    return res
+
+
+def leg_batched(args, clk=None, cpu=True):
     """Uneven batch: 256 circuits (n ~ U[16,64], 40n gates, T ~ U[8,36]), 64 uniform y each,
     one persistent graph launch per step vs the plain per-circuit and per-boundary paths."""
     import ctypes as ct
@@ -415,6 +472,7 @@ def run_batched(args):
     import torch
 
     pq, N = _gpu_setup()
+    L = N.lib()
     from polyq_gb300.rng import random_outputs, workload_batch
     t0 = time.perf_counter()
     circs = workload_batch(256, seed=3)
@@ -436,12 +494,16 @@ def run_batched(args):
     dout = torch.zeros(2 * n, dtype=torch.float64, device="cuda")
     stream = torch.cuda.Stream()
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    steps = max(1, args.batch_steps)
     with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
+        for _ in range(max(3, args.warmup)):
             b.run_device(ct.c_void_p(dx.data_ptr()), ct.c_void_p(dy.data_ptr()), ct.c_void_p(dout.data_ptr()),
                          None, ct.c_void_p(stream.cuda_stream))
-        ms = []
-        for _ in range(args.steps):
+        torch.cuda.synchronize()
+        ms, enum_ms = [], []
+        kms = (ct.c_float * 3)()
+        tw0 = time.perf_counter()
+        for _ in range(steps):
             flush.zero_()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
@@ -450,74 +512,89 @@ def run_batched(args):
             e1.record(stream)
             e1.synchronize()
             ms.append(e0.elapsed_time(e1))
+            N.check(L.pq_batch_kernel_ms(b._h, kms))
+            enum_ms.append(kms[1])
+        tw1 = time.perf_counter()
     batched_ms = sum(ms) / len(ms)
-    import ctypes as _ct
-    kms = (_ct.c_float * 3)()
-    N.check(N.lib().pq_batch_kernel_ms(b._h, kms))
-    benum = (_ct.c_double * 4)()
-    N.check(N.lib().pq_batch_enumerated(b._h, benum))
+    enum_avg = sum(enum_ms) / len(enum_ms)
+    benum = (ct.c_double * 4)()
+    N.check(L.pq_batch_enumerated(b._h, benum))
     got = dout.cpu().numpy().view(np.complex128)
     # plain path 1: one launch per circuit (its 64 boundaries), host buffers, sequential
     for s, o in zip(sims, outs):
         s.amplitudes([0] * 64, o)  # plans and graphs built outside the timing
-    per_circ = []
-    same = True
-    plain_amps = []
-    t0 = time.perf_counter()
-    for i, (s, o) in enumerate(zip(sims, outs)):
+    per_circ, plain_amps = [], []
+    tp0 = time.perf_counter()
+    for s, o in zip(sims, outs):
         t1 = time.perf_counter()
-        a = s.amplitudes([0] * 64, o)
+        plain_amps.append(s.amplitudes([0] * 64, o))
         per_circ.append(time.perf_counter() - t1)
-        plain_amps.append(a)
-    plain_circ_s = time.perf_counter() - t0
+    plain_circ_s = time.perf_counter() - tp0
     plain_all = np.concatenate(plain_amps)
     same = bool(np.array_equal(plain_all, got))
     scale = np.maximum(np.abs(plain_all), 1e-300)
     max_rel_diff = float(np.max(np.abs(plain_all - got) / scale))
+    enum_circ = [enumerated(L, N, s, 64)[0] for s in sims]
     # plain path 2: one launch per (circuit, boundary)
     for s, o in zip(sims, outs):
         s.amplitudes_plain([0], o[:1])
-    t0 = time.perf_counter()
+    tb0 = time.perf_counter()
     for s, o in zip(sims, outs):
         s.amplitudes_plain([0] * 64, o)
-    plain_bnd_s = time.perf_counter() - t0
+    plain_bnd_s = time.perf_counter() - tb0
     buckets = {}
     for s, t in zip(sims, per_circ):
-        d = s.stats_full()["branch_dim"]
-        key = "d<=12" if d <= 12 else ("d13-18" if d <= 18 else "d>=19")
-        bk = buckets.setdefault(key, [0, 0.0])
+        bk = buckets.setdefault(_bucket(s.stats_full()["branch_dim"]), [0, 0.0])
         bk[0] += 64
         bk[1] += t
-    line = {"metric": METRIC, "workload": "batched", "value": n / (batched_ms * 1e-3), "unit": "amplitudes/s",
-            "branches_per_s": benum[0] / (batched_ms * 1e-3), "ms_per_step": batched_ms, "steps": args.steps,
-            "warmup": args.warmup, "n_gpus": 1, "higher_is_better": True, "data": "synthetic",
-            "plain_per_circuit_amps_per_s": n / plain_circ_s, "plain_per_boundary_amps_per_s": n / plain_bnd_s,
-            "speedup_vs_plain_per_circuit": plain_circ_s / (batched_ms * 1e-3),
-            "speedup_vs_plain_per_boundary": plain_bnd_s / (batched_ms * 1e-3),
-            "batched_equals_per_circuit_bitwise": bool(same),
-            "batched_vs_per_circuit_max_rel_diff": max_rel_diff,
-            "kernel_ms_last_step": {"prepare": kms[0], "enumerate": kms[1], "reduce": kms[2]},
-            "per_d_bucket_amps_per_s_plain": {k: v[0] / v[1] for k, v in buckets.items()},
-            "config": {"workload": "256 circuits, n~U[16,64], 40n gates, T~U[8,36] (seed 3), 64 uniform y each, "
-                                   "strategy auto", "branches_enumerated_per_step": benum[0],
-                       "branches_all_engines_per_step": b.branches, "host_build_s": build_s,
-                       "l2": "flushed between steps", "tuning": tuning,
-                       "tuning_source": "fixed" if tuning is None else "pq_batch_autotune (%.1f s)" % t_tune}}
+    peaks = (ct.c_double * 4)()
+    N.check(L.pq_measure_peaks(peaks))
+    achieved = FMA_OPS_PER_BRANCH * benum[0] / (enum_avg * 1e-3)
+    leg = {"value": n / (batched_ms * 1e-3), "unit": "amplitudes/s",
+           "branches_per_s": benum[0] / (batched_ms * 1e-3), "ms_per_step": batched_ms, "steps": steps,
+           "plain_per_circuit_amps_per_s": n / plain_circ_s, "plain_per_boundary_amps_per_s": n / plain_bnd_s,
+           "speedup_vs_plain_per_circuit": plain_circ_s / (batched_ms * 1e-3),
+           "speedup_vs_plain_per_boundary": plain_bnd_s / (batched_ms * 1e-3),
+           "batched_equals_per_circuit_bitwise": same, "batched_vs_per_circuit_max_rel_diff": max_rel_diff,
+           "enum_kernel_ms": enum_avg,
+           "fma_pipe_frac_of_measured": achieved / peaks[2],
+           "per_d_bucket_amps_per_s_plain_per_circuit": {k: v[0] / v[1] for k, v in sorted(buckets.items())},
+           "config": {"workload": "256 circuits, n~U[16,64], 40n gates, T~U[8,36] (seed 3), 64 uniform y each, "
+                                  "x=0, strategy auto", "branches_enumerated_per_step": benum[0],
+                      "branches_all_engines_per_step": b.branches, "host_build_s": build_s,
+                      "l2": "flushed between steps (512 MiB write)", "tuning": tuning,
+                      "tuning_source": "fixed" if tuning is None else "pq_batch_autotune (%.1f s)" % t_tune}}
+    if clk is not None:
+        leg["clocks"] = clk.summary(tw0, tw1)
+        leg["clocks_plain_per_circuit"] = clk.summary(tp0, tp0 + plain_circ_s)
+    if cpu:
+        cb = cpu_batched_buckets(circs, outs, enum_circ, cpu_threads())
+        tot = sum(v["cpu_seconds_for_bucket"] for v in cb.values())
+        leg["cpu_baseline"] = {"value": n / tot, "unit": "amplitudes/s", "cores": cpu_threads(), "kind": "port",
+                               "per_d_bucket": cb,
+                               "sample": "per bucket, circuits in order until 4 s of CPU time (all 64 boundaries "
+                                         "for d <= 18, 2 above); the rest charged their enumerated branches at "
+                                         "the bucket's measured rate"}
+    return leg
+
+
+def run_batched(args):
+    leg = leg_batched(args, cpu=not args.no_cpu)
+    line = {"metric": METRIC, "workload": "batched", "n_gpus": 1, "higher_is_better": True, "data": "synthetic",
+            "warmup": args.warmup, **leg}
     print(json.dumps(line), flush=True)
     return 0
 
 
-def run_serve(args):
+def leg_serve(args, clk=None):
     """Poisson stream of amplitude / probability / single-qubit-marginal requests against 64
     resident circuits (n~U[16,64], 40n gates, T~U[8,40]); throughput and p50/p99 latency at the
     offered load and below saturation, beside plain per-request launches."""
     import random
 
-    import numpy as np
-
     pq, N = _gpu_setup()
     from polyq_gb300.rng import random_outputs, workload_batch
-    from polyq_gb300.serve import AMPLITUDE, MARGINAL, Server
+    from polyq_gb300.serve import MARGINAL, Server
     circs = [c for c, _ in workload_batch(64, seed=5, t_max=40)]
     sims = [pq.Simulator(c) for c in circs]
     srv = Server(sims, max_slots=args.slots, mem_budget_bytes=8 << 30, max_branch_dim=args.max_d)
@@ -544,6 +621,7 @@ def run_serve(args):
             arrivals.append(t)
         reqs = [make(i) for i in range(nreq)]
         start = time.monotonic()
+        w0 = time.perf_counter()
         i = 0
         while i < nreq:
             now = time.monotonic() - start
@@ -556,17 +634,22 @@ def run_serve(args):
             else:
                 time.sleep(max(0.0, min(0.0005, arrivals[i] - now)))
         res = srv.collect(nreq, 600)
+        w1 = time.perf_counter()
         ok = [r for r in res if r["status"] == 0]
         lat = [r["done_s"] - r["submit_s"] for r in ok]
         span = (max(r["done_s"] for r in ok) - min(r["submit_s"] for r in ok)) if ok else 0.0
         okt = set(r["tag"] for r in ok)
-        return {"offered_per_s": rate, "requests": nreq, "completed": len(ok),
-                "refused": sum(1 for r in res if r["status"] == 3), "other_errors": sum(1 for r in res if r["status"] not in (0, 3)),
-                "throughput_per_s": len(ok) / span if span > 0 else None,
-                "evaluated_at_level": {name: sum(1 for r in ok if r["level"] == lv)
-                                       for lv, name in enumerate(("fp32_walk", "chunk_tables", "fp64_walk"))},
-                "p50_ms": 1e3 * _pct(lat, 0.5) if lat else None,
-                "p99_ms": 1e3 * _pct(lat, 0.99) if lat else None}, [q for q in reqs if q["tag"] in okt]
+        out = {"offered_per_s": rate, "requests": nreq, "completed": len(ok),
+               "refused": sum(1 for r in res if r["status"] == 3),
+               "other_errors": sum(1 for r in res if r["status"] not in (0, 3)),
+               "throughput_per_s": len(ok) / span if span > 0 else None,
+               "evaluated_at_level": {name: sum(1 for r in ok if r["level"] == lv)
+                                      for lv, name in enumerate(("fp32_walk", "chunk_tables", "fp64_walk"))},
+               "p50_ms": 1e3 * _pct(lat, 0.5) if lat else None,
+               "p99_ms": 1e3 * _pct(lat, 0.99) if lat else None}
+        if clk is not None:
+            out["clocks"] = clk.summary(w0, w1)
+        return out, [q for q in reqs if q["tag"] in okt]
 
     full, served = load(args.rate, args.duration)
     cap = full["throughput_per_s"] or args.rate
@@ -597,24 +680,27 @@ def run_serve(args):
             continue
         lat.append(time.perf_counter() - t1)
     plain = {"requests": len(reqs), "completed": len(lat), "throughput_per_s": len(lat) / (time.perf_counter() - t0),
-             "p50_ms": 1e3 * _pct(lat, 0.5), "p99_ms": 1e3 * _pct(lat, 0.99)}
+             "p50_ms": 1e3 * _pct(lat, 0.5) if lat else None, "p99_ms": 1e3 * _pct(lat, 0.99) if lat else None}
     srv.close()
-    line = {"metric": METRIC, "workload": "serve", "value": full["throughput_per_s"], "unit": "requests/s",
-            "at_offered_load": full, "sub_saturation": sub, "saturated": sat, "plain_per_request": plain,
-            "n_gpus": 1,
-            "data": "synthetic",
-            "config": {"workload": "64 resident circuits n~U[16,64], 40n gates, T~U[8,40] (seed 5); Poisson arrivals; "
-                                   "amplitude/probability/marginal 1:1:1; marginals on one of the first 4 qubits",
-                       "max_slots": args.slots, "max_branch_dim": args.max_d, "duration_s": args.duration}}
+    return {"value": full["throughput_per_s"], "unit": "requests/s", "at_offered_load": full,
+            "sub_saturation": sub, "saturated": sat, "plain_per_request": plain,
+            "config": {"workload": "64 resident circuits n~U[16,64], 40n gates, T~U[8,40] (seed 5); Poisson "
+                                   "arrivals; amplitude/probability/marginal 1:1:1; marginals on one of the first "
+                                   "4 qubits", "max_slots": args.slots, "max_branch_dim": args.max_d,
+                       "duration_s": args.duration}}
+
+
+def run_serve(args):
+    leg = leg_serve(args)
+    line = {"metric": METRIC, "workload": "serve", "n_gpus": 1, "data": "synthetic", **leg}
     print(json.dumps(line), flush=True)
     return 0
 
 
-def run_small(args):
+def leg_small(args, clk=None, cpu_runs=200):
     """One amplitude <0|C|0> and its probability: n=20, 200 gates, 16 T (seed 2, the first seed
-    whose <0|C|0> is non-zero)."""
-    import numpy as np
-
+    whose <0|C|0> is non-zero), per call through the public host-buffer API, beside the CPU
+    restatement's median over `cpu_runs` calls."""
     pq, N = _gpu_setup()
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle
@@ -625,7 +711,9 @@ def run_small(args):
     build = time.perf_counter() - t0
     for _ in range(20):
         sim.amplitudes([0], [0])
+        sim.probability(0, 0)
     lat, plat = [], []
+    w0 = time.perf_counter()
     for _ in range(200):
         t1 = time.perf_counter()
         a = sim.amplitudes([0], [0])[0]
@@ -633,14 +721,34 @@ def run_small(args):
         t1 = time.perf_counter()
         p = sim.probability(0, 0)
         plat.append(time.perf_counter() - t1)
-    ref = oracle.OracleSim(c).amplitude(0, 0)
+    w1 = time.perf_counter()
+    ref = oracle.OracleSim(c)
+    # the reference evaluates a subspace of d < 16 on the calling thread (src/engine.rs:688)
+    ref.amplitudes([0], [0], nthreads=1)
+    cpu = []
+    for _ in range(cpu_runs):
+        t1 = time.perf_counter()
+        want = ref.amplitudes([0], [0], nthreads=1)[0]
+        cpu.append(time.perf_counter() - t1)
     dense = oracle.dense_statevector(c, 0)[0]
-    line = {"metric": METRIC, "workload": "small", "value": 1.0 / _pct(lat, 0.5), "unit": "amplitudes/s (serial)",
-            "amplitude": [a.real, a.imag], "probability": p, "p50_ms": 1e3 * _pct(lat, 0.5),
-            "p99_ms": 1e3 * _pct(lat, 0.99), "probability_p50_ms": 1e3 * _pct(plat, 0.5),
-            "abs_err_vs_fp64_oracle": abs(a - ref), "abs_err_vs_dense": abs(a - dense),
-            "prob_abs_err_vs_dense": abs(p - abs(dense) ** 2), "build_s": build, "stats": sim.stats_full(),
-            "config": {"workload": "n=20, 200 gates, 16 T (seed 2), <0|C|0>"}}
+    leg = {"value": 1.0 / _pct(lat, 0.5), "unit": "amplitudes/s (serial calls)",
+           "amplitude": [a.real, a.imag], "probability": p, "p50_ms": 1e3 * _pct(lat, 0.5),
+           "p99_ms": 1e3 * _pct(lat, 0.99), "probability_p50_ms": 1e3 * _pct(plat, 0.5),
+           "abs_err_vs_fp64_oracle": abs(a - want), "abs_err_vs_dense": abs(a - dense),
+           "prob_abs_err_vs_dense": abs(p - abs(dense) ** 2), "build_s": build, "stats": sim.stats_full(),
+           "cpu_baseline": {"p50_ms": 1e3 * _pct(cpu, 0.5), "p99_ms": 1e3 * _pct(cpu, 0.99), "runs": cpu_runs,
+                            "cores": 1, "kind": "port", "unit": "ms per amplitude call",
+                            "sample": "the same amplitude, %d calls, one thread" % cpu_runs},
+           "gpu_p50_over_cpu_p50": _pct(lat, 0.5) / _pct(cpu, 0.5),
+           "config": {"workload": "n=20, 200 gates, 16 T (seed 2), <0|C|0>, FP64 complex output"}}
+    if clk is not None:
+        leg["clocks"] = clk.summary(w0, w1)
+    return leg
+
+
+def run_small(args):
+    leg = leg_small(args)
+    line = {"metric": METRIC, "workload": "small", "n_gpus": 1, "data": "synthetic", **leg}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -790,6 +898,9 @@ def main():
     ap.add_argument("--duration", type=float, default=2.0, help="serve: seconds of arrivals")
     ap.add_argument("--slots", type=int, default=256, help="serve: requests per wave")
     ap.add_argument("--max-d", type=int, default=28, help="serve: log2 cap on a request's branches")
+    ap.add_argument("--batch-steps", type=int, default=20, help="batched: timed launches")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="default workload only (no small / batched / serving legs)")
     args = ap.parse_args()
     WORKLOAD["boundaries"] = args.boundaries
     if args.warmup < 3:

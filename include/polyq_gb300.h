@@ -142,21 +142,31 @@ PQ_API pq_status pq_sample_many(pq_sim *sim, const uint64_t *x, int64_t shots, u
  * stream) without a host synchronisation. */
 PQ_API pq_status pq_amplitudes_device(pq_sim *sim, int64_t n, const uint64_t *x, const uint64_t *y, double *out,
                                       double *errbound, void *stream);
+/* Device self-check of the last launch of the simulator's size-n plan (pq_amplitudes_device,
+ * and every host-buffer call of that size): waits for it, then *failed = 1 if its prepare kernel
+ * saw an odd Z8 increment -- impossible for a correct closed form; its results are then NaN --
+ * else 0.  The host-buffer calls check this themselves and return PQ_ERR_INTERNAL. */
+PQ_API pq_status pq_sim_device_check(pq_sim *sim, int64_t n, int32_t *failed);
 /* Same evaluation split into one launch sequence per boundary (the plain one-circuit,
  * one-boundary-per-launch path, kept as the comparison baseline for batching). */
 PQ_API pq_status pq_amplitudes_plain(pq_sim *sim, int64_t n, const uint64_t *x, const uint64_t *y, double *out);
 
 /* Allocation-free amplitudes (no counterpart in the reference crate).  For callers that may
- * not allocate device memory when they need results -- code inside CUDA graph capture, hosts
- * under an externally enforced device-memory budget, callbacks that forbid allocation.
- * x, y (n bitstrings each) and out (2n doubles) are DEVICE pointers owned by the caller; the
- * work is enqueued on `stream` (NULL = legacy default stream) and not waited for.  Per-call
- * state lives in one fixed 1.7 MiB static device array: n x (branch engines) <= 4096, at most
- * 64 branch engines and 65536 work items, else PQ_ERR_INVALID_ARG.  The first call on a
- * device looks up that array's address, so make one call before any stream capture.  Calls
- * share the array: calls that overlap on the GPU race, serialise them. */
+ * not allocate device memory when they need results: hosts whose device memory belongs to an
+ * outer allocator with a fixed budget (a framework's caching allocator, a server that reserved
+ * its memory up front), and plugin or callback code running where an allocation would block,
+ * fragment the caller's pool or fail.  x, y (n bitstrings each), out (2n doubles) and errbound
+ * (optional, n doubles, NULL = not wanted) are DEVICE pointers owned by the caller; the work is
+ * enqueued on `stream` (NULL = legacy default stream) and not waited for.  It runs on the
+ * structures uploaded by pq_sim_create and, for all per-call state, one fixed 1.6 MiB static
+ * device array: n x (branch engines) <= 4096 and at most 65536 work items, else
+ * PQ_ERR_INVALID_ARG.  The results are those of pq_amplitudes_device at the simulator's launch
+ * shape (same per-job work decomposition and summation order); a failed device self-check
+ * shows as NaN in out and errbound.  The first call on a device looks up that array's address,
+ * so make one call before any stream capture.  Calls share the array, which keeps the last
+ * call's contents: calls that overlap on the GPU race, serialise them. */
 PQ_API pq_status pq_amplitudes_noalloc(pq_sim *sim, int64_t n, const uint64_t *x, const uint64_t *y, double *out,
-                                       void *stream);
+                                       double *errbound, void *stream);
 
 /* ---- batched multi-circuit launch (one persistent, graph-captured launch) ------------ */
 /* Amplitudes of counts[i] boundaries on sims[i], all i, in one CUDA-graph launch of a
@@ -260,6 +270,14 @@ PQ_API pq_status pq_debug_engine_shape(const pq_sim *sim, int32_t branch, int64_
  * or -2 (error). */
 PQ_API int32_t pq_debug_branch_phases(pq_sim *sim, int32_t branch, const uint64_t *x, const uint64_t *y,
                                       uint8_t *out);
+/* Engine::prepare (src/engine.rs:569-610, Elim::solve_into :188-201) as the device's prepare
+ * kernel computes it, for n boundaries x every branch engine (boundary-major), 12 uint64 words
+ * per job: [0] 1 if the job vanishes (contradictory boundary, zero engine or inconsistent
+ * radical system; the other words are then 0), [1] the constant phase (uint32 ring units),
+ * [2] k0 = the Z8 index at the start shift (src/normal_form.rs:479-493), [3] the particular
+ * solution's pivot bits y0 (pivots in elimination order), [4..11] the Z4 increments Lp_j of the
+ * kernel coordinates j < min(d, 64) as bytes, in the reference's coordinate order. */
+PQ_API pq_status pq_debug_prepare(pq_sim *sim, int64_t n, const uint64_t *x, const uint64_t *y, uint64_t *out);
 /* Same amplitudes as pq_amplitudes with FP64 branch weights and FP64 accumulation on the
  * device (verification mode). */
 PQ_API pq_status pq_amplitudes_fp64(pq_sim *sim, int64_t n, const uint64_t *x, const uint64_t *y, double *out);

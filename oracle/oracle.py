@@ -71,6 +71,9 @@ def lib():
             L.pqo_engine_dump.argtypes = [P, ct.c_int, u64p, ct.c_int64]
             L.pqo_branch_phases.restype = ct.c_int
             L.pqo_branch_phases.argtypes = [P, ct.c_int, u64p, u64p, u8p]
+            L.pqo_branch_dim.restype = ct.c_int
+            L.pqo_branch_dim.argtypes = [P, ct.c_int]
+            L.pqo_prepare_info.argtypes = [P, ct.c_int, u64p, u64p, u64p]
             L.pqo_check_structure.restype = ct.c_int
             L.pqo_check_structure.argtypes = [ct.c_int, u8p, u8p, ct.c_int, i32p]
             L.pqo_gauss_sum.argtypes = [ct.c_int, u8p, u8p, u8p, ct.c_int, f64p, f64p]
@@ -106,6 +109,7 @@ def pack_bits(values, nq):
 
 
 STRATEGY = {"auto": 0, "cached": 1, "pairs": 2}
+PREP_WORDS = 12  # u64 words per job of prepare_info (PQO_PREP_WORDS)
 
 
 class OracleSim:
@@ -207,9 +211,27 @@ class OracleSim:
         self.L.pqo_engine_dump(self.h, branch, _ptr(out, ct.c_uint64), n)
         return out[:n]
 
+    def branch_dim(self, branch=0):
+        """Dimension d of branch engine `branch`'s affine branch subspace."""
+        d = int(self.L.pqo_branch_dim(self.h, branch))
+        if d < 0:
+            raise ValueError("no branch engine %d" % branch)
+        return d
+
+    def prepare_info(self, xs, ys):
+        """Engine::prepare integers (src/engine.rs:569-610) of every (boundary, branch engine)
+        job, boundary-major: an (n, branches, PREP_WORDS) uint64 array -- vanish flag, constant
+        phase, k0, pivot bits y0, then the Z4 increments Lp_j as bytes (0xFF: odd)."""
+        xs = pack_bits(xs, self.nq)
+        ys = pack_bits(ys, self.nq)
+        n = xs.shape[0]
+        nb = self.stats()["branches"]
+        out = np.zeros((max(n, 1), nb, PREP_WORDS), dtype=np.uint64)
+        self.L.pqo_prepare_info(self.h, n, _ptr(xs, ct.c_uint64), _ptr(ys, ct.c_uint64), _ptr(out, ct.c_uint64))
+        return out[:n]
+
     def branch_phases(self, x, y, branch=0):
-        st = self.stats()
-        d = st["branch_dim"]
+        d = self.branch_dim(branch)
         if d > 24:
             raise ValueError("d too large")
         xs = pack_bits([x], self.nq)

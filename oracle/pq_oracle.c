@@ -1584,16 +1584,80 @@ int pqo_branch_phases(pqo_sim *s, int br, const uint64_t *x, const uint64_t *y, 
     int ok = engine_prepare(E, vals, &p);
     int d = E->el.d;
     if (ok) {
+        /* the kernel points in Gray order (engine.rs:696-722 walks them the same way): point
+         * s = i ^ (i >> 1) differs from the previous one in kernel column ctz(i) */
         uvec u; uv_init(&u, &E->st);
-        for (uint64_t sidx = 0; sidx < (1ull << d); sidx++) {
-            uv_copy(&u, &p.u);
-            for (int j = 0; j < d; j++) if ((sidx >> j) & 1) uv_xor(&u, &E->el.kernel_u[j]);
-            out[sidx] = (uint8_t)phase8(&E->dg, &u);
+        uv_copy(&u, &p.u);
+        out[0] = (uint8_t)phase8(&E->dg, &u);
+        for (uint64_t i = 1; i < (1ull << d); i++) {
+            uv_xor(&u, &E->el.kernel_u[__builtin_ctzll(i)]);
+            out[i ^ (i >> 1)] = (uint8_t)phase8(&E->dg, &u);
         }
         uv_free(&u);
     }
     prep_free(&p); free(vals); free(a);
     return ok ? d : -1;
+}
+
+/* Branch dimension d of branch engine `br` (-1 out of range). */
+int pqo_branch_dim(const pqo_sim *s, int br) {
+    if (br < 0 || br >= s->eng.nbr) return -1;
+    return s->eng.br[br]->el.d;
+}
+
+/*
+ * Integers of Engine::prepare (engine.rs:569-610, Elim::solve_into :188-201) for every
+ * (boundary, branch engine) job, boundary-major: PQO_PREP_WORDS u64 words per job,
+ *   [0] 1 if the job vanishes (contradictory boundary, sim.rs:172-174; zero engine, :570;
+ *       inconsistent radical system, :595-597), else 0 -- the other words are 0 then
+ *   [1] the constant phase (u32 ring units: global + fixed thetas + Z4 fixed terms, :575-588)
+ *   [2] k0 = phase8 of the start shift u (normal_form.rs:479-493)
+ *   [3] y0: bit i = the particular solution s0 at pivot column i (pivots in Elim order)
+ *   [4..11] Lp_j = (phase8(u ^ kernel_u[j]) - k0) / 2 mod 4 as bytes, j < min(d, 64);
+ *       an odd increment is recorded as 0xFF (the closed form has only even ones)
+ */
+void pqo_prepare_info(pqo_sim *s, int n, const uint64_t *xs, const uint64_t *ys, uint64_t *out) {
+    int nw = (s->ps.nq + 63) / 64;
+    if (nw == 0) nw = 1;
+    const int nb = s->eng.nbr;
+    asg_t *a = (asg_t *)malloc(sizeof(asg_t) * (size_t)(2 * s->ps.nq + 1));
+    for (int i = 0; i < n; i++) {
+        int na = ps_boundary(&s->ps, xs + (size_t)i * nw, ys + (size_t)i * nw, a);
+        for (int b = 0; b < nb; b++) {
+            uint64_t *rec = out + ((size_t)i * nb + b) * PQO_PREP_WORDS;
+            memset(rec, 0, sizeof(uint64_t) * PQO_PREP_WORDS);
+            const engine *E = s->eng.br[b];
+            int ok = 0;
+            prep_t p; prep_init(&p, E);
+            if (na >= 0) {
+                uint8_t *vals = (uint8_t *)malloc((size_t)E->nf + 1);
+                values_from_asg(E, a, na, vals);
+                ok = engine_prepare(E, vals, &p);
+                free(vals);
+            }
+            if (!ok) {
+                rec[0] = 1;
+                prep_free(&p);
+                continue;
+            }
+            const unsigned k0 = phase8(&E->dg, &p.u);
+            rec[1] = p.phase;
+            rec[2] = k0;
+            for (int r = 0; r < E->el.rank && r < 64; r++)
+                if (bv_get(&p.s0, E->el.piv_col[r])) rec[3] |= 1ull << r;
+            uvec u; uv_init(&u, &E->st);
+            for (int j = 0; j < E->el.d && j < 64; j++) {
+                uv_copy(&u, &p.u);
+                uv_xor(&u, &E->el.kernel_u[j]);
+                const unsigned L = (phase8(&E->dg, &u) - k0) & 7u;
+                const uint64_t byte = (L & 1u) ? 0xFFull : (uint64_t)(L >> 1);
+                rec[4 + (j >> 3)] |= byte << (8 * (j & 7));
+            }
+            uv_free(&u);
+            prep_free(&p);
+        }
+    }
+    free(a);
 }
 
 /* ------------------------------------------------------------------ raw-form checks (normal_form.rs tests) */

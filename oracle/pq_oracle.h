@@ -76,6 +76,17 @@ int64_t pqo_engine_dump(const pqo_sim *s, int br, uint64_t *out, int64_t cap);
  */
 int pqo_branch_phases(pqo_sim *s, int br, const uint64_t *x, const uint64_t *y, uint8_t *out);
 
+/* Branch dimension d of branch engine `br` (-1 out of range). */
+int pqo_branch_dim(const pqo_sim *s, int br);
+
+/*
+ * Integers of Engine::prepare for all n boundaries x all branch engines (boundary-major),
+ * PQO_PREP_WORDS u64 words per job: vanish flag, constant phase, k0, pivot bits y0, then the
+ * Z4 increments Lp_j as bytes (layout in pq_oracle.c, pqo_prepare_info).
+ */
+#define PQO_PREP_WORDS 12
+void pqo_prepare_info(pqo_sim *s, int n, const uint64_t *xs, const uint64_t *ys, uint64_t *out);
+
 /* Pivot-rule-parametrised normal form check on a raw form (src/normal_form.rs:555-606):
  * returns 0 if the basis block-diagonalises the Gram matrix and is invertible. */
 int pqo_check_structure(int m, const uint8_t *bmat /* m*m */, const uint8_t *parity, int rule,

@@ -132,6 +132,11 @@ struct Target {
     std::vector<EngineDev> dev;                // rebased onto device addresses
     DevMem iom_mem;
     IoMapDev iom_dev{};
+    // the engine records and the boundary map as device structs (launch-independent; the
+    // allocation-free entry point launches on them directly)
+    DevMem rec_mem;
+    const EngineDev *dev_rec = nullptr;
+    const IoMapDev *map_rec = nullptr;
     int64_t bytes = 0;
     double branches_per_amp = 0.0;
     int max_d = 0, max_rank = 0, max_words = 0;
@@ -230,6 +235,14 @@ static pq_status upload_target(Target &T, int di_max) {
     T.bytes += (int64_t)T.iom_mem.n;
     for (auto &e : T.rs.branches)
         if ((int)T.iom.src.size() != e->nf) return fail(PQ_ERR_INTERNAL, "boundary map does not match engine");
+    // engine records then the boundary map, one allocation
+    const size_t rb = sizeof(EngineDev) * T.dev.size();
+    CU(T.rec_mem.alloc(rb + sizeof(IoMapDev)));
+    CU(cudaMemcpy(T.rec_mem.p, T.dev.data(), rb, cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(T.rec_mem.as<uint8_t>() + rb, &T.iom_dev, sizeof(IoMapDev), cudaMemcpyHostToDevice));
+    T.dev_rec = T.rec_mem.as<EngineDev>();
+    T.map_rec = reinterpret_cast<const IoMapDev *>(T.rec_mem.as<uint8_t>() + rb);
+    T.bytes += (int64_t)T.rec_mem.n;
     return PQ_OK;
 }
 
@@ -653,6 +666,7 @@ struct pq_batch {
 
 static int words_for(int nq) { return std::max(1, (nq + 63) / 64); }
 static const size_t kMaxPlans = 16;  // cached launch plans per simulator (boundary counts)
+static const size_t kPrepWords = 12;  // u64 words per job of pq_debug_prepare
 
 // puts for <y|C|x> (src/pathsum.rs:430-450)
 static IoMapHost main_iomap(const PathSum &ps) {
@@ -1451,6 +1465,20 @@ PQ_API pq_status pq_batch_run_device(pq_batch *b, const uint64_t *x, const uint6
     return run_device(*b->plan, x, y, out, err, (cudaStream_t)stream);
 }
 
+PQ_API pq_status pq_sim_device_check(pq_sim *s, int64_t n, int32_t *failed) {
+    if (!s || !failed) return fail(PQ_ERR_INVALID_ARG, "null argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->plans.find(n);
+    if (it == s->plans.end() || !it->second->graph_ready) return fail(PQ_ERR_INVALID_ARG, "no launch of that size yet");
+    Plan &P = *it->second;
+    CU(cudaSetDevice(s->device));
+    CU(cudaStreamSynchronize(P.stream));
+    int f = 0;
+    CU(cudaMemcpy(&f, P.errflag.p, sizeof(int), cudaMemcpyDeviceToHost));
+    *failed = f ? 1 : 0;
+    return PQ_OK;
+}
+
 PQ_API pq_status pq_sim_kernel_ms(pq_sim *s, int64_t n, float *ms) {
     if (!s || !ms) return fail(PQ_ERR_INVALID_ARG, "null argument");
     std::lock_guard<std::mutex> lk(s->mu);
@@ -1796,32 +1824,73 @@ PQ_API int32_t pq_debug_branch_phases(pq_sim *s, int32_t branch, const uint64_t 
     return J.vanish ? -1 : d;
 }
 
+PQ_API pq_status pq_debug_prepare(pq_sim *s, int64_t n, const uint64_t *x, const uint64_t *y, uint64_t *out) {
+    if (!s || !x || !y || !out) return fail(PQ_ERR_INVALID_ARG, "null argument");
+    pq_status st = check_n(n);
+    if (st != PQ_OK) return st;
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->host_only) return fail(PQ_ERR_NO_DEVICE, "simulator was created by pq_analyze (host structures only)");
+    CU(cudaSetDevice(s->device));
+    Plan *P = nullptr;
+    st = sim_plan(s, n, &P);
+    if (st != PQ_OK) return st;
+    const size_t bw = (size_t)n * s->nw * 8;
+    CU(cudaMemcpyAsync(P->x.p, x, bw, cudaMemcpyHostToDevice, P->stream));
+    CU(cudaMemcpyAsync(P->y.p, y, bw, cudaMemcpyHostToDevice, P->stream));
+    CU(cudaMemsetAsync(P->errflag.p, 0, sizeof(int), P->stream));
+    prepare_kernel<<<P->grid_prep, 128, (size_t)4 * P->smem_words * 8, P->stream>>>(P->args);
+    CU(cudaGetLastError());
+    std::vector<JobDev> jobs((size_t)P->njobs);
+    CU(cudaMemcpyAsync(jobs.data(), P->jobs.p, sizeof(JobDev) * jobs.size(), cudaMemcpyDeviceToHost, P->stream));
+    CU(cudaStreamSynchronize(P->stream));
+    // jobs are laid out boundary-major, then branch engine (build_plan); the Z4 increments of
+    // the low coordinates are mapped from the device's coordinate order back to the reference's
+    const size_t nb = s->main.dev.size();
+    for (size_t j = 0; j < jobs.size(); j++) {
+        const JobDev &J = jobs[j];
+        const EngineDev &E = s->main.dev[j % nb];
+        uint64_t *rec = out + j * kPrepWords;
+        std::memset(rec, 0, sizeof(uint64_t) * kPrepWords);
+        if (J.vanish) {
+            rec[0] = 1;
+            continue;
+        }
+        if (J.err) return fail(PQ_ERR_INTERNAL, "device self-check failed (odd Z8 increment)");
+        rec[1] = J.phase;
+        rec[2] = J.k0;
+        rec[3] = J.y0;
+        for (int jd = 0; jd < E.d && jd < 64; jd++) {
+            const int jr = (jd < E.DI && jd < 16) ? E.cperm[jd] : jd;
+            rec[4 + (jr >> 3)] |= (uint64_t)J.Lp[jd] << (8 * (jr & 7));
+        }
+    }
+    return PQ_OK;
+}
+
 }  // extern "C"
 
 // ========================================================================================
 // Allocation-free evaluation
 //
-// Some callers cannot allocate device memory at the point where they need amplitudes:
-// code running while a CUDA graph is being captured (cudaMalloc is not capturable), hosts
-// that run under a fixed device-memory budget enforced by an outer allocator, or plugin
-// callbacks invoked from a context that forbids allocation.  For them,
-// pq_amplitudes_noalloc evaluates a resident simulator's amplitudes using only the
-// simulator's already-uploaded structures plus one fixed scratch array that lives in this
-// file as a static __device__ variable (it exists on every GPU that loads the library,
-// until the process exits).  The caller passes device pointers for the boundaries and the
-// results.  The scratch holds the per-call job records, work-item layout and partial sums;
-// every call overwrites it, so calls that overlap on the GPU (two streams, or two host
-// threads) race on it and must be serialised by the caller.
+// Some callers cannot allocate device memory at the point where they need amplitudes: hosts
+// whose device memory is owned by an outer allocator with a fixed budget (a framework's
+// caching allocator, a serving process that has reserved its memory up front), and plugin or
+// callback code that is called from a context where allocating would block, fragment the
+// caller's pool or fail.  For them, pq_amplitudes_noalloc evaluates a resident simulator's
+// amplitudes using only the simulator's already-uploaded structures (engine tables, engine
+// records and boundary map, all allocated when the simulator was created) plus one fixed
+// scratch array that lives in this file as a static __device__ variable (it exists on every
+// GPU that loads the library, until the process exits).  The caller passes device pointers
+// for the boundaries and the results.  The scratch holds the per-call job records, work-item
+// layout and partial sums; every call overwrites it, so calls that overlap on the GPU (two
+// streams, or two host threads) race on it and must be serialised by the caller.
 // ========================================================================================
 namespace pq {
 
-static const int kNaMaxEngines = 64;    // branch engines of the simulator (2^pairs <= 64)
 static const int kNaMaxJobs = 4096;     // boundaries x branch engines per call
 static const int kNaMaxItems = 65536;   // work items (chunk ranges) per call
 
 struct NoAllocScratch {
-    EngineDev engines[kNaMaxEngines];
-    IoMapDev map;
     JobDev jobs[kNaMaxJobs];
     int perm[kNaMaxJobs], kinv[kNaMaxJobs], jdl[kNaMaxJobs];
     unsigned jcpi[kNaMaxJobs];
@@ -1835,17 +1904,19 @@ struct NoAllocScratch {
     int errflag;
 };
 
-// The scratch array (about 1.7 MiB).  Host code must not take its address directly: the
+// The scratch array (about 1.6 MiB).  Host code must not take its address directly: the
 // host-side symbol is only a stand-in; the device address comes from cudaGetSymbolAddress.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocScratch)];
 
 static std::mutex g_na_mu;
 static NoAllocScratch *g_na_ptr[64] = {nullptr};  // device address of the scratch, per device
 
-// Same per-job work shape as the regular launch layout, so each job's partial sums come out
-// in the same order (and the results bit-identical to pq_amplitudes).
-// One block: job records, identity item order, per-job shapes and the item prefix sums.
-__global__ void __launch_bounds__(1024) na_layout_kernel(NoAllocScratch *S, int nreq, int nb, int cpl, int umax) {
+// One block: job records (boundary-major, then branch engine, as build_plan lays them out),
+// identity item order, per-job shapes and the item prefix sums.  Each job gets the work shape
+// the simulator's own launch plans give it, so its partial sums are the same numbers in the
+// same order.
+__global__ void __launch_bounds__(1024) na_layout_kernel(NoAllocScratch *S, const EngineDev *eng, int nreq, int nb,
+                                                         int cpl, int umax, int umax_ctab, int use_ctab) {
     __shared__ long long part[1024];
     const int njobs = nreq * nb;
     const int per = (njobs + 1023) / 1024;
@@ -1859,8 +1930,8 @@ __global__ void __launch_bounds__(1024) na_layout_kernel(NoAllocScratch *S, int 
         J.out = j / nb;
         S->perm[j] = j;
         S->kinv[j] = j;
-        const EngineDev &E = S->engines[j % nb];
-        job_shape(E, cpl, umax, S->jdl[j], S->jnch[j], S->jcpi[j]);
+        const EngineDev &E = eng[j % nb];
+        job_shape(E, cpl, (use_ctab && E.ctab) ? umax_ctab : umax, S->jdl[j], S->jnch[j], S->jcpi[j]);
         local += (long long)((S->jnch[j] + S->jcpi[j] - 1) / S->jcpi[j]);
     }
     part[threadIdx.x] = local;
@@ -1886,37 +1957,32 @@ __global__ void __launch_bounds__(1024) na_layout_kernel(NoAllocScratch *S, int 
 }  // namespace pq
 
 extern "C" PQ_API pq_status pq_amplitudes_noalloc(pq_sim *s, int64_t n, const uint64_t *x, const uint64_t *y,
-                                                  double *out, void *stream) {
+                                                  double *out, double *errbound, void *stream) {
     if (!s || !x || !y || !out) return fail(PQ_ERR_INVALID_ARG, "null argument");
     if (s->host_only) return fail(PQ_ERR_NO_DEVICE, "simulator was created by pq_analyze (host structures only)");
+    std::lock_guard<std::mutex> lk(s->mu);
     const int nb = (int)s->main.dev.size();
-    if (nb > kNaMaxEngines)
-        return fail(PQ_ERR_INVALID_ARG, "pq_amplitudes_noalloc: simulator has " + std::to_string(nb) +
-                                            " branch engines; the fixed scratch holds at most 64");
-    if (n <= 0 || n * nb > kNaMaxJobs)
+    if (n <= 0 || n > kNaMaxJobs || n * nb > kNaMaxJobs)
         return fail(PQ_ERR_INVALID_ARG, "pq_amplitudes_noalloc: boundaries x branch engines = " +
-                                            std::to_string(n * nb) + " outside 1..4096 (fixed scratch size)");
-    pq_tuning tu;
-    {
-        std::lock_guard<std::mutex> lk(g_mu);
-        tu = g_tuning;
-    }
+                                            std::to_string(n * (int64_t)nb) + " outside 1..4096 (fixed scratch size)");
+    // the simulator's own launch shape, as its plans use it
+    const pq_tuning tu = s->tu;
+    const int umax = unit_max_of(tu);
+    const int use_ctab = tu.chunk_tables == 1 ? 1 : 0;
     long long nitems = 0;
-    for (int64_t r = 0; r < n; r++)
-        for (int b = 0; b < nb; b++) {
-            const EngineDev &E = s->main.dev[b];
-            if (E.d > kMaxD || E.rank > kMaxPivots) return fail(PQ_ERR_UNSUPPORTED, "branch engine outside kernel limits");
-            if (E.d > tu.max_branch_dim) return fail(PQ_ERR_ADMISSION_REFUSED, "branch dimension above the cap");
-            int dl;
-            unsigned long long nch;
-            unsigned cpi;
-            job_shape(E, tu.chunks_per_lane, std::min(unit_max_of(tu), 4), dl, nch, cpi);
-            nitems += (long long)((nch + cpi - 1) / cpi);
-        }
+    for (int b = 0; b < nb; b++) {
+        const EngineDev &E = s->main.dev[b];
+        if (E.d > kMaxD || E.rank > kMaxPivots) return fail(PQ_ERR_UNSUPPORTED, "branch engine outside kernel limits");
+        if (E.d > tu.max_branch_dim) return fail(PQ_ERR_ADMISSION_REFUSED, "branch dimension above the cap");
+        int dl;
+        unsigned long long nch;
+        unsigned cpi;
+        job_shape(E, tu.chunks_per_lane, unit_max_for(E, tu), dl, nch, cpi);
+        nitems += n * (long long)((nch + cpi - 1) / cpi);
+    }
     if (nitems > kNaMaxItems)
         return fail(PQ_ERR_INVALID_ARG, "pq_amplitudes_noalloc: " + std::to_string(nitems) +
                                             " work items exceed the fixed scratch (65536); pass fewer boundaries");
-    std::lock_guard<std::mutex> lk(s->mu);
     CU(cudaSetDevice(s->device));
     if (s->device < 0 || s->device >= 64) return fail(PQ_ERR_INVALID_ARG, "device index above 63");
     NoAllocScratch *S = nullptr;
@@ -1932,14 +1998,12 @@ extern "C" PQ_API pq_status pq_amplitudes_noalloc(pq_sim *s, int64_t n, const ui
         S = g_na_ptr[s->device];
     }
     cudaStream_t st = (cudaStream_t)stream;
-    CU(cudaMemcpyAsync(S->engines, s->main.dev.data(), sizeof(EngineDev) * (size_t)nb, cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(&S->map, &s->main.iom_dev, sizeof(IoMapDev), cudaMemcpyHostToDevice, st));
     // counter and error flag must start at zero; everything else is fully rewritten below
     CU(cudaMemsetAsync(&S->counter, 0, sizeof(unsigned long long) + sizeof(int), st));
-    na_layout_kernel<<<1, 1024, 0, st>>>(S, (int)n, nb, tu.chunks_per_lane, std::min(unit_max_of(tu), 4));
+    na_layout_kernel<<<1, 1024, 0, st>>>(S, s->main.dev_rec, (int)n, nb, tu.chunks_per_lane, umax, 1, use_ctab);
     KArgs a{};
-    a.engines = S->engines;
-    a.maps = &S->map;
+    a.engines = s->main.dev_rec;
+    a.maps = s->main.map_rec;
     a.jobs = S->jobs;
     a.njobs = (int)(n * nb);
     a.perm = S->perm;
@@ -1956,7 +2020,7 @@ extern "C" PQ_API pq_status pq_amplitudes_noalloc(pq_sim *s, int64_t n, const ui
     a.out_jobs = S->out_jobs;
     a.nout = (int)n;
     a.out = out;
-    a.err = nullptr;
+    a.err = errbound;
     a.out_prob = 0;
     a.xs = x;
     a.ys = y;
@@ -1964,15 +2028,21 @@ extern "C" PQ_API pq_status pq_amplitudes_noalloc(pq_sim *s, int64_t n, const ui
     a.smem_words = std::max(8, s->main.max_words);
     a.dbg = nullptr;
     a.errflag = &S->errflag;
+    a.use_ctab = use_ctab;
     const size_t psmem = (size_t)4 * a.smem_words * 8;
     if (psmem > 48 * 1024) CU(cudaFuncSetAttribute(prepare_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
     const int bw = std::max(1, std::min(8, tu.block_warps));
+    const int minb = (tu.blocks_per_sm >= 2 && tu.blocks_per_sm <= 4) ? tu.blocks_per_sm : 3;
     int occ = 0;
-    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, enum_kernel<0>, 32 * bw, 0));
+    if (minb == 4) CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, enum_kernel<0, 4>, 32 * bw, 0));
+    else if (minb == 2) CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, enum_kernel<0, 2>, 32 * bw, 0));
+    else CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, enum_kernel<0, 3>, 32 * bw, 0));
     const long long want = (long long)sm_count() * std::max(occ, 1);
     const int grid_enum = (int)std::max(1LL, std::min<long long>(want, (nitems + bw - 1) / bw));
     prepare_kernel<<<std::max(1, std::min(a.njobs / 4 + 1, 65535)), 128, psmem, st>>>(a);
-    enum_kernel<0><<<grid_enum, 32 * bw, 0, st>>>(a);
+    if (minb == 4) enum_kernel<0, 4><<<grid_enum, 32 * bw, 0, st>>>(a);
+    else if (minb == 2) enum_kernel<0, 2><<<grid_enum, 32 * bw, 0, st>>>(a);
+    else enum_kernel<0, 3><<<grid_enum, 32 * bw, 0, st>>>(a);
     job_reduce_kernel<<<(a.njobs + 255) / 256, 256, 0, st>>>(a);
     out_reduce_kernel<<<(a.nout + 255) / 256, 256, 0, st>>>(a);
     CU(cudaGetLastError());

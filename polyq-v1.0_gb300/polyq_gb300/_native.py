@@ -78,7 +78,8 @@ SIGNATURES = {
     "pq_amplitudes_device": (ct.c_int, [P, ct.c_int64, P, P, P, P, P]),
     "pq_amplitudes_plain": (ct.c_int, [P, ct.c_int64, u64p, u64p, f64p]),
     "pq_amplitudes_fp64": (ct.c_int, [P, ct.c_int64, u64p, u64p, f64p]),
-    "pq_amplitudes_noalloc": (ct.c_int, [P, ct.c_int64, P, P, P, P]),
+    "pq_amplitudes_noalloc": (ct.c_int, [P, ct.c_int64, P, P, P, P, P]),
+    "pq_sim_device_check": (ct.c_int, [P, ct.c_int64, ct.POINTER(ct.c_int32)]),
     "pq_batch_create": (ct.c_int, [ct.c_int32, ct.POINTER(P), i64p, ct.POINTER(P)]),
     "pq_batch_destroy": (None, [P]),
     "pq_batch_run": (ct.c_int, [P, u64p, u64p, f64p, f64p]),
@@ -103,6 +104,7 @@ SIGNATURES = {
     "pq_debug_engine_dump": (ct.c_int64, [P, ct.c_int32, u64p, ct.c_int64]),
     "pq_debug_engine_shape": (ct.c_int, [P, ct.c_int32, i64p]),
     "pq_debug_branch_phases": (ct.c_int32, [P, ct.c_int32, u64p, u64p, u8p]),
+    "pq_debug_prepare": (ct.c_int, [P, ct.c_int64, u64p, u64p, u64p]),
 }
 
 

@@ -232,10 +232,12 @@ class Simulator:
         return out[:n]
 
     def branch_phases(self, input: int, output: int, branch: int = 0):
-        d = self.stats_full()["branch_dim"] if branch == 0 else None
+        d = self.engine_shape(branch)["d"]
+        if d > 24:
+            raise ValueError("branch dimension above 24")
         xs = pack_bits([input], self.num_qubits)
         ys = pack_bits([output], self.num_qubits)
-        buf = np.zeros(1 << 24 if d is None else max(1, 1 << d), dtype=np.uint8)
+        buf = np.zeros(max(1, 1 << d), dtype=np.uint8)
         r = self._L.pq_debug_branch_phases(self._h, branch, _p(xs, ct.c_uint64), _p(ys, ct.c_uint64),
                                            _p(buf, ct.c_uint8))
         if r == -2:
@@ -243,6 +245,20 @@ class Simulator:
         if r == -1:
             return None
         return buf[: 1 << r]
+
+
+    def prepare_info(self, inputs, outputs) -> np.ndarray:
+        """Engine::prepare integers as the device computes them (pq_debug_prepare): an
+        (n, branch engines, 12) uint64 array -- vanish flag, constant phase, k0, pivot bits
+        y0, then the Z4 increments Lp_j as bytes in the reference's coordinate order."""
+        xs = pack_bits(inputs, self.num_qubits)
+        ys = pack_bits(outputs, self.num_qubits)
+        n = xs.shape[0]
+        nb = self.stats_full()["num_branches"]
+        out = np.zeros((n, nb, 12), dtype=np.uint64)
+        N.check(self._L.pq_debug_prepare(self._h, n, _p(xs, ct.c_uint64), _p(ys, ct.c_uint64),
+                                         _p(out, ct.c_uint64)))
+        return out
 
 
 class Batch:

@@ -58,27 +58,53 @@ def test_known_answers(gpu):
 
 
 def test_branch_phases_bit_exact(gpu):
+    # every branch engine b of every strategy: the 2^p T-pair engines (src/rank.rs:88-103,
+    # src/pathsum.rs:360-394) as well as the cached engine, Z8 index of every branch
+    # (src/normal_form.rs:479-493) bit-exact against the oracle
     rng = Rng(21)
-    checked = 0
+    checked = checked_pairs = 0
     for trial in range(60):
         n = 1 + rng.below(4)
         c = random_clifford_t(n, 8 + rng.below(14), rng.below(6), trial % 3 == 0, rng)
-        for strat in ("cached", "auto"):
-            s = Simulator(c, strat)
-            r = O.OracleSim(c, strat)
+        for strat, p in (("cached", None), ("auto", None), ("pairs", 2)):
+            s = Simulator(c, strat, p)
+            r = O.OracleSim(c, strat, p or 0)
             nb = s.stats_full()["num_branches"]
+            assert nb == r.stats()["branches"]
             for b in range(nb):
+                assert s.engine_shape(b)["d"] == r.branch_dim(b)
                 for x, y in ((0, 0), (1 % (1 << n), (1 << n) - 1)):
                     want = r.branch_phases(x, y, b)
-                    got = s.branch_phases(x, y, b) if b == 0 else None
-                    if b != 0:
-                        continue
+                    got = s.branch_phases(x, y, b)
+                    assert (want is None) == (got is None), (trial, strat, b)
                     if want is None:
-                        assert got is None
                         continue
-                    assert got is not None and np.array_equal(got, want)
+                    assert np.array_equal(got, want), (trial, strat, b)
                     checked += 1
-    assert checked > 40
+                    checked_pairs += b > 0
+    # layered circuits (src/rng.rs random_layered) keep their T gates apart, so they have pair
+    # candidates: up to 8 branch engines of d = 0..9 each
+    rng = Rng(77)
+    for trial in range(30):
+        n = 3 + rng.below(3)
+        c = random_layered(n, 2 + rng.below(3), rng)
+        for strat, p in (("auto", None), ("pairs", 3)):
+            s = Simulator(c, strat, p)
+            r = O.OracleSim(c, strat, p or 0)
+            nb = s.stats_full()["num_branches"]
+            assert nb == r.stats()["branches"]
+            for b in range(nb):
+                assert s.engine_shape(b)["d"] == r.branch_dim(b)
+                for x, y in ((0, 0), (1, (1 << n) - 1), (2, 5 % (1 << n))):
+                    want = r.branch_phases(x, y, b)
+                    got = s.branch_phases(x, y, b)
+                    assert (want is None) == (got is None), (trial, strat, b)
+                    if want is None:
+                        continue
+                    assert np.array_equal(got, want), (trial, strat, b)
+                    checked += 1
+                    checked_pairs += b > 0
+    assert checked > 400 and checked_pairs > 200
 
 
 def test_branch_phases_bit_exact_workloads(gpu):
@@ -93,12 +119,21 @@ def test_branch_phases_bit_exact_workloads(gpu):
         if want is not None:
             assert np.array_equal(got, want)
             seen += 1
+    # the many-boundaries workload, strategy auto: all 16 branch engines (d = 20..22)
     c = workload_many_boundaries(0)
     s, r = Simulator(c, "auto"), O.OracleSim(c, "auto")
-    for y in random_outputs(50, 3, 9):
-        want = r.branch_phases(0, y, 0)
-        got = s.branch_phases(0, y, 0)
-        assert want is not None and np.array_equal(got, want)
+    nb = s.stats_full()["num_branches"]
+    assert nb == 16
+    live = 0
+    for y in random_outputs(50, 2, 9):
+        for b in range(nb):
+            want = r.branch_phases(0, y, b)
+            got = s.branch_phases(0, y, b)
+            assert (want is None) == (got is None), b
+            if want is not None:
+                assert got.shape == want.shape and np.array_equal(got, want), b
+                live += 1
+    assert live >= 4
 
 
 def test_engine_dumps_match_oracle(gpu):
@@ -249,6 +284,10 @@ def test_device_resident_path_matches_host_path(gpu):
     torch.cuda.synchronize()
     dev = out.cpu().numpy().view(np.complex128)
     assert np.array_equal(dev, host)
+    # the prepare kernel's self-check of that launch (a failure would also make it NaN)
+    failed = ct.c_int32(-1)
+    N.check(N.lib().pq_sim_device_check(s.handle, 64, ct.byref(failed)))
+    assert failed.value == 0 and np.all(np.isfinite(dev))
 
 
 def test_autotune_keeps_results(gpu):

@@ -344,3 +344,36 @@ def test_lazy_pair_sampling_monte_carlo_branches():
         re, im, se = sim.amplitude_estimate_pairs(0, y, 3, 400, 9, 0)
         assert abs(complex(re, im) - want) < 6.0 * se + 5e-3
     assert tested >= 3
+
+
+def test_prepare_integers_agree_with_branch_phases():
+    # the oracle's Engine::prepare record (src/engine.rs:569-610) against its own per-branch Z8
+    # indices (src/normal_form.rs:479-493) for every branch engine: k0 is the index at s = 0,
+    # Lp_j half the increment along kernel column j (always even), and a job vanishes exactly
+    # when the branch phases are undefined
+    rng = Rng(5)
+    checked = 0
+    for trial in range(40):
+        n = 1 + rng.below(4)
+        c = random_clifford_t(n, 10 + rng.below(14), rng.below(7), trial % 3 == 0, rng)
+        for strat, p in (("cached", 0), ("auto", 0), ("pairs", 2)):
+            sim = O.OracleSim(c, strat, p)
+            xs = [0, (1 << n) - 1]
+            ys = [rng.below(1 << n), rng.below(1 << n)]
+            info = sim.prepare_info(xs, ys)
+            for i in range(2):
+                for b in range(sim.stats()["branches"]):
+                    rec = info[i, b]
+                    ph = sim.branch_phases(xs[i], ys[i], b)
+                    assert (ph is None) == bool(rec[0])
+                    if ph is None:
+                        assert not rec[1:].any()
+                        continue
+                    d = sim.branch_dim(b)
+                    assert int(rec[2]) == int(ph[0])
+                    lp = rec[4:].view(np.uint8)
+                    for j in range(d):
+                        assert int(lp[j]) == ((int(ph[1 << j]) - int(ph[0])) % 8) // 2
+                    assert not lp[d:].any()
+                    checked += 1
+    assert checked > 100
