@@ -1,10 +1,11 @@
-"""Throughput of the GB300 amplitude path on the one-circuit, many-boundaries workload.
+"""Throughput of the GB300 amplitude path on the one-circuit, many-boundaries workload, with the
+other configurations measured in the same run.
 
-Workload: a seeded Clifford+T circuit with n=50 qubits, 2000 gates from {H,S,CX,CZ,T}
-(exactly 32 T, seed 0: the radical-constrained branch subspace of the cached engine has
-2^29 > 2^22 branches), 4096 uniform output bitstrings y, x = 0, strategy auto (the
-reference's Simulator::new default: 16 branch engines of d = 20..22).  One step evaluates
-all 4096 amplitudes.
+Workload of the headline: a seeded Clifford+T circuit with n=50 qubits, 2000 gates from
+{H,S,CX,CZ,T} (exactly 32 T, seed 0: the radical-constrained branch subspace of the cached engine
+has 2^29 > 2^22 branches), 4096 uniform output bitstrings y, x = 0, strategy auto (the
+reference's Simulator::new default: 16 branch engines of d = 20..22).  One step evaluates all
+4096 amplitudes.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -13,9 +14,16 @@ value      branches/s with boundaries resident in HBM (pq_amplitudes_device), CU
 e2e        same metric through the public host-buffer call pq_amplitudes (H2D of the
            boundaries and D2H of amplitudes + error bounds inside the timed region)
 roofline   enumeration kernel: its FP32 FMA-pipe work (4 ops per enumerated branch) per launch
-           over its event-timed duration, against the fma.f32 rate measured on the device;
-           reference_form beside it: the reference engine's integer work for the same branches
-           (5 W_o + 6 W_g int64 ops each) against the measured lop3 / popc rates
+           over its event-timed duration, against the fma.f32 rate measured on the device and
+           the nominal rate (SMs x 128 lanes x 2070 MHz); reference_form beside it: the
+           reference engine's integer work for the same branches (5 W_o + 6 W_g int64 ops each)
+           against the measured lop3 / popc rates
+cfg1_small, cfg3_batched, cfg5_serve
+           at N=1 the same line carries the single small amplitude (p50/p99 per call beside the
+           CPU restatement's), the uneven 256-circuit batch (one graph launch vs the plain
+           per-circuit and per-boundary paths, CPU restatement per branch-dimension bucket) and
+           the served Poisson stream (throughput, p50/p99 at the offered load, below saturation
+           and saturated); each leg with its own clock summary (nvidia-smi every 50 ms)
 workloads  --workload many_boundaries (default) | batched | serve | small | rotations | sample | estimate
 cpu_baseline  the CPU oracle (a restatement of the reference engine) on all host threads
 --impl reference  times the same CPU restatement on the same workload (bounded sample)
@@ -426,7 +434,7 @@ def _bucket(d):
     return "d<=12" if d <= 12 else ("d13-18" if d <= 18 else "d>=19")
 
 
-def cpu_batched_buckets(circs, outs, enum_per_circuit, threads, budget_s=4.0):
+def cpu_batched_buckets(circs, dims, outs, enum_per_circuit, threads, budget_s=4.0):
     """CPU restatement on the uneven batch, per branch-dimension bucket: each bucket's
     circuits are evaluated in order (all 64 boundaries for d <= 18, 2 boundaries above) until
     `budget_s` of CPU time is spent; the bucket's remaining circuits are charged their
@@ -435,7 +443,7 @@ def cpu_batched_buckets(circs, outs, enum_per_circuit, threads, budget_s=4.0):
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle
     by = {}
-    for i, ((c, d), o) in enumerate(zip(circs, outs)):
+    for i, d in enumerate(dims):
         by.setdefault(_bucket(d), []).append(i)
     res = {}
     for key, idx in sorted(by.items()):
@@ -443,7 +451,7 @@ def cpu_batched_buckets(circs, outs, enum_per_circuit, threads, budget_s=4.0):
         for i in idx:
             if spent >= budget_s:
                 break
-            c, d = circs[i]
+            c, d = circs[i][0], dims[i]
             k = 64 if d <= 18 else 2
             r = oracle.OracleSim(c, "auto")
             t0 = time.perf_counter()
@@ -474,6 +482,11 @@ def leg_batched(args, clk=None, cpu=True):
     pq, N = _gpu_setup()
     L = N.lib()
     from polyq_gb300.rng import random_outputs, workload_batch
+    if args.tuning:  # a fixed launch shape (profiling): no autotuning
+        vals = [int(v) for v in args.tuning.split(",")] + [0]
+        pq.set_tuning(inner_dims=vals[0], chunks_per_lane=vals[1], block_warps=vals[2], blocks_per_sm=vals[3],
+                      unit_chunks=vals[4])
+        args.no_autotune = True
     t0 = time.perf_counter()
     circs = workload_batch(256, seed=3)
     sims = [pq.Simulator(c) for c, _ in circs]
@@ -520,6 +533,9 @@ def leg_batched(args, clk=None, cpu=True):
     benum = (ct.c_double * 4)()
     N.check(L.pq_batch_enumerated(b._h, benum))
     got = dout.cpu().numpy().view(np.complex128)
+    if args.batch_only:  # profiling: the batched launch alone
+        return {"value": n / (batched_ms * 1e-3), "unit": "amplitudes/s", "ms_per_step": batched_ms,
+                "enum_kernel_ms": enum_avg, "branches_per_s": benum[0] / (batched_ms * 1e-3), "tuning": tuning}
     # plain path 1: one launch per circuit (its 64 boundaries), host buffers, sequential
     for s, o in zip(sims, outs):
         s.amplitudes([0] * 64, o)  # plans and graphs built outside the timing
@@ -568,7 +584,7 @@ def leg_batched(args, clk=None, cpu=True):
         leg["clocks"] = clk.summary(tw0, tw1)
         leg["clocks_plain_per_circuit"] = clk.summary(tp0, tp0 + plain_circ_s)
     if cpu:
-        cb = cpu_batched_buckets(circs, outs, enum_circ, cpu_threads())
+        cb = cpu_batched_buckets(circs, [s.stats_full()["branch_dim"] for s in sims], outs, enum_circ, cpu_threads())
         tot = sum(v["cpu_seconds_for_bucket"] for v in cb.values())
         leg["cpu_baseline"] = {"value": n / tot, "unit": "amplitudes/s", "cores": cpu_threads(), "kind": "port",
                                "per_d_bucket": cb,
@@ -637,8 +653,10 @@ def leg_serve(args, clk=None):
         w1 = time.perf_counter()
         ok = [r for r in res if r["status"] == 0]
         lat = [r["done_s"] - r["submit_s"] for r in ok]
+        lat_fg = [r["done_s"] - r["submit_s"] for r in ok if r["pieces"] == 0]
+        lat_bg = [r["done_s"] - r["submit_s"] for r in ok if r["pieces"] > 0]
         span = (max(r["done_s"] for r in ok) - min(r["submit_s"] for r in ok)) if ok else 0.0
-        okt = set(r["tag"] for r in ok)
+        okt = set(r["tag"] for r in ok if r["pieces"] == 0)  # the plain comparison takes one-wave requests
         out = {"offered_per_s": rate, "requests": nreq, "completed": len(ok),
                "refused": sum(1 for r in res if r["status"] == 3),
                "other_errors": sum(1 for r in res if r["status"] not in (0, 3)),
@@ -646,7 +664,13 @@ def leg_serve(args, clk=None):
                "evaluated_at_level": {name: sum(1 for r in ok if r["level"] == lv)
                                       for lv, name in enumerate(("fp32_walk", "chunk_tables", "fp64_walk"))},
                "p50_ms": 1e3 * _pct(lat, 0.5) if lat else None,
-               "p99_ms": 1e3 * _pct(lat, 0.99) if lat else None}
+               "p99_ms": 1e3 * _pct(lat, 0.99) if lat else None,
+               "one_wave": {"completed": len(lat_fg), "p50_ms": 1e3 * _pct(lat_fg, 0.5) if lat_fg else None,
+                            "p99_ms": 1e3 * _pct(lat_fg, 0.99) if lat_fg else None},
+               "background_pieces": {"completed": len(lat_bg),
+                                     "pieces": sum(r["pieces"] for r in ok if r["pieces"] > 0),
+                                     "p50_ms": 1e3 * _pct(lat_bg, 0.5) if lat_bg else None,
+                                     "p99_ms": 1e3 * _pct(lat_bg, 0.99) if lat_bg else None}}
         if clk is not None:
             out["clocks"] = clk.summary(w0, w1)
         return out, [q for q in reqs if q["tag"] in okt]
@@ -658,7 +682,7 @@ def leg_serve(args, clk=None):
     # what the server sustains when arrivals outrun it)
     sat, _ = load(4.0 * args.rate, 0.25 * args.duration)
     # plain per-request launches (one synchronous call per request, no batching) on a sample of
-    # the requests the server admitted
+    # the requests the server evaluated in one wave
     reqs = served[:300]
     for r in reqs:  # plans built outside the timing
         s = sims[r["sim"]]
@@ -731,7 +755,37 @@ def leg_small(args, clk=None, cpu_runs=200):
         want = ref.amplitudes([0], [0], nthreads=1)[0]
         cpu.append(time.perf_counter() - t1)
     dense = oracle.dense_statevector(c, 0)[0]
-    leg = {"value": 1.0 / _pct(lat, 0.5), "unit": "amplitudes/s (serial calls)",
+    # the same calls at the C-ABI level: buffers packed once, one ctypes call each
+    import ctypes as ct
+
+    import numpy as np
+    L = N.lib()
+    xb = np.zeros(1, dtype=np.uint64)
+    yb = np.zeros(1, dtype=np.uint64)
+    ob = np.zeros(2)
+    P = lambda arr, t: arr.ctypes.data_as(ct.POINTER(t))  # noqa: E731
+    gcall = lambda: L.pq_amplitudes(sim.handle, 1, P(xb, ct.c_uint64), P(yb, ct.c_uint64), P(ob, ct.c_double),  # noqa: E731
+                                    None)
+    ccall = lambda: ref.L.pqo_amplitudes(ref.h, 1, P(xb, ct.c_uint64), P(yb, ct.c_uint64), P(ob, ct.c_double), 1)  # noqa: E731
+    for f in (gcall, ccall):
+        for _ in range(20):
+            f()
+    glat, clat = [], []
+    for _ in range(max(200, cpu_runs)):
+        t1 = time.perf_counter()
+        gcall()
+        glat.append(time.perf_counter() - t1)
+        t1 = time.perf_counter()
+        ccall()
+        clat.append(time.perf_counter() - t1)
+    kms = (ct.c_float * 3)()
+    N.check(L.pq_sim_kernel_ms(sim.handle, 1, kms))
+    leg_cabi = {"gpu_p50_ms": 1e3 * _pct(glat, 0.5), "gpu_p99_ms": 1e3 * _pct(glat, 0.99),
+                "device_ms_last_call": kms[0] + kms[1] + kms[2],
+                "cpu_p50_ms": 1e3 * _pct(clat, 0.5), "cpu_p99_ms": 1e3 * _pct(clat, 0.99), "runs": len(glat),
+                "note": "pq_amplitudes vs the CPU restatement's pqo_amplitudes (one thread), buffers packed once, "
+                        "one ctypes call per amplitude"}
+    leg = {"value": 1.0 / _pct(lat, 0.5), "unit": "amplitudes/s (serial calls)", "c_abi_level": leg_cabi,
            "amplitude": [a.real, a.imag], "probability": p, "p50_ms": 1e3 * _pct(lat, 0.5),
            "p99_ms": 1e3 * _pct(lat, 0.99), "probability_p50_ms": 1e3 * _pct(plat, 0.5),
            "abs_err_vs_fp64_oracle": abs(a - want), "abs_err_vs_dense": abs(a - dense),
@@ -897,8 +951,9 @@ def main():
     ap.add_argument("--rate", type=float, default=5000.0, help="serve: offered requests/s")
     ap.add_argument("--duration", type=float, default=2.0, help="serve: seconds of arrivals")
     ap.add_argument("--slots", type=int, default=256, help="serve: requests per wave")
-    ap.add_argument("--max-d", type=int, default=28, help="serve: log2 cap on a request's branches")
+    ap.add_argument("--max-d", type=int, default=28, help="serve: log2 cap on a request's branches (refused above)")
     ap.add_argument("--batch-steps", type=int, default=20, help="batched: timed launches")
+    ap.add_argument("--batch-only", action="store_true", help="batched: the batched launch alone (profiling)")
     ap.add_argument("--headline-only", action="store_true",
                     help="default workload only (no small / batched / serving legs)")
     args = ap.parse_args()

@@ -205,13 +205,19 @@ typedef struct pq_result {
     int32_t level;        /* evaluation that produced it: 0 the FP32 walk, 1 chunk-sum tables,
                              2 the FP64 walk (probabilities and marginals whose bound could not
                              show 1e-12 absolute are re-evaluated at the next level) */
-    int32_t reserved;
+    int32_t pieces;       /* background pieces the request was evaluated in (0: one wave) */
 } pq_result;
 /* max_slots: requests per launched wave; mem_budget_bytes: device memory the in-flight waves
  * may hold; max_branch_dim: a request whose work -- branches summed over its branch engines --
  * exceeds 2^max_branch_dim is refused (PQ_ERR_ADMISSION_REFUSED) rather than run. */
 PQ_API pq_status pq_server_create(int32_t nsims, pq_sim *const *sims, int32_t max_slots, int64_t mem_budget_bytes,
                                   int32_t max_branch_dim, pq_server **out);
+/* Requests whose work is above 2^split_log2 branches (default 28) are not refused but evaluated
+ * in the background, in pieces of at most 2^piece_log2 branches (default 32) -- ranges of their
+ * branch engines or of one engine's work items -- one piece at a time on half of the SMs, beside
+ * the waves of smaller requests; a request's pieces are summed in FP64 and its bounds added.
+ * Only requests above 2^max_branch_dim branches are refused. */
+PQ_API pq_status pq_server_set_pieces(pq_server *s, int32_t split_log2, int32_t piece_log2);
 PQ_API void pq_server_destroy(pq_server *s);
 /* Non-blocking: queues n requests; refused requests complete immediately with a status. */
 PQ_API pq_status pq_server_submit(pq_server *s, int64_t n, const pq_request *reqs);

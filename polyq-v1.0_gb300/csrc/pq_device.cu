@@ -55,6 +55,11 @@ static int unit_max_for(const EngineDev &E, const pq_tuning &tu) {
     return (tu.chunk_tables == 1 && E.ctab) ? 1 : unit_max_of(tu);
 }
 
+// A launch takes the fused single-kernel path when each of its outputs sums at most this many
+// branches (over all of its branch engines): prepare and enumeration of such an output take a
+// few microseconds, less than the launches of a four-kernel sequence.
+static const double kSmallMaxBranches = 16384.0;
+
 static pq_status fail(pq_status s, const std::string &m) {
     g_err = m;
     return s;
@@ -98,8 +103,11 @@ struct DevMem {
     }
     template <class T> T *as() const { return reinterpret_cast<T *>(p); }
 };
+// Pinned host memory, mapped into the device's address space: kernels of small launches read
+// their boundaries from it and write their results to it directly (no copies).
 struct HostPinned {
     void *p = nullptr;
+    void *d = nullptr;  // the device's address of the same memory
     size_t n = 0;
     HostPinned() = default;
     HostPinned(const HostPinned &) = delete;
@@ -109,11 +117,14 @@ struct HostPinned {
     }
     cudaError_t alloc(size_t bytes) {
         if (p) cudaFreeHost(p);
-        p = nullptr;
+        p = d = nullptr;
         n = std::max<size_t>(bytes, 16);
-        return cudaMallocHost(&p, n);
+        cudaError_t e = cudaHostAlloc(&p, n, cudaHostAllocMapped);
+        if (e != cudaSuccess) return e;
+        return cudaHostGetDevicePointer(&d, p, 0);
     }
     template <class T> T *as() const { return reinterpret_cast<T *>(p); }
+    template <class T> T *dev() const { return reinterpret_cast<T *>(d); }
 };
 template <class T> static cudaError_t upload(DevMem &m, const std::vector<T> &v) {
     cudaError_t e = m.alloc(v.size() * sizeof(T));
@@ -247,9 +258,17 @@ static pq_status upload_target(Target &T, int di_max) {
 }
 
 // ------------------------------------------------------------------------ plans
+// `count` boundaries on target tg, each evaluated over branch engines [eb, ee) (ee < 0: all);
+// a segment of one engine may cover only work items [ib, ie) of its jobs (ie < 0: all).
 struct Segment {
     Target *tg;
     int64_t count;
+    int eb = 0, ee = -1;
+    long long ib = 0, ie = -1;
+    Segment(Target *t, int64_t c) : tg(t), count(c) {}
+    Segment(Target *t, int64_t c, int e0, int e1, long long i0, long long i1)
+        : tg(t), count(c), eb(e0), ee(e1), ib(i0), ie(i1) {}
+    int engines() const { return (ee < 0 ? (int)tg->dev.size() : ee) - eb; }
 };
 
 struct Plan {
@@ -270,8 +289,19 @@ struct Plan {
     bool own_stream = false;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
+    // small launches: one fused kernel (small_kernel) instead of the four-kernel sequence; host-
+    // buffer calls run it on mapped pinned memory through their own graph
+    bool fused = false;
+    int fused_grid = 1, fused_block = 32;
+    size_t fused_smem = 0;
+    KArgs args_host{};
+    bool graph_host_ready = false;
+    bool ran = false;           // a graph of this plan has been launched
+    bool last_host_io = false;  // the last launch was a fused one on the mapped host buffers
+    cudaGraph_t graph_host = nullptr;
+    cudaGraphExec_t gexec_host = nullptr;
     DevMem engines, maps, jobs, perm, kinv, istart, jdl, jcpi, jnch, partials, counter, job_vals, job_err, out_jobs,
-        x, y, out, err, errflag;
+        x, y, out, err, errflag, ioff;
     HostPinned hx, hy, hout, herr, herrflag;
     std::vector<int> job_engine_d;
     std::vector<JobDev> jobs_host;
@@ -282,6 +312,8 @@ struct Plan {
     ~Plan() {
         if (gexec) cudaGraphExecDestroy(gexec);
         if (graph) cudaGraphDestroy(graph);
+        if (gexec_host) cudaGraphExecDestroy(gexec_host);
+        if (graph_host) cudaGraphDestroy(graph_host);
         if (ev_in) cudaEventDestroy(ev_in);
         if (ev_out) cudaEventDestroy(ev_out);
         for (auto &e : tev)
@@ -317,13 +349,13 @@ static pq_status build_plan(const std::vector<Segment> &segs, int nw, cudaStream
     if (light) {
         for (DevMem *m : {&P.engines, &P.maps, &P.jobs, &P.perm, &P.kinv, &P.istart, &P.jdl, &P.jcpi, &P.jnch,
                           &P.partials, &P.counter, &P.job_vals, &P.job_err, &P.out_jobs, &P.x, &P.y, &P.out, &P.err,
-                          &P.errflag})
+                          &P.errflag, &P.ioff})
             m->astream = P.stream;
     }
     {
         // (boundary, branch engine) jobs are indexed with 32-bit integers on the device
         double total = 0.0;
-        for (const auto &sg : segs) total += (double)sg.count * (double)sg.tg->dev.size();
+        for (const auto &sg : segs) total += (double)sg.count * (double)sg.engines();
         if (total > (double)(1 << 28))
             return fail(PQ_ERR_INVALID_ARG, "boundaries x branch engines above 2^28 in one launch; split the call");
     }
@@ -332,12 +364,20 @@ static pq_status build_plan(const std::vector<Segment> &segs, int nw, cudaStream
     std::vector<JobDev> jobs;
     std::vector<int> out_jobs;
     std::vector<int> jd;
+    std::vector<long long> jib, jie;  // per job: work-item range [ib, ie) (ie < 0: all)
+    bool ranged = false;
     int64_t req = 0;
     int maxw = 8;
     for (size_t si = 0; si < segs.size(); si++) {
-        Target *T = segs[si].tg;
+        const Segment &sg = segs[si];
+        Target *T = sg.tg;
+        const int e0 = sg.eb, e1 = sg.ee < 0 ? (int)T->dev.size() : sg.ee;
+        if (e0 < 0 || e1 > (int)T->dev.size() || e0 >= e1 || (sg.ie >= 0 && (e1 - e0 != 1 || sg.ib >= sg.ie)))
+            return fail(PQ_ERR_INTERNAL, "bad launch segment");
+        ranged = ranged || sg.ie >= 0 || sg.ib > 0;
         const int ebase = (int)eng.size();
-        for (auto &e : T->dev) {
+        for (int b = e0; b < e1; b++) {
+            const EngineDev &e = T->dev[(size_t)b];
             if (e.rank > kMaxPivots || (e.d > kMaxD && !prepare_only))
                 return fail(PQ_ERR_UNSUPPORTED, "branch engine outside kernel limits");
             if (e.d > tu.max_branch_dim && !prepare_only)
@@ -347,17 +387,19 @@ static pq_status build_plan(const std::vector<Segment> &segs, int nw, cudaStream
         }
         maps.push_back(T->iom_dev);
         maxw = std::max(maxw, T->max_words);
-        for (int64_t r = 0; r < segs[si].count; r++, req++) {
+        for (int64_t r = 0; r < sg.count; r++, req++) {
             out_jobs.push_back((int)jobs.size());
-            for (size_t b = 0; b < T->dev.size(); b++) {
+            for (int b = e0; b < e1; b++) {
                 JobDev J;
                 std::memset(&J, 0, sizeof(J));
-                J.engine = ebase + (int)b;
+                J.engine = ebase + (b - e0);
                 J.iomap = (int)si;
                 J.req = (int)req;
                 J.out = (int)req;
                 jobs.push_back(J);
-                jd.push_back(T->dev[b].d);
+                jd.push_back(T->dev[(size_t)b].d);
+                jib.push_back(sg.ib);
+                jie.push_back(sg.ie);
             }
         }
     }
@@ -390,8 +432,13 @@ static pq_status build_plan(const std::vector<Segment> &segs, int nw, cudaStream
         } else {
             job_shape(E, tu.chunks_per_lane, unit_max_for(E, tu), jdl[j], jnch[j], jcpi[j]);
         }
-        istart[k + 1] = istart[k] + (long long)((jnch[j] + jcpi[j] - 1) / jcpi[j]);
-        P.branches += std::ldexp(1.0, E.d);
+        const long long nit = (long long)((jnch[j] + jcpi[j] - 1) / jcpi[j]);
+        const long long i1 = jie[j] < 0 ? nit : std::min<long long>(jie[j], nit);
+        const long long i0 = std::min<long long>(jib[j], i1);
+        jib[j] = i0;
+        istart[k + 1] = istart[k] + (i1 - i0);
+        P.branches += prepare_only || nit == 0 ? std::ldexp(1.0, E.d)
+                                               : std::ldexp(1.0, E.d) * (double)(i1 - i0) / (double)nit;
         const bool covered = E.ctab && (jdl[j] & 255) == E.DI;
         P.any_ctab = P.any_ctab || covered;
         P.fp32_any = P.fp32_any || E.joint;
@@ -408,6 +455,7 @@ static pq_status build_plan(const std::vector<Segment> &segs, int nw, cudaStream
     CU(upload(P.jcpi, jcpi));
     CU(upload(P.jnch, jnch));
     CU(upload(P.out_jobs, out_jobs));
+    if (ranged) CU(upload(P.ioff, jib));
     CU(P.partials.alloc((size_t)P.nitems * sizeof(double2)));
     CU(P.counter.alloc(sizeof(unsigned long long)));
     CU(P.job_vals.alloc((size_t)P.njobs * sizeof(double2)));
@@ -456,6 +504,7 @@ static pq_status build_plan(const std::vector<Segment> &segs, int nw, cudaStream
     a.smem_words = P.smem_words;
     a.dbg = nullptr;
     a.errflag = P.errflag.as<int>();
+    a.ioff = ranged ? P.ioff.as<long long>() : nullptr;
     const int bw = std::max(1, std::min(8, tu.block_warps));
     P.block_enum = 32 * bw;
     P.minb = (tu.blocks_per_sm >= 2 && tu.blocks_per_sm <= 4) ? tu.blocks_per_sm : 3;
@@ -471,17 +520,57 @@ static pq_status build_plan(const std::vector<Segment> &segs, int nw, cudaStream
         CU(cudaFuncSetAttribute(prepare_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)(4 * P.smem_words * 8)));
     }
+    // one fused kernel when every output is small: at most kSmallMaxJobs branch engines and
+    // kSmallMaxBranches branches summed over them
+    if (!prepare_only) {
+        bool small = true;
+        int maxj = 1;
+        for (const auto &sg : segs) {
+            const int nb = sg.engines();
+            small = small && nb <= kSmallMaxJobs && sg.tg->branches_per_amp <= kSmallMaxBranches;
+            maxj = std::max(maxj, nb);
+        }
+        const int wpb = std::min(maxj, 8);
+        const size_t smem = (size_t)(2 * nw + wpb * P.smem_words) * 8;
+        if (small && smem <= 32 * 1024) {
+            P.fused = true;
+            P.fused_block = 32 * wpb;
+            P.fused_smem = smem;
+            P.fused_grid = (int)std::max<long long>(1, std::min<long long>(P.nout, (long long)sm_count() * 8));
+            if (!light) {
+                P.args_host = P.args;
+                P.args_host.xs = P.hx.dev<uint64_t>();
+                P.args_host.ys = P.hy.dev<uint64_t>();
+                P.args_host.out = P.hout.dev<double>();
+                P.args_host.err = P.herr.dev<double>();
+                P.args_host.errflag = P.herrflag.dev<int>();
+            }
+        }
+    }
     return PQ_OK;
 }
 
 // Enqueue the core launch sequence on P.stream (capturable).  mode 1 walks in FP64; ctab >= 0
 // overrides the plan's use of chunk-sum tables (which, where they apply, are FP64 in either mode).
-static cudaError_t enqueue_core(Plan &P, int mode, int ctab = -1) {
+// `io` (optional) replaces the plan's boundary, result and flag pointers (the mapped host
+// buffers of a fused launch).
+static cudaError_t enqueue_core(Plan &P, int mode, int ctab = -1, const KArgs *io = nullptr) {
     cudaError_t e;
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     if ((e = cudaStreamIsCapturing(P.stream, &cs)) != cudaSuccess) return e;
     // timing events become event-record nodes of the graph while capturing
     const unsigned evflag = cs == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
+    if (P.fused && mode == 0 && (ctab < 0 || ctab == P.args.use_ctab)) {
+        KArgs args = io ? *io : P.args;
+        if ((e = cudaMemsetAsync(args.errflag, 0, sizeof(int), P.stream)) != cudaSuccess) return e;
+        if ((e = cudaEventRecordWithFlags(P.tev[0], P.stream, evflag)) != cudaSuccess) return e;
+        if ((e = cudaEventRecordWithFlags(P.tev[1], P.stream, evflag)) != cudaSuccess) return e;
+        if (P.minb == 2) small_kernel<2><<<P.fused_grid, P.fused_block, P.fused_smem, P.stream>>>(args);
+        else small_kernel<3><<<P.fused_grid, P.fused_block, P.fused_smem, P.stream>>>(args);
+        if ((e = cudaEventRecordWithFlags(P.tev[2], P.stream, evflag)) != cudaSuccess) return e;
+        if ((e = cudaEventRecordWithFlags(P.tev[3], P.stream, evflag)) != cudaSuccess) return e;
+        return cudaGetLastError();
+    }
     e = cudaMemsetAsync(P.errflag.p, 0, sizeof(int), P.stream);
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(P.counter.p, 0, sizeof(unsigned long long), P.stream);
@@ -503,19 +592,41 @@ static cudaError_t enqueue_core(Plan &P, int mode, int ctab = -1) {
     return cudaGetLastError();
 }
 
+static pq_status capture(Plan &P, const KArgs *io, cudaGraph_t &graph, cudaGraphExec_t &gexec) {
+    CU(cudaStreamBeginCapture(P.stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = enqueue_core(P, 0, -1, io);
+    cudaGraph_t g = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(P.stream, &g);
+    if (e != cudaSuccess) { if (g) cudaGraphDestroy(g); return cuda_fail(e, "capture"); }
+    if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
+    graph = g;
+    CU(cudaGraphInstantiate(&gexec, graph, 0));
+    return PQ_OK;
+}
+
 static pq_status launch_graph(Plan &P) {
     if (!P.graph_ready) {
-        CU(cudaStreamBeginCapture(P.stream, cudaStreamCaptureModeThreadLocal));
-        cudaError_t e = enqueue_core(P, 0);
-        cudaGraph_t g = nullptr;
-        cudaError_t e2 = cudaStreamEndCapture(P.stream, &g);
-        if (e != cudaSuccess) { if (g) cudaGraphDestroy(g); return cuda_fail(e, "capture"); }
-        if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
-        P.graph = g;
-        CU(cudaGraphInstantiate(&P.gexec, P.graph, 0));
+        pq_status st = capture(P, nullptr, P.graph, P.gexec);
+        if (st != PQ_OK) return st;
         P.graph_ready = true;
     }
     CU(cudaGraphLaunch(P.gexec, P.stream));
+    P.ran = true;
+    P.last_host_io = false;
+    return PQ_OK;
+}
+
+// Fused plans on host buffers: the kernel reads the boundaries from, and writes the results to,
+// the plan's mapped pinned buffers.  The timing events are shared with launch_graph's graph.
+static pq_status launch_graph_host(Plan &P) {
+    if (!P.graph_host_ready) {
+        pq_status st = capture(P, &P.args_host, P.graph_host, P.gexec_host);
+        if (st != PQ_OK) return st;
+        P.graph_host_ready = true;
+    }
+    CU(cudaGraphLaunch(P.gexec_host, P.stream));
+    P.ran = true;
+    P.last_host_io = true;
     return PQ_OK;
 }
 
@@ -531,13 +642,20 @@ static pq_status run_host(Plan &P, const uint64_t *x, const uint64_t *y, double 
     const size_t bw = (size_t)P.nreq * P.nw * 8;
     std::memcpy(P.hx.p, x, bw);
     std::memcpy(P.hy.p, y, bw);
-    CU(cudaMemcpyAsync(P.x.p, P.hx.p, bw, cudaMemcpyHostToDevice, P.stream));
-    CU(cudaMemcpyAsync(P.y.p, P.hy.p, bw, cudaMemcpyHostToDevice, P.stream));
-    pq_status st = launch_graph(P);
-    if (st != PQ_OK) return st;
-    CU(cudaMemcpyAsync(P.hout.p, P.out.p, (size_t)P.nout * 16, cudaMemcpyDeviceToHost, P.stream));
-    CU(cudaMemcpyAsync(P.herr.p, P.err.p, (size_t)P.nout * 8, cudaMemcpyDeviceToHost, P.stream));
-    CU(cudaMemcpyAsync(P.herrflag.p, P.errflag.p, sizeof(int), cudaMemcpyDeviceToHost, P.stream));
+    pq_status st;
+    if (P.fused) {
+        // one graph launch: the fused kernel reads and writes the mapped buffers
+        st = launch_graph_host(P);
+        if (st != PQ_OK) return st;
+    } else {
+        CU(cudaMemcpyAsync(P.x.p, P.hx.p, bw, cudaMemcpyHostToDevice, P.stream));
+        CU(cudaMemcpyAsync(P.y.p, P.hy.p, bw, cudaMemcpyHostToDevice, P.stream));
+        st = launch_graph(P);
+        if (st != PQ_OK) return st;
+        CU(cudaMemcpyAsync(P.hout.p, P.out.p, (size_t)P.nout * 16, cudaMemcpyDeviceToHost, P.stream));
+        CU(cudaMemcpyAsync(P.herr.p, P.err.p, (size_t)P.nout * 8, cudaMemcpyDeviceToHost, P.stream));
+        CU(cudaMemcpyAsync(P.herrflag.p, P.errflag.p, sizeof(int), cudaMemcpyDeviceToHost, P.stream));
+    }
     CU(cudaStreamSynchronize(P.stream));
     if (*P.herrflag.as<int>()) return fail(PQ_ERR_INTERNAL, "device self-check failed (odd Z8 increment)");
     const double *ho = P.hout.as<double>();
@@ -554,7 +672,13 @@ static pq_status run_host(Plan &P, const uint64_t *x, const uint64_t *y, double 
             if (bound_of(o) > 1e-12) return true;
         return false;
     };
+    bool staged = !P.fused;  // boundaries in the plan's device buffers
     auto rerun = [&](int mode, int ctab) -> pq_status {
+        if (!staged) {
+            CU(cudaMemcpyAsync(P.x.p, P.hx.p, bw, cudaMemcpyHostToDevice, P.stream));
+            CU(cudaMemcpyAsync(P.y.p, P.hy.p, bw, cudaMemcpyHostToDevice, P.stream));
+            staged = true;
+        }
         CU(enqueue_core(P, mode, ctab));
         CU(cudaMemcpyAsync(P.hout.p, P.out.p, (size_t)P.nout * 16, cudaMemcpyDeviceToHost, P.stream));
         CU(cudaMemcpyAsync(P.herr.p, P.err.p, (size_t)P.nout * 8, cudaMemcpyDeviceToHost, P.stream));
@@ -940,30 +1064,43 @@ PQ_API pq_status pq_amplitudes_fp64(pq_sim *s, int64_t n, const uint64_t *x, con
 // Sandwich engines of one measured-qubit list, built and uploaded on first use and cached
 // (caller holds s->mu).  Their fixed set is the first-occurrence order of the variables put
 // by Sandwich::assignment: inputs, C^dagger C outputs, measured junctions (src/sim.rs:95-124).
-static pq_status marg_target(pq_sim *s, const int32_t *qubits, int nmeas, pq_sim::Marg **out) {
-    const int nq = s->circ.nq;
-    std::vector<int> key(qubits, qubits + nmeas);
-    auto it = s->marg.find(key);
-    if (it != s->marg.end()) {
-        *out = it->second.get();
-        return PQ_OK;
-    }
+// The sandwich path sum (built once, under s->mu; immutable afterwards).
+static void ensure_sandwich(pq_sim *s) {
     if (!s->have_sw) {
         s->sw = PathSum::sandwich(s->circ, s->junction, s->jneg);
         s->have_sw = true;
     }
+}
+
+// Build and upload the sandwich engines of one measured-qubit list.  Reads only the simulator's
+// immutable parts (circuit, sandwich path sum, strategy), so it runs without s->mu once
+// ensure_sandwich has run.
+static pq_status marg_build(pq_sim *s, const int32_t *qubits, int nmeas, int di_max, std::unique_ptr<pq_sim::Marg> &M) {
+    const int nq = s->circ.nq;
     std::vector<std::pair<int, int32_t>> puts;
     for (int q = 0; q < nq; q++) puts.push_back({q, io_src(q, 0, 0)});
     for (int q = 0; q < nq; q++) puts.push_back({s->sw.outputs[q], io_src(q, 0, s->sw.out_neg[q])});
     for (int i = 0; i < nmeas; i++) puts.push_back({s->junction[qubits[i]], io_src(qubits[i], 1, s->jneg[qubits[i]])});
-    auto M = std::make_unique<pq_sim::Marg>();
+    M = std::make_unique<pq_sim::Marg>();
     M->tg.iom = build_iomap(puts);
     try {
         M->tg.rs = build_rank(s->sw, M->tg.iom.fixed, s->strategy, s->pairs);
     } catch (const std::exception &e) {
         return fail(PQ_ERR_INTERNAL, std::string("marginal engine build: ") + e.what());
     }
-    pq_status st = upload_target(M->tg, s->di_max);
+    return upload_target(M->tg, di_max);
+}
+
+static pq_status marg_target(pq_sim *s, const int32_t *qubits, int nmeas, pq_sim::Marg **out) {
+    std::vector<int> key(qubits, qubits + nmeas);
+    auto it = s->marg.find(key);
+    if (it != s->marg.end()) {
+        *out = it->second.get();
+        return PQ_OK;
+    }
+    ensure_sandwich(s);
+    std::unique_ptr<pq_sim::Marg> M;
+    pq_status st = marg_build(s, qubits, nmeas, s->di_max, M);
     if (st != PQ_OK) return st;
     *out = M.get();
     s->marg.emplace(key, std::move(M));
@@ -1390,6 +1527,11 @@ PQ_API pq_status pq_sample_many(pq_sim *s, const uint64_t *x, int64_t shots, uin
             any_tie = any_tie || tie[i];
         }
         if (any_tie) {
+            if (P.fused) {  // the fused launch read the boundaries from the mapped buffers
+                const size_t bwb = ns * (size_t)nw * 8;
+                CU(cudaMemcpyAsync(P.x.p, P.hx.p, bwb, cudaMemcpyHostToDevice, P.stream));
+                CU(cudaMemcpyAsync(P.y.p, P.hy.p, bwb, cudaMemcpyHostToDevice, P.stream));
+            }
             CU(enqueue_core(P, 1));
             CU(cudaMemcpyAsync(P.hout.p, P.out.p, ns * 16, cudaMemcpyDeviceToHost, P.stream));
             CU(cudaStreamSynchronize(P.stream));
@@ -1469,12 +1611,13 @@ PQ_API pq_status pq_sim_device_check(pq_sim *s, int64_t n, int32_t *failed) {
     if (!s || !failed) return fail(PQ_ERR_INVALID_ARG, "null argument");
     std::lock_guard<std::mutex> lk(s->mu);
     auto it = s->plans.find(n);
-    if (it == s->plans.end() || !it->second->graph_ready) return fail(PQ_ERR_INVALID_ARG, "no launch of that size yet");
+    if (it == s->plans.end() || !it->second->ran) return fail(PQ_ERR_INVALID_ARG, "no launch of that size yet");
     Plan &P = *it->second;
     CU(cudaSetDevice(s->device));
     CU(cudaStreamSynchronize(P.stream));
     int f = 0;
-    CU(cudaMemcpy(&f, P.errflag.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (P.last_host_io) f = *P.herrflag.as<int>();
+    else CU(cudaMemcpy(&f, P.errflag.p, sizeof(int), cudaMemcpyDeviceToHost));
     *failed = f ? 1 : 0;
     return PQ_OK;
 }
@@ -1483,14 +1626,14 @@ PQ_API pq_status pq_sim_kernel_ms(pq_sim *s, int64_t n, float *ms) {
     if (!s || !ms) return fail(PQ_ERR_INVALID_ARG, "null argument");
     std::lock_guard<std::mutex> lk(s->mu);
     auto it = s->plans.find(n);
-    if (it == s->plans.end() || !it->second->graph_ready) return fail(PQ_ERR_INVALID_ARG, "no launch of that size yet");
+    if (it == s->plans.end() || !it->second->ran) return fail(PQ_ERR_INVALID_ARG, "no launch of that size yet");
     CU(cudaEventSynchronize(it->second->tev[3]));
     return last_kernel_ms(*it->second, ms);
 }
 PQ_API pq_status pq_batch_kernel_ms(pq_batch *b, float *ms) {
     if (!b || !ms) return fail(PQ_ERR_INVALID_ARG, "null argument");
     std::lock_guard<std::mutex> lk(b->mu);
-    if (!b->plan || !b->plan->graph_ready) return fail(PQ_ERR_INVALID_ARG, "batch has not run yet");
+    if (!b->plan || !b->plan->ran) return fail(PQ_ERR_INVALID_ARG, "batch has not run yet");
     CU(cudaEventSynchronize(b->plan->tev[3]));
     return last_kernel_ms(*b->plan, ms);
 }
@@ -1524,13 +1667,13 @@ PQ_API pq_status pq_sim_enumerated(pq_sim *s, int64_t n, double *out, double *pe
     if (!s || !out) return fail(PQ_ERR_INVALID_ARG, "null argument");
     std::lock_guard<std::mutex> lk(s->mu);
     auto it = s->plans.find(n);
-    if (it == s->plans.end() || !it->second->graph_ready) return fail(PQ_ERR_INVALID_ARG, "no launch of that size yet");
+    if (it == s->plans.end() || !it->second->ran) return fail(PQ_ERR_INVALID_ARG, "no launch of that size yet");
     return plan_enumerated(*it->second, out, per_boundary);
 }
 PQ_API pq_status pq_batch_enumerated(pq_batch *b, double *out) {
     if (!b || !out) return fail(PQ_ERR_INVALID_ARG, "null argument");
     std::lock_guard<std::mutex> lk(b->mu);
-    if (!b->plan || !b->plan->graph_ready) return fail(PQ_ERR_INVALID_ARG, "batch has not run yet");
+    if (!b->plan || !b->plan->ran) return fail(PQ_ERR_INVALID_ARG, "batch has not run yet");
     return plan_enumerated(*b->plan, out, nullptr);
 }
 PQ_API int64_t pq_sim_launch_items(pq_sim *s, int64_t n) {
@@ -2065,12 +2208,21 @@ extern "C" PQ_API pq_status pq_amplitudes_noalloc(pq_sim *s, int64_t n, const ui
 namespace pq {
 static const int kSrvStreams = 4;
 
+// A request whose work is above 2^split_log2 branches (pq_server::split_log2, default 28) is
+// evaluated in the background, in pieces -- ranges of its branch engines, or of one engine's work
+// items -- of at most 2^piece_log2 branches each (default 32: about 1.5 ms on half the SMs), one
+// piece per background wave on a reduced grid, so that it never holds the whole device for long.
+
 struct SrvReq {
     pq_request r;
     double t_submit = 0.0;
     Target *tg = nullptr;
     int64_t bytes = 0;
     int precise = 0;  // 0 the FP32 walk; 1 chunk-sum tables; 2 FP64 walk (probability re-evaluation)
+    int64_t group = -1;  // piece of a split request (see pq_server::groups), else -1
+    int pieces = 0;      // of a completed split request: how many pieces it took
+    int eb = 0, ee = -1;
+    long long ib = 0, ie = -1;
 };
 struct SrvWave {
     std::vector<SrvReq> reqs;
@@ -2078,9 +2230,62 @@ struct SrvWave {
     pq_tuning tu{};  // launch shape of the wave
     int slot = -1;
     int precise = 0;
+    bool background = false;  // one piece of a split request
     int64_t bytes = 0;
     cudaEvent_t done = nullptr;
 };
+// The running sum of a split request's pieces.
+struct SrvGroup {
+    SrvReq base;
+    int remaining = 0, npieces = 0;
+    int32_t status = PQ_OK;
+    double re = 0.0, im = 0.0, eb = 0.0;
+};
+
+// Pieces of a request on target T under launch shape tu: consecutive branch engines while their
+// branches stay within `piece`; an engine above it alone, split into ranges of its work
+// items of at most `piece` branches each.
+static std::vector<SrvReq> srv_split(const SrvReq &q, const pq_tuning &tu, double piece) {
+    std::vector<SrvReq> out;
+    const Target &T = *q.tg;
+    const int nb = (int)T.dev.size();
+    int b = 0;
+    while (b < nb) {
+        const EngineDev &E = T.dev[(size_t)b];
+        const double w = std::ldexp(1.0, E.d);
+        if (w > piece) {
+            int dl;
+            unsigned long long nch;
+            unsigned cpi;
+            job_shape(E, tu.chunks_per_lane, unit_max_for(E, tu), dl, nch, cpi);
+            const long long nit = (long long)((nch + cpi - 1) / cpi);
+            const long long per = std::max<long long>(1, (long long)(piece / (w / (double)nit)));
+            for (long long i = 0; i < nit; i += per) {
+                SrvReq p = q;
+                p.eb = b;
+                p.ee = b + 1;
+                p.ib = i;
+                p.ie = std::min(nit, i + per);
+                out.push_back(p);
+            }
+            b++;
+            continue;
+        }
+        double acc = 0.0;
+        int e = b;
+        while (e < nb && std::ldexp(1.0, T.dev[(size_t)e].d) <= piece &&
+               acc + std::ldexp(1.0, T.dev[(size_t)e].d) <= piece) {
+            acc += std::ldexp(1.0, T.dev[(size_t)e].d);
+            e++;
+        }
+        SrvReq p = q;
+        p.eb = b;
+        p.ee = e;
+        out.push_back(p);
+        b = e;
+    }
+    return out;
+}
 
 // The launch shape of a request at a re-evaluation level (1: chunk-sum tables where they apply,
 // the FP32 walk elsewhere; 2: the tables, the FP64 walk elsewhere).
@@ -2139,6 +2344,19 @@ struct pq_server {
     int64_t inflight_bytes = 0;
     bool stop = false;
     std::thread worker;
+    // marginal requests whose sandwich engines are not built yet wait here, by (simulator,
+    // qubit), while the builder thread builds them; the worker keeps admitting other requests
+    std::map<std::pair<int, int>, std::vector<pq::SrvReq>> parked;
+    std::deque<std::pair<int, int>> build_q;
+    std::condition_variable cv_build;
+    std::thread builder;
+    bool stop_builder = false;  // set once the worker has exited
+    // pieces of split requests, launched one per background wave while a stream is free
+    std::deque<pq::SrvReq> bg;
+    std::map<int64_t, pq::SrvGroup> groups;
+    int64_t next_group = 0;
+    bool bg_inflight = false;
+    int split_log2 = 28, piece_log2 = 32;
     ~pq_server() {
         for (auto s : streams) cudaStreamDestroy(s);
         for (auto p : hbuf) cudaFreeHost(p);
@@ -2157,21 +2375,73 @@ static pq_result srv_result(const SrvReq &q, int32_t status, double t) {
     r.submit_s = q.t_submit;
     r.done_s = t;
     r.level = q.precise;
+    r.pieces = q.pieces;
     return r;
 }
 
-// Resolve a request's target (marginal engines are built on first use).
-static pq_status srv_resolve(pq_server *S, SrvReq &q) {
+// Resolve a request's target.  A marginal whose sandwich engines are not built yet returns
+// false: the caller parks it for the builder thread.
+static bool srv_resolve(pq_server *S, SrvReq &q) {
     pq_sim *s = S->sims[q.r.sim];
     if (q.r.kind != PQ_REQ_MARGINAL) {
         q.tg = &s->main;
-        return PQ_OK;
+        return true;
     }
     std::lock_guard<std::mutex> lk(s->mu);
-    pq_sim::Marg *M = nullptr;
-    pq_status st = marg_target(s, &q.r.qubit, 1, &M);
-    if (st == PQ_OK) q.tg = &M->tg;
-    return st;
+    auto it = s->marg.find(std::vector<int>{q.r.qubit});
+    if (it == s->marg.end()) return false;
+    q.tg = &it->second->tg;
+    return true;
+}
+
+// Builder thread: builds the sandwich engines of parked marginal requests, one measured qubit
+// at a time, without holding the server's or the simulator's lock during the build, then
+// returns the requests to the head of the queue (or completes them with the build's error).
+static void srv_build_loop(pq_server *S) {
+    cudaSetDevice(S->device);
+    std::unique_lock<std::mutex> lk(S->mu);
+    while (true) {
+        S->cv_build.wait(lk, [&] { return S->stop_builder || !S->build_q.empty(); });
+        if (S->build_q.empty()) break;  // the worker has exited: nothing can be parked any more
+        const std::pair<int, int> key = S->build_q.front();
+        S->build_q.pop_front();
+        lk.unlock();
+        pq_sim *s = S->sims[key.first];
+        const int32_t qb = key.second;
+        int di = 10;
+        bool have = false;
+        {
+            std::lock_guard<std::mutex> l2(s->mu);
+            ensure_sandwich(s);
+            di = s->di_max;
+            have = s->marg.count(std::vector<int>{qb}) != 0;
+        }
+        pq_status st = PQ_OK;
+        std::string why;
+        if (!have) {
+            std::unique_ptr<pq_sim::Marg> M;
+            st = marg_build(s, &qb, 1, di, M);
+            if (st != PQ_OK) why = g_err;
+            else {
+                std::lock_guard<std::mutex> l2(s->mu);
+                s->marg.emplace(std::vector<int>{qb}, std::move(M));  // kept if another call built it first
+            }
+        }
+        lk.lock();
+        auto it = S->parked.find(key);
+        if (it != S->parked.end()) {
+            std::vector<SrvReq> rs = std::move(it->second);
+            S->parked.erase(it);
+            if (st == PQ_OK) {
+                for (auto r = rs.rbegin(); r != rs.rend(); ++r) S->pending.push_front(*r);
+            } else {
+                const double t = srv_now(S);
+                for (auto &r : rs) S->finished.push_back(srv_result(r, st, t));
+                S->cv_done.notify_all();
+            }
+        }
+        S->cv_work.notify_all();
+    }
 }
 
 static pq_status srv_launch(pq_server *S, SrvWave &w, const pq_tuning &tu) {
@@ -2179,7 +2449,9 @@ static pq_status srv_launch(pq_server *S, SrvWave &w, const pq_tuning &tu) {
     std::stable_sort(w.reqs.begin(), w.reqs.end(), [](const SrvReq &a, const SrvReq &b) { return a.tg < b.tg; });
     std::vector<Segment> segs;
     for (auto &q : w.reqs) {
-        if (segs.empty() || segs.back().tg != q.tg) segs.push_back({q.tg, 0});
+        const bool same = !segs.empty() && segs.back().tg == q.tg && segs.back().eb == q.eb && segs.back().ee == q.ee &&
+                          segs.back().ib == q.ib && segs.back().ie == q.ie;
+        if (!same) segs.push_back(Segment(q.tg, 0, q.eb, q.ee, q.ib, q.ie));
         segs.back().count++;
     }
     const int n = (int)w.reqs.size();
@@ -2202,6 +2474,8 @@ static pq_status srv_launch(pq_server *S, SrvWave &w, const pq_tuning &tu) {
     pq_status ps = build_plan(segs, 2, st, w.tu, *w.plan, true);
     if (ps != PQ_OK) return ps;
     Plan &P = *w.plan;
+    // a background piece runs on one block per SM, leaving room for foreground waves
+    if (w.background) P.grid_enum = std::min(P.grid_enum, sm_count());
     CU(cudaMemcpyAsync(P.x.p, xs.data(), xs.size() * 8, cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(P.y.p, ys.data(), ys.size() * 8, cudaMemcpyHostToDevice, st));
     CU(enqueue_core(P, w.precise == 2 ? 1 : 0));
@@ -2211,6 +2485,49 @@ static pq_status srv_launch(pq_server *S, SrvWave &w, const pq_tuning &tu) {
     CU(cudaEventCreateWithFlags(&w.done, cudaEventDisableTiming));
     CU(cudaEventRecord(w.done, st));
     return PQ_OK;
+}
+
+// Completion of request rq with value (re, im) and bound eb from a launch at tuning tu that did
+// (used) or did not use chunk-sum tables.  Probabilities and marginals are promised to 1e-12
+// absolute: when the bound cannot show it, the request goes back to the head of the queue at the
+// next level that can tighten it -- the chunk-sum tables where some engine has them and this
+// launch did not use them, else the FP64 walk where some engine walked in FP32 (engines without a
+// joint table already used FP64 weights).  Caller holds S->mu.
+static void srv_complete(pq_server *S, const SrvReq &rq, int32_t status, double re, double im, double eb,
+                         const pq_tuning &tu, bool used, double t) {
+    pq_result r = srv_result(rq, status, t);
+    if (status == PQ_OK && rq.r.kind != PQ_REQ_AMPLITUDE && rq.precise < 2) {
+        const double pb = rq.r.kind == PQ_REQ_PROBABILITY ? eb * (2.0 * std::sqrt(re * re + im * im) + eb) : eb;
+        if (pb > 1e-12) {
+            bool any_ctab = false, fp32_any = false, fp32_rest = false;
+            eval_cover(*rq.tg, tu, any_ctab, fp32_any, fp32_rest);
+            const int next = !used && any_ctab ? 1 : ((used ? fp32_rest : fp32_any) ? 2 : -1);
+            if (next > 0) {
+                SrvReq again = rq;
+                again.precise = next;
+                again.pieces = 0;
+                again.group = -1;
+                again.eb = 0;
+                again.ee = -1;
+                again.ib = 0;
+                again.ie = -1;
+                S->pending.push_front(again);
+                return;
+            }
+        }
+    }
+    if (rq.r.kind == PQ_REQ_AMPLITUDE) {
+        r.re = re;
+        r.im = im;
+        r.errbound = eb;
+    } else if (rq.r.kind == PQ_REQ_PROBABILITY) {
+        r.re = re * re + im * im;
+        r.errbound = eb * (2.0 * std::sqrt(r.re) + eb);
+    } else {
+        r.re = re > 0.0 ? re : 0.0;
+        r.errbound = eb;
+    }
+    S->finished.push_back(r);
 }
 
 static void srv_loop(pq_server *S) {
@@ -2228,45 +2545,32 @@ static void srv_loop(pq_server *S) {
             }
             const double t = srv_now(S);
             const double *hb = S->hbuf[w->slot];
+            const bool used = w->plan && w->plan->args.use_ctab;
+            const int32_t status = q == cudaSuccess ? PQ_OK : PQ_ERR_DEVICE;
             for (size_t k = 0; k < w->reqs.size(); k++) {
                 const SrvReq &rq = w->reqs[k];
-                pq_result r = srv_result(rq, q == cudaSuccess ? PQ_OK : PQ_ERR_DEVICE, t);
                 const double re = hb[2 * k], im = hb[2 * k + 1], eb = hb[2 * S->max_slots + k];
-                if (q == cudaSuccess && rq.r.kind != PQ_REQ_AMPLITUDE && rq.precise < 2) {
-                    // probabilities (and marginals) are promised to 1e-12 absolute: when the
-                    // bound cannot show it, the request is re-evaluated at the next level that
-                    // can tighten it -- the chunk-sum tables where some engine has them and
-                    // this wave did not use them, else the FP64 walk where some engine walked
-                    // in FP32 (engines without a joint table already used FP64 weights)
-                    const double pb = rq.r.kind == PQ_REQ_PROBABILITY
-                                          ? eb * (2.0 * std::sqrt(re * re + im * im) + eb)
-                                          : eb;
-                    if (pb > 1e-12) {
-                        bool any_ctab = false, fp32_any = false, fp32_rest = false;
-                        eval_cover(*rq.tg, w->tu, any_ctab, fp32_any, fp32_rest);
-                        const bool used = w->plan && w->plan->args.use_ctab;
-                        const int next = !used && any_ctab ? 1 : ((used ? fp32_rest : fp32_any) ? 2 : -1);
-                        if (next > 0) {
-                            SrvReq again = rq;
-                            again.precise = next;
-                            S->pending.push_front(again);
-                            continue;
-                        }
-                    }
+                if (rq.group < 0) {
+                    srv_complete(S, rq, status, re, im, eb, w->tu, used, t);
+                    continue;
                 }
-                if (rq.r.kind == PQ_REQ_AMPLITUDE) {
-                    r.re = re;
-                    r.im = im;
-                    r.errbound = eb;
-                } else if (rq.r.kind == PQ_REQ_PROBABILITY) {
-                    r.re = re * re + im * im;
-                    r.errbound = eb * (2.0 * std::sqrt(r.re) + eb);
-                } else {
-                    r.re = re > 0.0 ? re : 0.0;
-                    r.errbound = eb;
-                }
-                S->finished.push_back(r);
+                // a piece: add it to its request's sum (in piece order: one piece at a time)
+                auto g = S->groups.find(rq.group);
+                if (g == S->groups.end()) continue;
+                SrvGroup &G = g->second;
+                if (status != PQ_OK) G.status = status;
+                G.re += re;
+                G.im += im;
+                G.eb += eb;
+                if (--G.remaining > 0) continue;
+                SrvGroup done = G;
+                S->groups.erase(g);
+                done.base.pieces = done.npieces;
+                // FP64 sums of the pieces: a few ulp of the magnitude
+                const double eb2 = done.eb + 4.0 * 1.1102230246251565e-16 * std::sqrt(done.re * done.re + done.im * done.im);
+                srv_complete(S, done.base, done.status, done.re, done.im, eb2, w->tu, used, t);
             }
+            if (w->background) S->bg_inflight = false;
             S->inflight_bytes -= w->bytes;
             S->busy[w->slot] = 0;
             std::unique_ptr<SrvWave> dead = std::move(S->inflight[i]);
@@ -2278,13 +2582,20 @@ static void srv_loop(pq_server *S) {
             progressed = true;
         }
         if (progressed) S->cv_done.notify_all();
-        if (S->stop && S->pending.empty() && S->inflight.empty()) break;
-        int slot = -1;
-        for (int k = 0; k < (int)S->busy.size(); k++)
-            if (!S->busy[k]) {
-                slot = k;
-                break;
-            }
+        if (S->stop && S->pending.empty() && S->inflight.empty() && S->parked.empty() && S->bg.empty()) break;
+        auto free_slot = [&]() {
+            for (int k = 0; k < (int)S->busy.size(); k++)
+                if (!S->busy[k]) return k;
+            return -1;
+        };
+        int slot = free_slot();
+        pq_tuning tu;
+        {
+            std::lock_guard<std::mutex> g(g_mu);
+            tu = g_tuning;
+        }
+        tu.max_branch_dim = std::min(tu.max_branch_dim, S->max_d);
+        bool launched = false;
         if (slot >= 0 && !S->pending.empty()) {
             // candidates from the head of the queue
             std::vector<SrvReq> cand;
@@ -2294,29 +2605,30 @@ static void srv_loop(pq_server *S) {
             }
             const int64_t room = S->budget - S->inflight_bytes;
             lk.unlock();
-            pq_tuning tu;
-            {
-                std::lock_guard<std::mutex> g(g_mu);
-                tu = g_tuning;
-            }
-            tu.max_branch_dim = std::min(tu.max_branch_dim, S->max_d);
             std::vector<pq_result> refused;
             auto w = std::make_unique<SrvWave>();
-            std::vector<SrvReq> back;
+            std::vector<SrvReq> back, park, split;
             w->precise = cand.empty() ? 0 : cand.front().precise;
             for (auto &q : cand) {
                 if (!back.empty() || q.precise != w->precise) {  // one re-evaluation level per wave
                     back.push_back(q);
                     continue;
                 }
-                pq_status st = srv_resolve(S, q);
-                if (st != PQ_OK) {
-                    refused.push_back(srv_result(q, st, srv_now(S)));
+                if (!srv_resolve(S, q)) {
+                    park.push_back(q);
                     continue;
                 }
                 // work of the request: branches over all of its branch engines
+                if (q.tg->branches_per_amp > std::ldexp(1.0, S->max_d)) {
+                    refused.push_back(srv_result(q, PQ_ERR_ADMISSION_REFUSED, srv_now(S)));
+                    continue;
+                }
+                if (q.tg->branches_per_amp > std::ldexp(1.0, S->split_log2)) {
+                    split.push_back(q);
+                    continue;
+                }
                 q.bytes = request_bytes(*q.tg, srv_tuning(tu, q.precise));
-                if (q.tg->branches_per_amp > std::ldexp(1.0, S->max_d) || q.bytes > S->budget) {
+                if (q.bytes > S->budget) {
                     refused.push_back(srv_result(q, PQ_ERR_ADMISSION_REFUSED, srv_now(S)));
                     continue;
                 }
@@ -2340,15 +2652,77 @@ static void srv_loop(pq_server *S) {
             }
             lk.lock();
             for (auto it = back.rbegin(); it != back.rend(); ++it) S->pending.push_front(*it);
+            for (auto &q : park) {
+                const std::pair<int, int> key(q.r.sim, q.r.qubit);
+                auto &v = S->parked[key];
+                if (v.empty()) {
+                    S->build_q.push_back(key);
+                    S->cv_build.notify_one();
+                }
+                v.push_back(q);
+            }
+            for (auto &q : split) {
+                std::vector<SrvReq> pieces = srv_split(q, srv_tuning(tu, q.precise), std::ldexp(1.0, S->piece_log2));
+                const int64_t gid = S->next_group++;
+                SrvGroup G;
+                G.base = q;
+                G.remaining = G.npieces = (int)pieces.size();
+                S->groups[gid] = G;
+                for (auto &pc : pieces) {
+                    pc.group = gid;
+                    pc.bytes = request_bytes(*pc.tg, srv_tuning(tu, pc.precise));
+                    S->bg.push_back(pc);
+                }
+            }
             for (auto &r : refused) S->finished.push_back(r);
             if (!refused.empty()) S->cv_done.notify_all();
             if (!w->reqs.empty()) {
                 S->busy[slot] = 1;
                 S->inflight_bytes += w->bytes;
                 S->inflight.push_back(std::move(w));
-                continue;
+            }
+            // requests were moved on (launched, parked, split or refused): look at the queue again
+            launched = launched || !w || !park.empty() || !split.empty() || !refused.empty();
+        }
+        // one background piece at a time, on a free stream, when memory allows
+        slot = free_slot();
+        if (slot >= 0 && !S->bg_inflight && !S->bg.empty() &&
+            S->bg.front().bytes <= S->budget - S->inflight_bytes) {
+            auto w = std::make_unique<SrvWave>();
+            w->reqs.push_back(S->bg.front());
+            S->bg.pop_front();
+            w->precise = w->reqs[0].precise;
+            w->background = true;
+            w->bytes = w->reqs[0].bytes;
+            w->slot = slot;
+            S->busy[slot] = 1;
+            S->bg_inflight = true;
+            S->inflight_bytes += w->bytes;
+            lk.unlock();
+            pq_status lst = srv_launch(S, *w, tu);
+            lk.lock();
+            if (lst != PQ_OK) {
+                // the piece's request completes with the launch's error once its other pieces are in
+                auto g = S->groups.find(w->reqs[0].group);
+                if (g != S->groups.end()) {
+                    g->second.status = lst;
+                    if (--g->second.remaining == 0) {
+                        S->finished.push_back(srv_result(g->second.base, lst, srv_now(S)));
+                        S->groups.erase(g);
+                        S->cv_done.notify_all();
+                    }
+                }
+                if (w->done) cudaEventDestroy(w->done);
+                w->plan.reset();
+                S->busy[slot] = 0;
+                S->bg_inflight = false;
+                S->inflight_bytes -= w->bytes;
+            } else {
+                S->inflight.push_back(std::move(w));
+                launched = true;
             }
         }
+        if (launched) continue;
         // nothing launchable now: wait for a submission or poll in-flight waves again
         S->cv_work.wait_for(lk, std::chrono::microseconds(S->inflight.empty() ? 2000 : 50));
     }
@@ -2385,7 +2759,17 @@ PQ_API pq_status pq_server_create(int32_t nsims, pq_sim *const *sims, int32_t ma
     }
     pq_server *raw = S.release();
     raw->worker = std::thread(srv_loop, raw);
+    raw->builder = std::thread(srv_build_loop, raw);
     *out = raw;
+    return PQ_OK;
+}
+
+PQ_API pq_status pq_server_set_pieces(pq_server *s, int32_t split_log2, int32_t piece_log2) {
+    if (!s || split_log2 < 10 || split_log2 > 62 || piece_log2 < split_log2 - 8 || piece_log2 > 62)
+        return fail(PQ_ERR_INVALID_ARG, "split_log2 in 10..62, piece_log2 in split_log2-8..62");
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->split_log2 = split_log2;
+    s->piece_log2 = piece_log2;
     return PQ_OK;
 }
 
@@ -2396,7 +2780,15 @@ PQ_API void pq_server_destroy(pq_server *s) {
         s->stop = true;
     }
     s->cv_work.notify_all();
+    // the worker finishes every queued and parked request (the builder keeps building for it),
+    // then the builder stops
     if (s->worker.joinable()) s->worker.join();
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop_builder = true;
+    }
+    s->cv_build.notify_all();
+    if (s->builder.joinable()) s->builder.join();
     delete s;
 }
 
@@ -2451,7 +2843,10 @@ PQ_API pq_status pq_server_drain(pq_server *s, double timeout_s) {
     if (!s) return fail(PQ_ERR_INVALID_ARG, "null server");
     std::unique_lock<std::mutex> lk(s->mu);
     bool ok = s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s),
-                                  [&] { return s->pending.empty() && s->inflight.empty(); });
+                                  [&] {
+                                      return s->pending.empty() && s->inflight.empty() && s->parked.empty() &&
+                                             s->bg.empty() && s->groups.empty();
+                                  });
     return ok ? PQ_OK : fail(PQ_ERR_TIMEOUT, "requests still pending after the timeout");
 }
 

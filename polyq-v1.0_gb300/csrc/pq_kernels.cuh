@@ -59,6 +59,8 @@ struct KArgs {
     int lpx_stride;
     int use_ctab;               // chunk sums from the engines' chunk-sum tables where they apply
     int fp64_mode;              // the enumeration ran with FP64 weights (error bound of that path)
+    const long long *ioff;      // optional, per job: index of its first work item (a launch that
+                                // evaluates a range of a job's items; null: all of them)
 };
 
 __device__ __forceinline__ int warp_sum_i(int v) {
@@ -71,74 +73,81 @@ __device__ __forceinline__ unsigned warp_sum_u(unsigned v) {
 }
 
 // ------------------------------------------------------------------------------ prepare
+// One (branch engine, boundary) job on one warp: boundary bits x, y -> fixed values, fixed
+// constants, boundary shift, radical system, start shift, k0 and Lp (src/engine.rs:569-610).
+// u: this warp's scratch of at least W + ceil(nf / 64) words.
+__device__ __forceinline__ void prepare_job(const KArgs &a, int jid, const uint64_t *x, const uint64_t *y,
+                                            uint64_t *u, int lane) {
+    JobDev *J = &a.jobs[jid];
+    const EngineDev &E = a.engines[J->engine];
+    const IoMapDev &M = a.maps[J->iomap];
+    uint64_t *vals = u + E.W;
+    // fixed-variable values from the boundary bits
+    for (int base = 0; base < E.nf; base += 64) {
+        int i0 = base + lane, i1 = base + 32 + lane;
+        int b0 = i0 < E.nf ? src_bit(M.src[i0], x, y) : 0;
+        int b1 = i1 < E.nf ? src_bit(M.src[i1], x, y) : 0;
+        unsigned lo = __ballot_sync(PQ_FULL, b0), hi = __ballot_sync(PQ_FULL, b1);
+        if (lane == 0) vals[base >> 6] = (uint64_t)lo | ((uint64_t)hi << 32);
+    }
+    __syncwarp();
+    int bad = 0;
+    for (int c = lane; c < M.ncf; c += 32) bad |= bit_at(vals, M.cf_pos[c]) != src_bit(M.cf_src[c], x, y);
+    bad = __any_sync(PQ_FULL, bad) || E.zero;
+    // constants from fixed-fixed terms (engine.rs:575-588)
+    uint32_t z4 = 0, th = 0;
+    fixed_constants_partial(E, vals, lane, 32, z4, th);
+    z4 = warp_sum_u(z4);
+    th = warp_sum_u(th);
+    // u0 = xor of boundary columns (engine.rs:589-592)
+    boundary_shift_partial(E, vals, u, lane, 32);
+    __syncwarp();
+    // radical system K s = kappa (engine.rs:593-597, :188-201)
+    int badc = 0;
+    for (int r = lane; r < E.ncons; r += 32) badc |= kappa_dot(E, E.cons + (size_t)r * E.we, u);
+    bad = bad || __any_sync(PQ_FULL, badc);
+    uint64_t y0 = 0;
+    for (int base = 0; base < E.rank; base += 32) {
+        int i = base + lane;
+        int bit = i < E.rank ? kappa_dot(E, E.pivrow + (size_t)i * E.we, u) : 0;
+        y0 |= (uint64_t)__ballot_sync(PQ_FULL, bit) << base;
+    }
+    // start shift u = u0 ^ sum of the pivot columns (engine.rs:598-607)
+    apply_pivots_partial(E, y0, u, lane, 32);
+    __syncwarp();
+    int n1 = 0, cnt = 0;
+    phase8_partial(E, u, nullptr, lane, 32, n1, cnt);
+    n1 = warp_sum_i(n1);
+    cnt = warp_sum_i(cnt);
+    const uint32_t k0 = phase8_finish(E, n1, cnt);
+    int lerr = 0;
+    for (int j = lane; j < E.d; j += 32) {
+        int a1 = 0, c1 = 0;
+        phase8_partial(E, u, E.ku + (size_t)j * E.abo, 0, 1, a1, c1);
+        uint32_t L = (phase8_finish(E, a1, c1) - k0) & 7u;
+        lerr |= (int)(L & 1u);
+        if (j < 64) J->Lp[j] = (uint8_t)(L >> 1);
+        if (a.lpx) a.lpx[(size_t)jid * a.lpx_stride + j] = (uint8_t)(L >> 1);
+    }
+    lerr = __any_sync(PQ_FULL, lerr);
+    if (lane == 0) {
+        J->vanish = bad ? 1 : 0;
+        J->phase = E.global + th + ((z4 & 3u) << 30);
+        J->k0 = k0;
+        J->y0 = y0;
+        J->err = (uint32_t)lerr;
+        if (lerr) atomicOr(a.errflag, 1);
+    }
+    __syncwarp();
+}
+
 __global__ void __launch_bounds__(128) prepare_kernel(KArgs a) {
     extern __shared__ uint64_t psm[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
     uint64_t *u = psm + (size_t)wib * a.smem_words;
     for (int jid = blockIdx.x * wpb + wib; jid < a.njobs; jid += gridDim.x * wpb) {
-        JobDev *J = &a.jobs[jid];
-        const EngineDev &E = a.engines[J->engine];
-        const IoMapDev &M = a.maps[J->iomap];
-        const uint64_t *x = a.xs + (size_t)J->req * a.nw;
-        const uint64_t *y = a.ys + (size_t)J->req * a.nw;
-        uint64_t *vals = u + E.W;
-        // fixed-variable values from the boundary bits
-        for (int base = 0; base < E.nf; base += 64) {
-            int i0 = base + lane, i1 = base + 32 + lane;
-            int b0 = i0 < E.nf ? src_bit(M.src[i0], x, y) : 0;
-            int b1 = i1 < E.nf ? src_bit(M.src[i1], x, y) : 0;
-            unsigned lo = __ballot_sync(PQ_FULL, b0), hi = __ballot_sync(PQ_FULL, b1);
-            if (lane == 0) vals[base >> 6] = (uint64_t)lo | ((uint64_t)hi << 32);
-        }
-        __syncwarp();
-        int bad = 0;
-        for (int c = lane; c < M.ncf; c += 32) bad |= bit_at(vals, M.cf_pos[c]) != src_bit(M.cf_src[c], x, y);
-        bad = __any_sync(PQ_FULL, bad) || E.zero;
-        // constants from fixed-fixed terms (engine.rs:575-588)
-        uint32_t z4 = 0, th = 0;
-        fixed_constants_partial(E, vals, lane, 32, z4, th);
-        z4 = warp_sum_u(z4);
-        th = warp_sum_u(th);
-        // u0 = xor of boundary columns (engine.rs:589-592)
-        boundary_shift_partial(E, vals, u, lane, 32);
-        __syncwarp();
-        // radical system K s = kappa (engine.rs:593-597, :188-201)
-        int badc = 0;
-        for (int r = lane; r < E.ncons; r += 32) badc |= kappa_dot(E, E.cons + (size_t)r * E.we, u);
-        bad = bad || __any_sync(PQ_FULL, badc);
-        uint64_t y0 = 0;
-        for (int base = 0; base < E.rank; base += 32) {
-            int i = base + lane;
-            int bit = i < E.rank ? kappa_dot(E, E.pivrow + (size_t)i * E.we, u) : 0;
-            y0 |= (uint64_t)__ballot_sync(PQ_FULL, bit) << base;
-        }
-        // start shift u = u0 ^ sum of the pivot columns (engine.rs:598-607)
-        apply_pivots_partial(E, y0, u, lane, 32);
-        __syncwarp();
-        int n1 = 0, cnt = 0;
-        phase8_partial(E, u, nullptr, lane, 32, n1, cnt);
-        n1 = warp_sum_i(n1);
-        cnt = warp_sum_i(cnt);
-        const uint32_t k0 = phase8_finish(E, n1, cnt);
-        int lerr = 0;
-        for (int j = lane; j < E.d; j += 32) {
-            int a1 = 0, c1 = 0;
-            phase8_partial(E, u, E.ku + (size_t)j * E.abo, 0, 1, a1, c1);
-            uint32_t L = (phase8_finish(E, a1, c1) - k0) & 7u;
-            lerr |= (int)(L & 1u);
-            if (j < 64) J->Lp[j] = (uint8_t)(L >> 1);
-            if (a.lpx) a.lpx[(size_t)jid * a.lpx_stride + j] = (uint8_t)(L >> 1);
-        }
-        lerr = __any_sync(PQ_FULL, lerr);
-        if (lane == 0) {
-            J->vanish = bad ? 1 : 0;
-            J->phase = E.global + th + ((z4 & 3u) << 30);
-            J->k0 = k0;
-            J->y0 = y0;
-            J->err = (uint32_t)lerr;
-            if (lerr) atomicOr(a.errflag, 1);
-        }
-        __syncwarp();
+        const int req = a.jobs[jid].req;
+        prepare_job(a, jid, a.xs + (size_t)req * a.nw, a.ys + (size_t)req * a.nw, u, lane);
     }
 }
 
@@ -466,6 +475,196 @@ __device__ __forceinline__ void walk_unit(const EngineDev &E, const JobDev &J, c
     accy += ux * chi.y + uy * chi.x;
 }
 
+// Stage job jb's walk data (quadratic form rows, pivot masks, Z4 increments and their negatives,
+// table byte strides) into one warp's shared arrays.
+__device__ __forceinline__ void stage_job(const KArgs &a, int jb, uint64_t *G, uint64_t *R, uint8_t *Lp, uint8_t *Lm,
+                                          uint32_t *Tg, int lane) {
+    const JobDev &J = a.jobs[jb];
+    const EngineDev &E = a.engines[J.engine];
+    __syncwarp();
+    const int dlj = a.jdl[jb] & 255;
+    for (int j = lane; j < E.d; j += 32) {
+        G[j] = E.G[j];
+        R[j] = E.R[j];
+        Lp[j] = J.Lp[j];
+        Lm[j] = (uint8_t)((4u - J.Lp[j]) & 3u);
+        if (j < dlj) Tg[j] = ((1u << j) | ((uint32_t)E.R[j] << E.DI)) << 4;
+    }
+    __syncwarp();
+}
+
+// Sum of work item iin of job `job` (its staged data in G, R, Lp, Lm, Tg): every lane walks its
+// units, then an FP64 warp-shuffle reduce in a fixed order; lane 0's value is the item's partial.
+template <int MODE, int MINB>
+__device__ __forceinline__ double2 item_partial(const KArgs &a, int job, long long iin, const uint64_t *G,
+                                                const uint64_t *R, const uint8_t *Lp, const uint8_t *Lm,
+                                                const uint32_t *Tg, int lane) {
+    const JobDev &J = a.jobs[job];
+    const EngineDev &E = a.engines[J.engine];
+    double accx = 0.0, accy = 0.0;
+    if (!J.vanish) {
+        const int dl = a.jdl[job] & 255;
+        const int np = (a.jdl[job] >> 8) & 3;  // pair coordinates used by this job's units
+        const int nk = 1 << np;
+        const unsigned cpi = a.jcpi[job];
+        const unsigned long long nun = a.jnch[job];
+        const unsigned long long c0 = (unsigned long long)iin * cpi;
+        unsigned long long cend = c0 + cpi;
+        if (cend > nun) cend = nun;
+        const uint64_t lomask = (E.DI >= 64) ? ~0ull : ((1ull << E.DI) - 1ull);
+        const uint32_t steps = 1u << dl;
+        if (MODE != 2 && a.use_ctab && E.ctab && dl == E.DI && np == 0 && (cpi & (cpi - 1)) == 0) {
+            // Chunk-sum tables: lane l sums the item's chunks base .. base + q - 1 (base =
+            // c0 + l q, q = cpi / 32 a power of two) in Gray order, one FP64 table lookup per
+            // chunk.  A step flips one high coordinate j: the folded index gains
+            // +-Lp_j + 2 parity(G_j & s), the pivot bits R_j, the low-coordinate signs b the
+            // row G_j; chunks past the item's end are walked but not added.
+            const unsigned long long q = (unsigned long long)(cpi >> 5) ? (unsigned long long)(cpi >> 5) : 1ull;
+            const unsigned long long base = c0 + (unsigned long long)lane * q;
+            if (base < cend) {
+                uint64_t s = (uint64_t)base << dl;
+                uint32_t m;
+                uint64_t yy;
+                chunk_start(Lp, G, R, J.y0, s, m, yy);
+                uint32_t b = 0;
+                for (int j = 0; j < dl; j++)
+                    b |= (((uint32_t)(Lp[j] >> 1) ^ (uint32_t)popc64(G[j] & s)) & 1u) << j;
+                const uint32_t lm32 = (uint32_t)lomask;
+                // the run varies the coordinates dl .. dl + log2(q) - 1; when they all lie in
+                // the first byte slice of the high weight, the other slices are one factor
+                const bool one_slice = (dl + ctz64(q)) <= E.DI + 8;
+                double rx = 0.0, ry = 0.0;
+                for (unsigned long long i = 0;; ++i) {
+                    const unsigned long long ch = base + (i ^ (i >> 1));
+                    if (ch < cend) {
+                        const double2 v = rot4d(E.ctab[(yy << E.DI) | b], m & 3u);
+                        const double2 chi = one_slice ? (E.nsl_th > 0 ? E.th[(int)((s >> E.DI) & 255ull)]
+                                                                      : make_double2(1.0, 0.0))
+                                                      : chunk_high_weight(E, s);
+                        rx += v.x * chi.x - v.y * chi.y;
+                        ry += v.x * chi.y + v.y * chi.x;
+                    }
+                    if (i + 1 == q) break;
+                    const int j = dl + ctz64(i + 1);
+                    m += (((s >> j) & 1ull) ? Lm[j] : Lp[j]) + 2u * (uint32_t)(popc64(G[j] & s) & 1);
+                    yy ^= R[j];
+                    b ^= (uint32_t)G[j] & lm32;
+                    s ^= 1ull << j;
+                }
+                double2 rest = make_double2(1.0, 0.0);
+                if (one_slice)
+                    for (int sl = 1; sl < E.nsl_th; sl++)
+                        rest = cmul_d(rest, E.th[sl * 256 + (int)((s >> (E.DI + 8 * sl)) & 255ull)]);
+                accx += rx * rest.x - ry * rest.y;
+                accy += rx * rest.y + ry * rest.x;
+            }
+        } else
+        for (unsigned long long un = c0 + lane; un < cend; un += 32) {
+            // unit -> its first chunk (zeros inserted at the pair coordinates' chunk bits)
+            unsigned long long ch = un;
+            for (int i = 0; i < np; i++) ch = insert_zero(ch, E.pairc[i] - dl);
+            const uint64_t s1 = (uint64_t)ch << dl;
+            if (MODE != 2 && a.use_ctab && E.ctab && dl == E.DI) {
+                // chunk-sum tables on a plan laid out for the walk (units of several
+                // chunks): each chunk from its own start
+                for (int kc = 0; kc < nk; kc++) {
+                    uint64_t s = s1;
+                    for (int i = 0; i < np; i++)
+                        if ((kc >> i) & 1) s |= 1ull << E.pairc[i];
+                    uint32_t m;
+                    uint64_t yy;
+                    chunk_start(Lp, G, R, J.y0, s, m, yy);
+                    uint32_t b = 0;
+                    for (int j = 0; j < dl; j++)
+                        b |= (((uint32_t)(Lp[j] >> 1) ^ (uint32_t)popc64(G[j] & s)) & 1u) << j;
+                    const double2 v = rot4d(E.ctab[(yy << E.DI) | b], m & 3u);
+                    const double2 chi = chunk_high_weight(E, s);
+                    accx += v.x * chi.x - v.y * chi.y;
+                    accy += v.x * chi.y + v.y * chi.x;
+                }
+                continue;
+            }
+            if (MODE != 1 && E.joint && dl >= 3) {
+                if (np == 3) {
+                    if (MINB == 2) {  // eight accumulators per lane: only with the 128-register budget
+                        walk_unit<MODE, (MINB == 2 ? 8 : 4)>(E, J, G, R, Lp, Tg, dl, s1, lomask, a.dbg, accx, accy);
+                    } else {
+                        walk_unit<MODE, 4>(E, J, G, R, Lp, Tg, dl, s1, lomask, a.dbg, accx, accy);
+                        walk_unit<MODE, 4>(E, J, G, R, Lp, Tg, dl, s1 | (1ull << E.pairc[2]), lomask, a.dbg, accx,
+                                           accy);
+                    }
+                } else if (np == 2) walk_unit<MODE, 4>(E, J, G, R, Lp, Tg, dl, s1, lomask, a.dbg, accx, accy);
+                else if (np == 1) walk_unit<MODE, 2>(E, J, G, R, Lp, Tg, dl, s1, lomask, a.dbg, accx, accy);
+                else walk_unit<MODE, 1>(E, J, G, R, Lp, Tg, dl, s1, lomask, a.dbg, accx, accy);
+                continue;
+            }
+            const uint64_t himask = ~lomask;
+            for (int kc = 0; kc < nk; kc++) {
+                uint64_t s = s1;
+                for (int i = 0; i < np; i++)
+                    if ((kc >> i) & 1) s |= 1ull << E.pairc[i];
+                uint32_t m;
+                uint64_t yy;
+                chunk_start(Lp, G, R, J.y0, s, m, yy);
+                uint64_t ss = s;
+                double vx, vy;  // the chunk's sum before the weight of the coordinates >= DI
+                if (MODE == 1 || !E.joint) {
+                    // FP64 weights and accumulation (verification mode, and engines with more
+                    // pivots than the joint table holds)
+                    double sx = 0.0, sy = 0.0;
+                    for (uint32_t i = 1;; ++i) {
+                        if (MODE == 2) a.dbg[ss] = (uint8_t)((J.k0 + 2u * m) & 7u);
+                        double2 w = E.tlo64[ss & lomask];
+                        for (int sl = 0; sl < E.nsl_tp; sl++)
+                            w = cmul_d(w, E.tp64[sl * 256 + (int)((yy >> (8 * sl)) & 255ull)]);
+                        w = rot4d(w, m & 3u);
+                        sx += w.x;
+                        sy += w.y;
+                        if (i == steps) break;
+                        const int j = ctz32(i);
+                        m += (((ss >> j) & 1ull) ? Lm[j] : Lp[j]) + 2u * (uint32_t)(popc64(G[j] & ss) & 1);
+                        ss ^= 1ull << j;
+                        yy ^= R[j];
+                    }
+                    vx = sx;
+                    vy = sy;
+                } else {
+                    // FP32, chunks of fewer than 8 steps: per-branch folded index over the
+                    // sign-folded table, plain sums
+                    m -= 2u * quad_parity(G, s & lomask);
+                    float hx = 0.f, hy = 0.f, lx = 0.f, ly = 0.f;
+                    const float4 *__restrict__ W = E.wtab;
+                    const int DI = E.DI;
+                    for (uint32_t i = 1;; ++i) {
+                        if (MODE == 2)
+                            a.dbg[ss] = (uint8_t)((J.k0 + 2u * (m + 2u * quad_parity(G, ss & lomask))) & 7u);
+                        const float4 w = rot4q(__ldg(&W[(yy << DI) | (ss & lomask)]), m & 3u);
+                        hx += w.x;
+                        hy += w.y;
+                        lx += w.z;
+                        ly += w.w;
+                        if (i == steps) break;
+                        const int j = ctz32(i);
+                        m += (((ss >> j) & 1ull) ? Lm[j] : Lp[j]) + 2u * (uint32_t)(popc64(G[j] & ss & himask) & 1);
+                        ss ^= 1ull << j;
+                        yy ^= R[j];
+                    }
+                    vx = (double)hx + (double)lx;
+                    vy = (double)hy + (double)ly;
+                }
+                const double2 chi = chunk_high_weight(E, s);
+                accx += vx * chi.x - vy * chi.y;
+                accy += vx * chi.y + vy * chi.x;
+            }
+        }
+    }
+    for (int o = 16; o; o >>= 1) {
+        accx += __shfl_xor_sync(PQ_FULL, accx, o);
+        accy += __shfl_xor_sync(PQ_FULL, accy, o);
+    }
+    return make_double2(accx, accy);
+}
+
 // MODE 0: FP32 weights (exact-grid hi + lo) in the rotating-frame walk.  MODE 1: FP64 weights
 // and accumulation.  In both, jobs with chunk-sum tables take their chunk sums from them when
 // the launch asks for tables (use_ctab).
@@ -501,186 +700,12 @@ __global__ void __launch_bounds__(256, MINB) enum_kernel(KArgs a) {
             cur_k = lo;
             kbeg = a.istart[lo];
             kend = a.istart[lo + 1];
-            const int jb = a.perm[lo];
-            const JobDev &J = a.jobs[jb];
-            const EngineDev &E = a.engines[J.engine];
-            __syncwarp();
-            const int dlj = a.jdl[jb] & 255;
-            for (int j = lane; j < E.d; j += 32) {
-                G[j] = E.G[j];
-                R[j] = E.R[j];
-                Lp[j] = J.Lp[j];
-                Lm[j] = (uint8_t)((4u - J.Lp[j]) & 3u);
-                if (j < dlj) Tg[j] = ((1u << j) | ((uint32_t)E.R[j] << E.DI)) << 4;
-            }
-            __syncwarp();
+            stage_job(a, a.perm[lo], G, R, Lp, Lm, Tg, lane);
         }
         const int job = a.perm[cur_k];
-        const JobDev &J = a.jobs[job];
-        const EngineDev &E = a.engines[J.engine];
-        const long long iin = it - kbeg;
-        double accx = 0.0, accy = 0.0;
-        if (!J.vanish) {
-            const int dl = a.jdl[job] & 255;
-            const int np = (a.jdl[job] >> 8) & 3;  // pair coordinates used by this job's units
-            const int nk = 1 << np;
-            const unsigned cpi = a.jcpi[job];
-            const unsigned long long nun = a.jnch[job];
-            const unsigned long long c0 = (unsigned long long)iin * cpi;
-            unsigned long long cend = c0 + cpi;
-            if (cend > nun) cend = nun;
-            const uint64_t lomask = (E.DI >= 64) ? ~0ull : ((1ull << E.DI) - 1ull);
-            const uint32_t steps = 1u << dl;
-            if (MODE != 2 && a.use_ctab && E.ctab && dl == E.DI && np == 0 && (cpi & (cpi - 1)) == 0) {
-                // Chunk-sum tables: lane l sums the item's chunks base .. base + q - 1 (base =
-                // c0 + l q, q = cpi / 32 a power of two) in Gray order, one FP64 table lookup per
-                // chunk.  A step flips one high coordinate j: the folded index gains
-                // +-Lp_j + 2 parity(G_j & s), the pivot bits R_j, the low-coordinate signs b the
-                // row G_j; chunks past the item's end are walked but not added.
-                const unsigned long long q = (unsigned long long)(cpi >> 5) ? (unsigned long long)(cpi >> 5) : 1ull;
-                const unsigned long long base = c0 + (unsigned long long)lane * q;
-                if (base < cend) {
-                    uint64_t s = (uint64_t)base << dl;
-                    uint32_t m;
-                    uint64_t yy;
-                    chunk_start(Lp, G, R, J.y0, s, m, yy);
-                    uint32_t b = 0;
-                    for (int j = 0; j < dl; j++)
-                        b |= (((uint32_t)(Lp[j] >> 1) ^ (uint32_t)popc64(G[j] & s)) & 1u) << j;
-                    const uint32_t lm32 = (uint32_t)lomask;
-                    // the run varies the coordinates dl .. dl + log2(q) - 1; when they all lie in
-                    // the first byte slice of the high weight, the other slices are one factor
-                    const bool one_slice = (dl + ctz64(q)) <= E.DI + 8;
-                    double rx = 0.0, ry = 0.0;
-                    for (unsigned long long i = 0;; ++i) {
-                        const unsigned long long ch = base + (i ^ (i >> 1));
-                        if (ch < cend) {
-                            const double2 v = rot4d(E.ctab[(yy << E.DI) | b], m & 3u);
-                            const double2 chi = one_slice ? (E.nsl_th > 0 ? E.th[(int)((s >> E.DI) & 255ull)]
-                                                                          : make_double2(1.0, 0.0))
-                                                          : chunk_high_weight(E, s);
-                            rx += v.x * chi.x - v.y * chi.y;
-                            ry += v.x * chi.y + v.y * chi.x;
-                        }
-                        if (i + 1 == q) break;
-                        const int j = dl + ctz64(i + 1);
-                        m += (((s >> j) & 1ull) ? Lm[j] : Lp[j]) + 2u * (uint32_t)(popc64(G[j] & s) & 1);
-                        yy ^= R[j];
-                        b ^= (uint32_t)G[j] & lm32;
-                        s ^= 1ull << j;
-                    }
-                    double2 rest = make_double2(1.0, 0.0);
-                    if (one_slice)
-                        for (int sl = 1; sl < E.nsl_th; sl++)
-                            rest = cmul_d(rest, E.th[sl * 256 + (int)((s >> (E.DI + 8 * sl)) & 255ull)]);
-                    accx += rx * rest.x - ry * rest.y;
-                    accy += rx * rest.y + ry * rest.x;
-                }
-            } else
-            for (unsigned long long un = c0 + lane; un < cend; un += 32) {
-                // unit -> its first chunk (zeros inserted at the pair coordinates' chunk bits)
-                unsigned long long ch = un;
-                for (int i = 0; i < np; i++) ch = insert_zero(ch, E.pairc[i] - dl);
-                const uint64_t s1 = (uint64_t)ch << dl;
-                if (MODE != 2 && a.use_ctab && E.ctab && dl == E.DI) {
-                    // chunk-sum tables on a plan laid out for the walk (units of several
-                    // chunks): each chunk from its own start
-                    for (int kc = 0; kc < nk; kc++) {
-                        uint64_t s = s1;
-                        for (int i = 0; i < np; i++)
-                            if ((kc >> i) & 1) s |= 1ull << E.pairc[i];
-                        uint32_t m;
-                        uint64_t yy;
-                        chunk_start(Lp, G, R, J.y0, s, m, yy);
-                        uint32_t b = 0;
-                        for (int j = 0; j < dl; j++)
-                            b |= (((uint32_t)(Lp[j] >> 1) ^ (uint32_t)popc64(G[j] & s)) & 1u) << j;
-                        const double2 v = rot4d(E.ctab[(yy << E.DI) | b], m & 3u);
-                        const double2 chi = chunk_high_weight(E, s);
-                        accx += v.x * chi.x - v.y * chi.y;
-                        accy += v.x * chi.y + v.y * chi.x;
-                    }
-                    continue;
-                }
-                if (MODE != 1 && E.joint && dl >= 3) {
-                    if (np == 3) {
-                        if (MINB == 2) {  // eight accumulators per lane: only with the 128-register budget
-                            walk_unit<MODE, (MINB == 2 ? 8 : 4)>(E, J, G, R, Lp, Tg, dl, s1, lomask, a.dbg, accx, accy);
-                        } else {
-                            walk_unit<MODE, 4>(E, J, G, R, Lp, Tg, dl, s1, lomask, a.dbg, accx, accy);
-                            walk_unit<MODE, 4>(E, J, G, R, Lp, Tg, dl, s1 | (1ull << E.pairc[2]), lomask, a.dbg, accx,
-                                               accy);
-                        }
-                    } else if (np == 2) walk_unit<MODE, 4>(E, J, G, R, Lp, Tg, dl, s1, lomask, a.dbg, accx, accy);
-                    else if (np == 1) walk_unit<MODE, 2>(E, J, G, R, Lp, Tg, dl, s1, lomask, a.dbg, accx, accy);
-                    else walk_unit<MODE, 1>(E, J, G, R, Lp, Tg, dl, s1, lomask, a.dbg, accx, accy);
-                    continue;
-                }
-                const uint64_t himask = ~lomask;
-                for (int kc = 0; kc < nk; kc++) {
-                    uint64_t s = s1;
-                    for (int i = 0; i < np; i++)
-                        if ((kc >> i) & 1) s |= 1ull << E.pairc[i];
-                    uint32_t m;
-                    uint64_t yy;
-                    chunk_start(Lp, G, R, J.y0, s, m, yy);
-                    uint64_t ss = s;
-                    double vx, vy;  // the chunk's sum before the weight of the coordinates >= DI
-                    if (MODE == 1 || !E.joint) {
-                        // FP64 weights and accumulation (verification mode, and engines with more
-                        // pivots than the joint table holds)
-                        double sx = 0.0, sy = 0.0;
-                        for (uint32_t i = 1;; ++i) {
-                            if (MODE == 2) a.dbg[ss] = (uint8_t)((J.k0 + 2u * m) & 7u);
-                            double2 w = E.tlo64[ss & lomask];
-                            for (int sl = 0; sl < E.nsl_tp; sl++)
-                                w = cmul_d(w, E.tp64[sl * 256 + (int)((yy >> (8 * sl)) & 255ull)]);
-                            w = rot4d(w, m & 3u);
-                            sx += w.x;
-                            sy += w.y;
-                            if (i == steps) break;
-                            const int j = ctz32(i);
-                            m += (((ss >> j) & 1ull) ? Lm[j] : Lp[j]) + 2u * (uint32_t)(popc64(G[j] & ss) & 1);
-                            ss ^= 1ull << j;
-                            yy ^= R[j];
-                        }
-                        vx = sx;
-                        vy = sy;
-                    } else {
-                        // FP32, chunks of fewer than 8 steps: per-branch folded index over the
-                        // sign-folded table, plain sums
-                        m -= 2u * quad_parity(G, s & lomask);
-                        float hx = 0.f, hy = 0.f, lx = 0.f, ly = 0.f;
-                        const float4 *__restrict__ W = E.wtab;
-                        const int DI = E.DI;
-                        for (uint32_t i = 1;; ++i) {
-                            if (MODE == 2)
-                                a.dbg[ss] = (uint8_t)((J.k0 + 2u * (m + 2u * quad_parity(G, ss & lomask))) & 7u);
-                            const float4 w = rot4q(__ldg(&W[(yy << DI) | (ss & lomask)]), m & 3u);
-                            hx += w.x;
-                            hy += w.y;
-                            lx += w.z;
-                            ly += w.w;
-                            if (i == steps) break;
-                            const int j = ctz32(i);
-                            m += (((ss >> j) & 1ull) ? Lm[j] : Lp[j]) + 2u * (uint32_t)(popc64(G[j] & ss & himask) & 1);
-                            ss ^= 1ull << j;
-                            yy ^= R[j];
-                        }
-                        vx = (double)hx + (double)lx;
-                        vy = (double)hy + (double)ly;
-                    }
-                    const double2 chi = chunk_high_weight(E, s);
-                    accx += vx * chi.x - vy * chi.y;
-                    accy += vx * chi.y + vy * chi.x;
-                }
-            }
-        }
-        for (int o = 16; o; o >>= 1) {
-            accx += __shfl_xor_sync(PQ_FULL, accx, o);
-            accy += __shfl_xor_sync(PQ_FULL, accy, o);
-        }
-        if (lane == 0) a.partials[it] = make_double2(accx, accy);
+        const double2 p = item_partial<MODE, MINB>(a, job, it - kbeg + (a.ioff ? a.ioff[job] : 0), G, R, Lp, Lm,
+                                                   Tg, lane);
+        if (lane == 0) a.partials[it] = p;
     }
 }
 
@@ -695,20 +720,14 @@ __device__ __forceinline__ double2 phase_to_complex_dev(uint32_t p) {
     return make_double2(c, s);
 }
 
-__global__ void job_reduce_kernel(KArgs a) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= a.njobs) return;
+// Value and error bound of job j from the sum (sx, sy) of its item partials in item order.
+__device__ __forceinline__ void job_finish(const KArgs &a, int j, double sx, double sy, double2 &v, double &eb) {
     const JobDev &J = a.jobs[j];
     const EngineDev &E = a.engines[J.engine];
-    double2 v = make_double2(0.0, 0.0);
-    double eb = 0.0;
+    v = make_double2(0.0, 0.0);
+    eb = 0.0;
     if (!J.vanish) {
         const int k = a.kinv[j];
-        double sx = 0.0, sy = 0.0;
-        for (long long i = a.istart[k]; i < a.istart[k + 1]; i++) {
-            sx += a.partials[i].x;
-            sy += a.partials[i].y;
-        }
         const double2 r8 = make_double2(c_root8[2 * (J.k0 & 7u)], c_root8[2 * (J.k0 & 7u) + 1]);
         v = cmul_d(cmul_d(make_double2(sx, sy), r8), phase_to_complex_dev(J.phase));
         const double mag = pow2_half(E.mag2 - E.num_h);
@@ -752,18 +771,35 @@ __global__ void job_reduce_kernel(KArgs a) {
         // of the sums' own bound)
         if (E.joint && !ctab && !a.fp64_mode) eb += E.errfac * (1.0 + 4.0 / n) * mag;
     }
+}
+
+__global__ void job_reduce_kernel(KArgs a) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= a.njobs) return;
+    double sx = 0.0, sy = 0.0;
+    if (!a.jobs[j].vanish) {
+        const int k = a.kinv[j];
+        for (long long i = a.istart[k]; i < a.istart[k + 1]; i++) {
+            sx += a.partials[i].x;
+            sy += a.partials[i].y;
+        }
+    }
+    double2 v;
+    double eb;
+    job_finish(a, j, sx, sy, v, eb);
     a.job_vals[j] = v;
     a.job_err[j] = eb;
 }
 
-__global__ void out_reduce_kernel(KArgs a) {
-    const int o = blockIdx.x * blockDim.x + threadIdx.x;
-    if (o >= a.nout) return;
+// Output o from its jobs' values and bounds (vals[i], errs[i] of job out_jobs[o] + i), summed
+// in job order.
+__device__ __forceinline__ void out_finish(const KArgs &a, int o, const double2 *vals, const double *errs) {
     double sx = 0.0, sy = 0.0, eb = 0.0;
-    for (int j = a.out_jobs[o]; j < a.out_jobs[o + 1]; j++) {
-        sx += a.job_vals[j].x;
-        sy += a.job_vals[j].y;
-        eb += a.job_err[j];
+    const int nj = a.out_jobs[o + 1] - a.out_jobs[o];
+    for (int i = 0; i < nj; i++) {
+        sx += vals[i].x;
+        sy += vals[i].y;
+        eb += errs[i];
     }
     // a failed device self-check (prepare saw an odd Z8 increment, which the closed form rules
     // out) makes every result of the launch NaN, so callers that do not wait on the host still
@@ -778,6 +814,71 @@ __global__ void out_reduce_kernel(KArgs a) {
         a.out[2 * o] = sx;
         a.out[2 * o + 1] = sy;
         if (a.err) a.err[o] = eb;
+    }
+}
+
+__global__ void out_reduce_kernel(KArgs a) {
+    const int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= a.nout) return;
+    out_finish(a, o, a.job_vals + a.out_jobs[o], a.job_err + a.out_jobs[o]);
+}
+
+// ------------------------------------------------------------------------------ fused small launch
+// The whole evaluation of a small launch (every output's branch engines of at most
+// kSmallMaxJobs jobs and few work items) in one kernel: a block per output, its warps take the
+// output's jobs in turn -- prepare, then the job's work items one after another with the
+// enumeration's own per-item code, summed in item order as job_reduce sums them -- and the
+// block sums the job values in job order as out_reduce does.  The arithmetic and its order are
+// those of the four-kernel sequence, so the results are the same numbers.  The output's
+// boundary is copied into shared memory first (it may live in mapped host memory).
+static const int kSmallMaxJobs = 64;
+
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) small_kernel(KArgs a) {
+    __shared__ uint64_t sG[8][64];
+    __shared__ uint64_t sR[8][64];
+    __shared__ uint8_t sLp[8][64];
+    __shared__ uint8_t sLm[8][64];
+    __shared__ uint32_t sTg[8][32];
+    __shared__ double2 sval[kSmallMaxJobs];
+    __shared__ double serr[kSmallMaxJobs];
+    extern __shared__ uint64_t fsm[];  // 2 nw words of boundary, then smem_words per warp
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    uint64_t *bx = fsm, *by = fsm + a.nw;
+    uint64_t *u = fsm + 2 * a.nw + (size_t)wib * a.smem_words;
+    for (int o = blockIdx.x; o < a.nout; o += gridDim.x) {
+        const int j0 = a.out_jobs[o], nj = a.out_jobs[o + 1] - j0;
+        __syncthreads();  // the previous output's values are consumed
+        for (int w = threadIdx.x; w < a.nw; w += blockDim.x) {
+            bx[w] = a.xs[(size_t)o * a.nw + w];
+            by[w] = a.ys[(size_t)o * a.nw + w];
+        }
+        __syncthreads();
+        for (int i = wib; i < nj; i += wpb) {
+            const int j = j0 + i;
+            prepare_job(a, j, bx, by, u, lane);
+            double sx = 0.0, sy = 0.0;
+            if (!a.jobs[j].vanish) {
+                stage_job(a, j, sG[wib], sR[wib], sLp[wib], sLm[wib], sTg[wib], lane);
+                const int k = a.kinv[j];
+                const long long nit = a.istart[k + 1] - a.istart[k], i0 = a.ioff ? a.ioff[j] : 0;
+                for (long long iin = 0; iin < nit; iin++) {
+                    const double2 p = item_partial<0, MINB>(a, j, i0 + iin, sG[wib], sR[wib], sLp[wib], sLm[wib],
+                                                            sTg[wib], lane);
+                    sx += __shfl_sync(PQ_FULL, p.x, 0);
+                    sy += __shfl_sync(PQ_FULL, p.y, 0);
+                }
+            }
+            if (lane == 0) {
+                double2 v;
+                double eb;
+                job_finish(a, j, sx, sy, v, eb);
+                sval[i] = v;
+                serr[i] = eb;
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) out_finish(a, o, sval, serr);
     }
 }
 

@@ -52,7 +52,7 @@ class Request(ct.Structure):
 class Result(ct.Structure):
     _fields_ = [("tag", ct.c_int64), ("status", ct.c_int32), ("kind", ct.c_int32), ("re", ct.c_double),
                 ("im", ct.c_double), ("errbound", ct.c_double), ("submit_s", ct.c_double), ("done_s", ct.c_double),
-                ("level", ct.c_int32), ("reserved", ct.c_int32)]
+                ("level", ct.c_int32), ("pieces", ct.c_int32)]
 
 
 # name -> (restype, argtypes)
@@ -88,6 +88,7 @@ SIGNATURES = {
     "pq_batch_branches": (ct.c_int64, [P]),
     "pq_server_create": (ct.c_int, [ct.c_int32, ct.POINTER(P), ct.c_int32, ct.c_int64, ct.c_int32, ct.POINTER(P)]),
     "pq_server_destroy": (None, [P]),
+    "pq_server_set_pieces": (ct.c_int, [P, ct.c_int32, ct.c_int32]),
     "pq_server_submit": (ct.c_int, [P, ct.c_int64, ct.POINTER(Request)]),
     "pq_server_poll": (ct.c_int64, [P, ct.POINTER(Result), ct.c_int64, ct.c_double]),
     "pq_server_now": (ct.c_double, [P]),

@@ -21,6 +21,11 @@ class Server:
         self._h = h
         self.max_slots = max_slots
 
+    def set_pieces(self, split_log2=28, piece_log2=32):
+        """Requests above 2^split_log2 branches run in the background in pieces of at most
+        2^piece_log2 branches (pq_server_set_pieces)."""
+        N.check(self._L.pq_server_set_pieces(self._h, int(split_log2), int(piece_log2)))
+
     def now(self) -> float:
         return float(self._L.pq_server_now(self._h))
 
@@ -48,7 +53,8 @@ class Server:
         for i in range(k):
             r = buf[i]
             out.append({"tag": r.tag, "status": r.status, "kind": r.kind, "re": r.re, "im": r.im,
-                        "errbound": r.errbound, "submit_s": r.submit_s, "done_s": r.done_s, "level": r.level})
+                        "errbound": r.errbound, "submit_s": r.submit_s, "done_s": r.done_s, "level": r.level,
+                        "pieces": r.pieces})
         return out
 
     def drain(self, timeout_s=60.0):

@@ -182,3 +182,52 @@ def test_served_probabilities_within_1e12_absolute(gpu):
     assert all(res[1000 + y]["level"] == 0 for y in range(0, 256, 8))  # amplitudes never do
     amps = s.amplitudes([0] * 32, list(range(0, 256, 8)))
     assert np.array_equal(np.array([complex(res[1000 + y]["re"], res[1000 + y]["im"]) for y in range(0, 256, 8)]), amps)
+
+
+def test_requests_above_the_piece_size_are_split_not_refused(gpu):
+    # the cached engine of the many-boundaries circuit has 2^29 branches per amplitude; with the
+    # split threshold and piece size at 2^26 the server evaluates it over work-item ranges in
+    # eight background waves and sums the pieces; the result agrees with the direct (one launch)
+    # evaluation within the two error bounds, and the probability is certified to 1e-12
+    from polyq_gb300.rng import workload_many_boundaries
+    c = workload_many_boundaries(0)
+    sim = Simulator(c, "cached")
+    assert sim.stats_full()["branches_per_amplitude"] > 2 ** 26
+    ys = random_outputs(50, 3, 17)
+    srv = Server([sim], max_slots=8, mem_budget_bytes=1 << 28, max_branch_dim=40)
+    srv.set_pieces(26, 26)
+    srv.submit([{"sim": 0, "kind": AMPLITUDE, "x": 0, "y": y, "tag": i} for i, y in enumerate(ys)] +
+               [{"sim": 0, "kind": PROBABILITY, "x": 0, "y": ys[0], "tag": 10}])
+    res = {r["tag"]: r for r in srv.collect(4, 300)}
+    srv.close()
+    assert len(res) == 4 and all(r["status"] == 0 for r in res.values())
+    direct, derr = sim.amplitudes([0] * 3, ys, with_error=True)
+    ref = sim.amplitudes_fp64([0] * 3, ys)
+    for i in range(3):
+        got = complex(res[i]["re"], res[i]["im"])
+        assert abs(got - direct[i]) <= res[i]["errbound"] + derr[i]
+        assert abs(got - ref[i]) <= res[i]["errbound"] + 1e-13 * abs(ref[i])
+        assert abs(got - ref[i]) <= 1e-6 * abs(ref[i])
+    assert abs(res[10]["re"] - abs(ref[0]) ** 2) <= 1e-12
+
+
+def test_marginal_engine_builds_do_not_hold_up_other_requests(pool):
+    # the first marginal on a qubit builds that qubit's sandwich engines on the server's builder
+    # thread; amplitude requests submitted with it are served meanwhile
+    circs, sims = pool
+    k = int(np.argmax([c.num_qubits for c in circs]))
+    fresh = Simulator(circs[k])  # no marginal engines built yet
+    srv = Server([fresh], max_slots=16, mem_budget_bytes=1 << 28, max_branch_dim=40)
+    n = circs[k].num_qubits
+    reqs = [{"sim": 0, "kind": MARGINAL, "x": 0, "qubit": q, "outcome": 0, "tag": 1000 + q} for q in range(n)]
+    reqs += [{"sim": 0, "kind": AMPLITUDE, "x": 0, "y": y, "tag": i}
+             for i, y in enumerate(random_outputs(n, 64, 5))]
+    srv.submit(reqs)
+    res = {r["tag"]: r for r in srv.collect(len(reqs), 300)}
+    srv.close()
+    assert len(res) == len(reqs) and all(r["status"] == 0 for r in res.values())
+    last_amp = max(res[i]["done_s"] for i in range(64))
+    last_marg = max(res[1000 + q]["done_s"] for q in range(n))
+    assert last_amp < last_marg  # the amplitudes did not wait for the n marginal builds
+    for q in range(n):
+        assert abs(res[1000 + q]["re"] - fresh.marginal(0, [(q, 0)])) <= 1e-12
