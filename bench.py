@@ -602,6 +602,14 @@ def run_batched(args):
     return 0
 
 
+def _rate(res):
+    """Completed results over the span from the first submission to the last completion."""
+    if not res:
+        return None
+    span = max(r["done_s"] for r in res) - min(r["submit_s"] for r in res)
+    return len(res) / span if span > 0 else None
+
+
 def leg_serve(args, clk=None):
     """Poisson stream of amplitude / probability / single-qubit-marginal requests against 64
     resident circuits (n~U[16,64], 40n gates, T~U[8,40]); throughput and p50/p99 latency at the
@@ -653,7 +661,8 @@ def leg_serve(args, clk=None):
         w1 = time.perf_counter()
         ok = [r for r in res if r["status"] == 0]
         lat = [r["done_s"] - r["submit_s"] for r in ok]
-        lat_fg = [r["done_s"] - r["submit_s"] for r in ok if r["pieces"] == 0]
+        fg = [r for r in ok if r["pieces"] == 0]
+        lat_fg = [r["done_s"] - r["submit_s"] for r in fg]
         lat_bg = [r["done_s"] - r["submit_s"] for r in ok if r["pieces"] > 0]
         span = (max(r["done_s"] for r in ok) - min(r["submit_s"] for r in ok)) if ok else 0.0
         okt = set(r["tag"] for r in ok if r["pieces"] == 0)  # the plain comparison takes one-wave requests
@@ -665,7 +674,7 @@ def leg_serve(args, clk=None):
                                       for lv, name in enumerate(("fp32_walk", "chunk_tables", "fp64_walk"))},
                "p50_ms": 1e3 * _pct(lat, 0.5) if lat else None,
                "p99_ms": 1e3 * _pct(lat, 0.99) if lat else None,
-               "one_wave": {"completed": len(lat_fg), "p50_ms": 1e3 * _pct(lat_fg, 0.5) if lat_fg else None,
+               "one_wave": {"completed": len(lat_fg), "throughput_per_s": _rate(fg), "p50_ms": 1e3 * _pct(lat_fg, 0.5) if lat_fg else None,
                             "p99_ms": 1e3 * _pct(lat_fg, 0.99) if lat_fg else None},
                "background_pieces": {"completed": len(lat_bg),
                                      "pieces": sum(r["pieces"] for r in ok if r["pieces"] > 0),
@@ -676,7 +685,8 @@ def leg_serve(args, clk=None):
         return out, [q for q in reqs if q["tag"] in okt]
 
     full, served = load(args.rate, args.duration)
-    cap = full["throughput_per_s"] or args.rate
+    # below saturation: half the rate the one-wave requests were served at
+    cap = full["one_wave"]["throughput_per_s"] or full["throughput_per_s"] or args.rate
     sub, _ = load(0.5 * min(cap, args.rate), args.duration)
     # capacity: four times the offered rate for a quarter of the time (the served rate there is
     # what the server sustains when arrivals outrun it)
@@ -951,7 +961,7 @@ def main():
     ap.add_argument("--rate", type=float, default=5000.0, help="serve: offered requests/s")
     ap.add_argument("--duration", type=float, default=2.0, help="serve: seconds of arrivals")
     ap.add_argument("--slots", type=int, default=256, help="serve: requests per wave")
-    ap.add_argument("--max-d", type=int, default=28, help="serve: log2 cap on a request's branches (refused above)")
+    ap.add_argument("--max-d", type=int, default=36, help="serve: log2 cap on a request's branches (refused above)")
     ap.add_argument("--batch-steps", type=int, default=20, help="batched: timed launches")
     ap.add_argument("--batch-only", action="store_true", help="batched: the batched launch alone (profiling)")
     ap.add_argument("--headline-only", action="store_true",

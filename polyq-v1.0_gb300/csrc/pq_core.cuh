@@ -48,7 +48,9 @@ struct EngineDev {
     int zero;
     int DI, nsl_tp, nsl_th;
     int joint;               // 1: weights from the joint hi/lo table; 0: FP64 product path
-    uint8_t cperm[16];       // reference coordinate of device coordinate j < DI (identity above)
+    int plo;                 // pivots indexed by the joint table (all of them, or those the
+    uint64_t pmask;          // walked coordinates touch: bits pmask of the pivot bits y)
+    uint8_t cperm[64];       // reference coordinate of device coordinate j (j < min(d, 64))
     int npairc;              // pair coordinates: the lowest (<= 3) coordinates >= DI with R = 0
     int pairc[3];            // (flipping one keeps every table index): chunks that differ only
                              // in them are walked together
@@ -69,15 +71,20 @@ struct EngineDev {
     const uint64_t *Gw;      // d x dw  the same for any d (Monte-Carlo sampling above 64)
     int dw;
     const uint64_t *R;       // d   pivot masks
+    const uint64_t *Rc;      // d   pivot masks of the walked coordinates in the joint table's
+                             //     pivot index (R compressed to the bits of pmask)
     const float2 *tlo;       // 2^DI
     const float2 *tp;        // nsl_tp x 256
     const double2 *th;       // nsl_th x 256
+    const double2 *thp;      // nsl_tp x 256: weights of the pivots outside pmask (null: none), a
+                             // per-unit FP64 factor of an engine whose table covers only some pivots
     const double2 *thr;      // nsl_th x 256: th with the pair coordinates' factors left out
     const float4 *pf;        // 2^npairc: the pair coordinates' weight for each pattern of their
                              // bits, as FP32 pairs (re hi, im hi, re lo, im lo), hi + lo = FP64
     const double2 *tlo64;    // 2^DI   (FP64 path)
     const double2 *tp64;     // nsl_tp x 256
-    const float4 *wtab;      // 2^(DI + rank): (hi.re, hi.im, lo.re, lo.im) of tlo[s] * TP(y)
+    const float4 *wtab;      // 2^(DI + plo): (hi.re, hi.im, lo.re, lo.im) of tlo[s] * TP(y) over
+                             // the pivots in pmask
     const double2 *ctab;     // 2^(rank + DI) chunk sums (null: none), index (y << DI) | b
 };
 
@@ -281,12 +288,33 @@ PQ_HD unsigned long long insert_zero(unsigned long long x, int b) {
 }
 
 // A point of the branch subspace in the reference's coordinates, in the device's order (the
-// low DI coordinates are reordered when the engine is packed).
+// coordinates are reordered when the engine is packed; only within the first 64, which holds the
+// reordering of every engine).
 PQ_HD uint64_t to_device_order(const EngineDev &E, uint64_t s_ref) {
-    const uint64_t lomask = E.DI >= 64 ? ~0ull : ((1ull << E.DI) - 1ull);
-    uint64_t s = s_ref & ~lomask;
-    for (int j = 0; j < E.DI && j < 16; j++) s |= ((s_ref >> E.cperm[j]) & 1ull) << j;
+    const int n = E.d < 64 ? E.d : 64;
+    const uint64_t mask = n >= 64 ? ~0ull : ((1ull << n) - 1ull);
+    uint64_t s = s_ref & ~mask;
+    for (int j = 0; j < n; j++) s |= ((s_ref >> E.cperm[j]) & 1ull) << j;
     return s;
+}
+
+// The joint table's pivot index of pivot bits y: y itself, or its bits at pmask packed down.
+PQ_HD uint64_t joint_pivots(const EngineDev &E, uint64_t y) {
+    if (!E.thp) return y;
+    uint64_t r = 0;
+    int k = 0;
+    for (uint64_t m = E.pmask; m; m &= m - 1, k++) r |= ((y >> ctz64(m)) & 1ull) << k;
+    return r;
+}
+
+// FP64 weight of the pivots outside the joint table's index at pivot bits y ((1, 0) if none).
+PQ_HD double2 high_pivot_weight(const EngineDev &E, uint64_t y) {
+    double2 c;
+    c.x = 1.0;
+    c.y = 0.0;
+    if (!E.thp) return c;
+    for (int sl = 0; sl < E.nsl_tp; sl++) c = cmul_d(c, E.thp[sl * 256 + (int)((y >> (8 * sl)) & 255ull)]);
+    return c;
 }
 
 // Chunk start: Z4 index m and pivot bits y at kernel point s (bits in ascending order).

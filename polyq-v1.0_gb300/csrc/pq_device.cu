@@ -150,6 +150,10 @@ struct Target {
     const IoMapDev *map_rec = nullptr;
     int64_t bytes = 0;
     double branches_per_amp = 0.0;
+    // Lower bound of the error bound the FP32 walk reports for any boundary whose sum does not
+    // vanish, largest over the branch engines (the bound's boundary-independent terms): above
+    // 1e-12 it can never certify a marginal probability
+    double fp32_floor = 0.0;
     int max_d = 0, max_rank = 0, max_words = 0;
 };
 
@@ -168,10 +172,10 @@ static pq_status upload_target(Target &T, int di_max) {
                 try {
                     const auto &e = T.rs.branches[i];
                     std::vector<int> perm;
-                    const HostEngine pe = device_order(*e, build_tables(*e, di_max).DI, perm);
+                    const HostEngine pe = device_order(*e, di_max, perm);
                     EngineTables tb = build_tables(pe, di_max);
                     pks[i] = pack_engine(pe, tb);
-                    for (int j = 0; j < 16; j++) pks[i].off.cperm[j] = (uint8_t)(j < tb.DI ? perm[(size_t)j] : j);
+                    for (int j = 0; j < 64; j++) pks[i].off.cperm[j] = (uint8_t)(j < pe.d ? perm[(size_t)j] : j);
                 } catch (const std::exception &ex) {
                     errs[i] = ex.what();
                 }
@@ -225,6 +229,14 @@ static pq_status upload_target(Target &T, int di_max) {
         T.dev.push_back(dev);
         const auto &e = T.rs.branches[i];
         T.branches_per_amp += std::ldexp(1.0, e->d);
+        {
+            // the FP32 walk's bound has a 1e-12 relative term and the lo-sum term (joint
+            // tables); FP64 weights at least 2^DI rounding errors of 2^-53 per chunk sum
+            const double mag = pow2_half(dev.mag2 - dev.num_h);
+            const double fl = dev.joint ? (1e-12 * dev.sum_abs_bound + dev.errfac) * mag
+                                        : std::ldexp(1.0, dev.DI) * 2.220446049250313e-16 * dev.sum_abs_bound * mag;
+            T.fp32_floor = std::max(T.fp32_floor, fl);
+        }
         T.max_d = std::max(T.max_d, e->d);
         T.max_rank = std::max(T.max_rank, e->rank);
         T.max_words = std::max(T.max_words, e->L.full() + e->wf + 2);
@@ -283,6 +295,7 @@ struct Plan {
     bool any_ctab = false;   // some job can take its chunk sums from a chunk-sum table
     bool fp32_any = false;   // some job walks in FP32 (joint table) without tables
     bool fp32_rest = false;  // some job walks in FP32 even with tables (none for its engine)
+    double fp32_floor = 0.0;  // largest over the launch's targets of Target::fp32_floor
     uint64_t last_use = 0;  // recency in the owning simulator's plan cache
     bool graph_ready = false;
     cudaStream_t stream = nullptr;
@@ -359,6 +372,7 @@ static pq_status build_plan(const std::vector<Segment> &segs, int nw, cudaStream
         if (total > (double)(1 << 28))
             return fail(PQ_ERR_INVALID_ARG, "boundaries x branch engines above 2^28 in one launch; split the call");
     }
+    for (const auto &sg : segs) P.fp32_floor = std::max(P.fp32_floor, sg.tg->fp32_floor);
     std::vector<EngineDev> eng;
     std::vector<IoMapDev> maps;
     std::vector<JobDev> jobs;
@@ -643,7 +657,16 @@ static pq_status run_host(Plan &P, const uint64_t *x, const uint64_t *y, double 
     std::memcpy(P.hx.p, x, bw);
     std::memcpy(P.hy.p, y, bw);
     pq_status st;
-    if (P.fused) {
+    // a marginal whose FP32 walk cannot show 1e-12 on any boundary (the floor of its bound is
+    // above it) starts at the level that can
+    const bool ctab0 = P.args.use_ctab != 0;
+    const bool skip_fp32 = cert == CERT_REAL && P.fp32_floor > 1e-12 &&
+                           ((P.any_ctab && !ctab0) || (ctab0 ? P.fp32_rest : P.fp32_any));
+    if (skip_fp32) {
+        CU(cudaMemcpyAsync(P.x.p, P.hx.p, bw, cudaMemcpyHostToDevice, P.stream));
+        CU(cudaMemcpyAsync(P.y.p, P.hy.p, bw, cudaMemcpyHostToDevice, P.stream));
+        *P.herrflag.as<int>() = 0;
+    } else if (P.fused) {
         // one graph launch: the fused kernel reads and writes the mapped buffers
         st = launch_graph_host(P);
         if (st != PQ_OK) return st;
@@ -656,7 +679,7 @@ static pq_status run_host(Plan &P, const uint64_t *x, const uint64_t *y, double 
         CU(cudaMemcpyAsync(P.herr.p, P.err.p, (size_t)P.nout * 8, cudaMemcpyDeviceToHost, P.stream));
         CU(cudaMemcpyAsync(P.herrflag.p, P.errflag.p, sizeof(int), cudaMemcpyDeviceToHost, P.stream));
     }
-    CU(cudaStreamSynchronize(P.stream));
+    if (!skip_fp32) CU(cudaStreamSynchronize(P.stream));
     if (*P.herrflag.as<int>()) return fail(PQ_ERR_INTERNAL, "device self-check failed (odd Z8 increment)");
     const double *ho = P.hout.as<double>();
     const double *he = P.herr.as<double>();
@@ -672,7 +695,7 @@ static pq_status run_host(Plan &P, const uint64_t *x, const uint64_t *y, double 
             if (bound_of(o) > 1e-12) return true;
         return false;
     };
-    bool staged = !P.fused;  // boundaries in the plan's device buffers
+    bool staged = !P.fused || skip_fp32;  // boundaries in the plan's device buffers
     auto rerun = [&](int mode, int ctab) -> pq_status {
         if (!staged) {
             CU(cudaMemcpyAsync(P.x.p, P.hx.p, bw, cudaMemcpyHostToDevice, P.stream));
@@ -685,18 +708,25 @@ static pq_status run_host(Plan &P, const uint64_t *x, const uint64_t *y, double 
         CU(cudaStreamSynchronize(P.stream));
         return PQ_OK;
     };
-    if (cert != CERT_NONE && uncertified()) {
-        bool tables = P.args.use_ctab != 0;
+    if (cert != CERT_NONE && (skip_fp32 || uncertified())) {
+        bool tables = ctab0;
+        bool have = !skip_fp32;  // the host buffers hold an evaluation of these boundaries
         if (P.any_ctab && !tables) {
             st = rerun(0, 1);
             if (st != PQ_OK) return st;
             tables = true;
+            have = true;
         }
         // then the FP64 walk for the jobs that walked in FP32 (the tables stay where they
         // apply; jobs without a joint table already used FP64 weights, so a rerun would repeat
         // them)
-        if (uncertified() && (tables ? P.fp32_rest : P.fp32_any)) {
+        if ((!have || uncertified()) && (tables ? P.fp32_rest : P.fp32_any)) {
             st = rerun(1, tables ? 1 : 0);
+            if (st != PQ_OK) return st;
+            have = true;
+        }
+        if (!have) {
+            st = rerun(0, -1);
             if (st != PQ_OK) return st;
         }
     }
@@ -1899,7 +1929,8 @@ PQ_API int64_t pq_debug_engine_dump(const pq_sim *s, int32_t branch, uint64_t *o
 PQ_API pq_status pq_debug_engine_shape(const pq_sim *s, int32_t branch, int64_t *out) {
     if (!s || !out || branch < 0 || branch >= (int)s->main.rs.branches.size())
         return fail(PQ_ERR_INVALID_ARG, "bad simulator or branch");
-    const HostEngine &e = *s->main.rs.branches[branch];
+    std::vector<int> perm;
+    const HostEngine e = device_order(*s->main.rs.branches[branch], s->di_max, perm);
     EngineTables tb = build_tables(e, s->di_max);
     PackedEngine pk = pack_engine(e, tb);
     int64_t r0 = 0, r0hi = 0;
@@ -2003,7 +2034,7 @@ PQ_API pq_status pq_debug_prepare(pq_sim *s, int64_t n, const uint64_t *x, const
         rec[2] = J.k0;
         rec[3] = J.y0;
         for (int jd = 0; jd < E.d && jd < 64; jd++) {
-            const int jr = (jd < E.DI && jd < 16) ? E.cperm[jd] : jd;
+            const int jr = jd < 64 ? E.cperm[jd] : jd;
             rec[4 + (jr >> 3)] |= (uint64_t)J.Lp[jd] << (8 * (jr & 7));
         }
     }
@@ -2622,6 +2653,18 @@ static void srv_loop(pq_server *S) {
                 if (q.tg->branches_per_amp > std::ldexp(1.0, S->max_d)) {
                     refused.push_back(srv_result(q, PQ_ERR_ADMISSION_REFUSED, srv_now(S)));
                     continue;
+                }
+                if (q.r.kind == PQ_REQ_MARGINAL && q.precise == 0 && q.tg->fp32_floor > 1e-12) {
+                    // the FP32 walk cannot certify this marginal: start at the level that can
+                    bool any_ctab = false, fp32_any = false, fp32_rest = false;
+                    eval_cover(*q.tg, srv_tuning(tu, 1), any_ctab, fp32_any, fp32_rest);
+                    const int lv = any_ctab ? 1 : (fp32_any ? 2 : 0);
+                    if (lv != w->precise) {
+                        q.precise = lv;
+                        back.push_back(q);  // evaluated in a wave of its own level
+                        continue;
+                    }
+                    q.precise = lv;
                 }
                 if (q.tg->branches_per_amp > std::ldexp(1.0, S->split_log2)) {
                     split.push_back(q);

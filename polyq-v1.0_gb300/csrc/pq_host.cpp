@@ -763,6 +763,31 @@ EngineTables build_tables(const HostEngine& e, int di_max) {
     T.DI = std::min(d, di_max);
     T.joint = e.rank <= kJointMaxPivots;
     if (T.joint && T.DI + e.rank > kJointMaxBits) T.DI = std::max(0, kJointMaxBits - e.rank);
+    T.pmask = e.rank >= 64 ? ~0ull : ((1ull << e.rank) - 1ull);
+    T.plo = e.rank;
+    if (!T.joint && e.dev_DI >= 3) {
+        // more pivots than one table holds: the table covers the pivots the dev_DI low
+        // coordinates (chosen by device_order) touch; the others become a per-chunk factor
+        uint64_t pm = 0;
+        for (int j = 0; j < e.dev_DI; j++) pm |= e.R[(size_t)j];
+        if (e.dev_DI + __builtin_popcountll(pm) <= kJointMaxBits) {
+            T.DI = e.dev_DI;
+            T.joint = T.partial = true;
+            T.pmask = pm;
+            T.plo = __builtin_popcountll(pm);
+        }
+    }
+    T.Rc.resize((size_t)d);
+    for (int j = 0; j < d; j++) {
+        uint64_t r = e.R[(size_t)j];
+        if (T.partial && j < T.DI) {
+            uint64_t c = 0;
+            int k = 0;
+            for (uint64_t m = T.pmask; m; m &= m - 1, k++) c |= ((r >> __builtin_ctzll(m)) & 1ull) << k;
+            r = c;
+        }
+        T.Rc[(size_t)j] = r;
+    }
     auto xw = [&](int j, int bit) { int k = e.free_col[j]; return bit ? e.beta[k] : e.alpha[k]; };
     auto pw = [&](int i, int bit) { int k = e.piv_col[i]; return bit ? e.beta[k] : e.alpha[k]; };
     const size_t nlo = (size_t)1 << T.DI;
@@ -789,12 +814,26 @@ EngineTables build_tables(const HostEngine& e, int di_max) {
             T.th[(size_t)sl * 256 + b] = c;
         }
     if (T.joint) {
-        T.w.resize((size_t)1 << (T.DI + e.rank));
-        for (size_t y = 0; y < ((size_t)1 << e.rank); y++) {
+        // pivot of table index bit k: the k-th set bit of pmask
+        std::vector<int> piv;
+        for (int i = 0; i < e.rank; i++)
+            if ((T.pmask >> i) & 1ull) piv.push_back(i);
+        T.w.resize((size_t)1 << (T.DI + T.plo));
+        for (size_t y = 0; y < ((size_t)1 << T.plo); y++) {
             Cplx tpv{1.0, 0.0};
-            for (int i = 0; i < e.rank; i++) tpv = cmul(tpv, pw(i, (int)((y >> i) & 1)));
+            for (int k = 0; k < T.plo; k++) tpv = cmul(tpv, pw(piv[(size_t)k], (int)((y >> k) & 1)));
             for (size_t s = 0; s < nlo; s++) T.w[(y << T.DI) | s] = cmul(T.tlo[s], tpv);
         }
+    }
+    if (T.partial) {
+        T.thp.resize((size_t)T.nsl_tp * 256);
+        for (int sl = 0; sl < T.nsl_tp; sl++)
+            for (int b = 0; b < 256; b++) {
+                Cplx c{1.0, 0.0};
+                for (int k = 0; k < 8 && 8 * sl + k < e.rank; k++)
+                    if (!((T.pmask >> (8 * sl + k)) & 1ull)) c = cmul(c, pw(8 * sl + k, (b >> k) & 1));
+                T.thp[(size_t)sl * 256 + b] = c;
+            }
     }
     return T;
 }
@@ -827,6 +866,7 @@ PackedEngine pack_engine(const HostEngine& e, const EngineTables& T) {
     d.wg = L.wg; d.wo = L.wo; d.we = L.we; d.wf = e.wf; d.W = L.full(); d.abo = L.abo();
     d.sigma = e.sigma; d.mag2 = e.mag2; d.num_h = e.num_h; d.global = e.global; d.zero = e.zero ? 1 : 0;
     d.DI = T.DI; d.nsl_tp = T.nsl_tp; d.nsl_th = T.nsl_th;
+    d.plo = T.plo; d.pmask = T.pmask;
     d.sum_abs_bound = e.sum_abs_bound;
     d.o1 = as_off<uint64_t>(k.vec(e.dg.o1.w));
     d.o3 = as_off<uint64_t>(k.vec(e.dg.o3.w));
@@ -850,6 +890,8 @@ PackedEngine pack_engine(const HostEngine& e, const EngineTables& T) {
     d.Gw = as_off<uint64_t>(k.vec(e.Gw));
     d.dw = e.dw;
     d.R = as_off<uint64_t>(k.vec(e.R));
+    d.Rc = as_off<uint64_t>(k.vec(T.Rc));
+    d.thp = T.partial ? as_off<double2>(k.vec(T.thp)) : nullptr;
     std::vector<float> tlo32, tp32;
     for (const auto& c : T.tlo) { tlo32.push_back((float)c.re); tlo32.push_back((float)c.im); }
     for (const auto& c : T.tp) { tp32.push_back((float)c.re); tp32.push_back((float)c.im); }
@@ -912,6 +954,14 @@ PackedEngine pack_engine(const HostEngine& e, const EngineTables& T) {
             int kk = e.free_col[j];
             hi_abs *= std::hypot(e.alpha[kk].re, e.alpha[kk].im) + std::hypot(e.beta[kk].re, e.beta[kk].im);
         }
+        // the pivots outside the table scale each chunk by at most the product of their
+        // larger weights
+        if (T.partial)
+            for (int i = 0; i < e.rank; i++)
+                if (!((T.pmask >> i) & 1ull)) {
+                    const int kk = e.piv_col[(size_t)i];
+                    hi_abs *= std::max(std::hypot(e.alpha[kk].re, e.alpha[kk].im), std::hypot(e.beta[kk].re, e.beta[kk].im));
+                }
         d.errfac = 4.0 * n * (grid / 2.0) * (gam + u) * hi_abs;
     }
     // The table entry of low coordinates s carries the sign (-1)^{q(s)} of the quadratic phase
@@ -943,8 +993,10 @@ PackedEngine pack_engine(const HostEngine& e, const EngineTables& T) {
     //   T[u][b] = sum_s i^{<Lp0, s>} (-1)^{<b, s>} W'[u ^ R_lo s][s],
     // a Walsh-Hadamard transform over s for each pivot pattern u (FP64, once per engine).
     d.ctab = nullptr;
-    if (T.joint && T.DI >= 1 && T.DI + e.rank <= 16) {
-        const size_t nlo = (size_t)1 << T.DI, nu = (size_t)1 << e.rank;
+    // (A partial table's chunk sums index its pivots the same way, through the packed masks Rc;
+    // the other pivots' weight multiplies each chunk's sum on the device.)
+    if (T.joint && T.DI >= 1 && T.DI + T.plo <= 16) {
+        const size_t nlo = (size_t)1 << T.DI, nu = (size_t)1 << T.plo;
         std::vector<Cplx> ct(nu * nlo);
         for (size_t u = 0; u < nu; u++) {
             Cplx *g = &ct[u * nlo];
@@ -953,7 +1005,7 @@ PackedEngine pack_engine(const HostEngine& e, const EngineTables& T) {
                 int ph = 0;
                 for (int j = 0; j < T.DI; j++)
                     if ((s >> j) & 1) {
-                        y ^= e.R[(size_t)j];
+                        y ^= T.Rc[(size_t)j];
                         ph += e.lp0[(size_t)j];
                     }
                 Cplx w = T.w[(y << T.DI) | s];
@@ -979,18 +1031,64 @@ PackedEngine pack_engine(const HostEngine& e, const EngineTables& T) {
     return P;
 }
 
-HostEngine device_order(const HostEngine& e, int DI, std::vector<int>& perm) {
-    // Coordinates whose Z4 increment is even first (stable), then the odd ones, among the low
-    // DI coordinates: the walk's fixed-position steps are then even quarter turns (paired FMA)
-    // for almost every engine.  perm[j] = reference coordinate of device coordinate j.
+// Low (walked) coordinates of an engine with more pivots than one joint table holds: the
+// pivot-free coordinates first -- all but three, which stay high as the pair coordinates of the
+// walk's units -- then, one at a time, the coordinate that touches the fewest pivots not yet
+// touched, while DI + (pivots touched) stays within kJointMaxBits.  Returns them ascending.
+static std::vector<int> low_coordinates_many_pivots(const HostEngine& e, int di_max) {
+    std::vector<int> zero, other;
+    for (int j = 0; j < e.d; j++) (e.R[(size_t)j] == 0 ? zero : other).push_back(j);
+    const size_t keep = std::min<size_t>(3, zero.size());
+    std::vector<int> L(zero.begin(), zero.end() - (long)keep);
+    const int cap = std::min(di_max, kJointMaxBits);
+    if ((int)L.size() > cap) L.resize((size_t)cap);
+    std::vector<char> used((size_t)e.d, 0);
+    for (int j : L) used[(size_t)j] = 1;
+    uint64_t pm = 0;
+    while ((int)L.size() < cap) {
+        int best = -1, bestc = 65;
+        for (int j : other)
+            if (!used[(size_t)j]) {
+                const int c = __builtin_popcountll(e.R[(size_t)j] & ~pm);
+                if (c < bestc) { bestc = c; best = j; }
+            }
+        if (best < 0 || (int)L.size() + 1 + __builtin_popcountll(pm | e.R[(size_t)best]) > kJointMaxBits) break;
+        L.push_back(best);
+        used[(size_t)best] = 1;
+        pm |= e.R[(size_t)best];
+    }
+    std::sort(L.begin(), L.end());
+    return L;
+}
+
+HostEngine device_order(const HostEngine& e, int di_max, std::vector<int>& perm) {
+    // The low DI coordinates (the walked ones) are those of the joint table: the first DI in the
+    // reference order, or for an engine with more pivots than one table holds (and d <= 62)
+    // those low_coordinates_many_pivots picks, moved to the front.  Among them the coordinates
+    // whose Z4 increment is even come first (stable), then the odd ones: the walk's fixed-
+    // position steps are then even quarter turns (paired FMA) for almost every engine.  The
+    // other coordinates keep the reference order.  perm[j] = reference coordinate of device
+    // coordinate j.
     const int d = e.d;
+    std::vector<int> low;
+    if (e.rank > kJointMaxPivots && d <= 62) low = low_coordinates_many_pivots(e, di_max);
+    if (low.size() < 3) {
+        low.clear();
+        int DI = std::min(d, di_max);
+        if (e.rank <= kJointMaxPivots && DI + e.rank > kJointMaxBits) DI = std::max(0, kJointMaxBits - e.rank);
+        for (int j = 0; j < DI; j++) low.push_back(j);
+    }
+    const int DI = (int)low.size();
     perm.resize((size_t)d);
     int k = 0;
-    for (int j = 0; j < DI; j++)
+    for (int j : low)
         if (!e.lp0[(size_t)j]) perm[(size_t)k++] = j;
-    for (int j = 0; j < DI; j++)
+    for (int j : low)
         if (e.lp0[(size_t)j]) perm[(size_t)k++] = j;
-    for (int j = DI; j < d; j++) perm[(size_t)j] = j;
+    std::vector<char> in_low((size_t)d, 0);
+    for (int j : low) in_low[(size_t)j] = 1;
+    for (int j = 0; j < d; j++)
+        if (!in_low[(size_t)j]) perm[(size_t)k++] = j;
     HostEngine p = e;
     const int abo = e.L.abo();
     std::vector<int> inv((size_t)d);
@@ -1011,6 +1109,7 @@ HostEngine device_order(const HostEngine& e, int DI, std::vector<int>& perm) {
                 p.Gw[(size_t)a * p.dw + (size_t)(b >> 6)] |= 1ull << (b & 63);
             }
     for (int j = 0; j < d; j++) p.G[(size_t)j] = p.Gw[(size_t)j * p.dw];
+    p.dev_DI = DI;
     return p;
 }
 
@@ -1024,6 +1123,8 @@ EngineDev rebase_engine(const EngineDev& o, const uint8_t* base) {
     d.tlo = shift(o.tlo, base); d.tp = shift(o.tp, base); d.th = shift(o.th, base);
     d.thr = shift(o.thr, base); d.pf = shift(o.pf, base);
     d.tlo64 = shift(o.tlo64, base); d.tp64 = shift(o.tp64, base); d.wtab = nullptr;
+    d.Rc = shift(o.Rc, base);
+    d.thp = o.thp ? shift(o.thp, base) : nullptr;
     d.ctab = o.ctab ? shift(o.ctab, base) : nullptr;
     return d;
 }

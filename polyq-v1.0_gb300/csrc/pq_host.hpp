@@ -153,6 +153,7 @@ struct HostEngine {
     std::vector<uint64_t> R;        // d pivot masks (bit i: kernel_j hits pivot column i)
     std::vector<int> free_col;      // d: term index of kernel vector j's free column
     double sum_abs_bound = 0.0;     // upper bound of sum_s |c(s)| (for the per-result error bound)
+    int dev_DI = -1;                // walked (low) coordinates chosen by device_order (-1: not set)
 
     // Z8 index of the Gauss sum for coordinates u (src/normal_form.rs:479-493)
     int phase8(const uint64_t* u_abo) const;
@@ -184,10 +185,18 @@ std::unique_ptr<HostEngine> pattern_engine(const PathSum& ps, const std::vector<
 //                       (FP64 products; the device stores them as FP32 hi + lo pairs)
 static const int kJointMaxPivots = 10;
 static const int kJointMaxBits = 13;  // DI + #pivots of the joint table
+//   An engine with more than kJointMaxPivots pivots gets a joint table over only the pivots its
+//   DI low coordinates touch (pmask, plo of them; device_order picks low coordinates that touch
+//   few): w[(ylo << DI) | s] over those pivots, and thp[b] = the other pivots' weights per byte
+//   slice of y, a per-chunk FP64 factor (the walked coordinates do not change those pivots).
 struct EngineTables {
     int DI = 0, nsl_tp = 0, nsl_th = 0;
     bool joint = false;
-    std::vector<Cplx> tlo, tp, th, w;
+    bool partial = false;       // the joint table covers the pivots in pmask only
+    int plo = 0;
+    uint64_t pmask = 0;
+    std::vector<Cplx> tlo, tp, th, w, thp;
+    std::vector<uint64_t> Rc;   // d: R_j compressed to the bits of pmask (j < DI), else R_j
 };
 EngineTables build_tables(const HostEngine& e, int di_max);
 
@@ -202,9 +211,10 @@ struct PackedEngine {
     std::vector<float> wtab;    // the joint weight table (4 floats per entry), uploaded apart
 };
 PackedEngine pack_engine(const HostEngine& e, const EngineTables& t);
-// Copy of e with its low DI coordinates reordered for the device (see pq_host.cpp); perm[j] is
-// the reference coordinate of device coordinate j.
-HostEngine device_order(const HostEngine& e, int DI, std::vector<int>& perm);
+// Copy of e with its coordinates reordered for the device (see pq_host.cpp) and its low
+// (walked) coordinate count set in dev_DI; perm[j] is the reference coordinate of device
+// coordinate j.
+HostEngine device_order(const HostEngine& e, int di_max, std::vector<int>& perm);
 EngineDev rebase_engine(const EngineDev& off, const uint8_t* base);
 
 // Boundary map: `puts` lists (variable, boundary source) in the order the reference's

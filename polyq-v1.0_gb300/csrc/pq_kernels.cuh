@@ -397,7 +397,7 @@ __device__ __forceinline__ void walk_unit(const EngineDev &E, const JobDev &J, c
     m1 -= 2u * quad_parity(G, s1 & lomask);  // the table holds the low-coordinate quadratic part
     uint32_t P1 = 0;
     for (int j = 0; j < dl; j++) P1 |= (uint32_t)(popc64(G[j] & s1 & himask) & 1) << j;
-    const uint32_t sidx = (uint32_t)((yy << E.DI) | (s1 & lomask));
+    const uint32_t sidx = (uint32_t)((joint_pivots(E, yy) << E.DI) | (s1 & lomask));
     // chunk k = s1 + the pair coordinates of the bits of k: its index grows by their linear terms
     // at s1 plus 2 G between each two of them; its c_j by their G rows
     uint32_t dlin[3] = {0u, 0u, 0u}, grow[3] = {0u, 0u, 0u};
@@ -470,7 +470,9 @@ __device__ __forceinline__ void walk_unit(const EngineDev &E, const JobDev &J, c
         ff_cmul_acc(P, hx, hy, lx, ly, urh, url, uih, uil);
     }
     const double ux = (double)urh + (double)url, uy = (double)uih + (double)uil;
-    const double2 chi = chunk_rest_weight(E, s1);
+    // the unit's chunks share their pivots outside a partial table (the walked and the pair
+    // coordinates do not touch them): one FP64 factor with the other high coordinates' weight
+    const double2 chi = E.thp ? cmul_d(chunk_rest_weight(E, s1), high_pivot_weight(E, yy)) : chunk_rest_weight(E, s1);
     accx += ux * chi.x - uy * chi.y;
     accy += ux * chi.y + uy * chi.x;
 }
@@ -488,7 +490,7 @@ __device__ __forceinline__ void stage_job(const KArgs &a, int jb, uint64_t *G, u
         R[j] = E.R[j];
         Lp[j] = J.Lp[j];
         Lm[j] = (uint8_t)((4u - J.Lp[j]) & 3u);
-        if (j < dlj) Tg[j] = ((1u << j) | ((uint32_t)E.R[j] << E.DI)) << 4;
+        if (j < dlj) Tg[j] = ((1u << j) | ((uint32_t)E.Rc[j] << E.DI)) << 4;
     }
     __syncwarp();
 }
@@ -537,7 +539,8 @@ __device__ __forceinline__ double2 item_partial(const KArgs &a, int job, long lo
                 for (unsigned long long i = 0;; ++i) {
                     const unsigned long long ch = base + (i ^ (i >> 1));
                     if (ch < cend) {
-                        const double2 v = rot4d(E.ctab[(yy << E.DI) | b], m & 3u);
+                        double2 v = rot4d(E.ctab[(joint_pivots(E, yy) << E.DI) | b], m & 3u);
+                        if (E.thp) v = cmul_d(v, high_pivot_weight(E, yy));
                         const double2 chi = one_slice ? (E.nsl_th > 0 ? E.th[(int)((s >> E.DI) & 255ull)]
                                                                       : make_double2(1.0, 0.0))
                                                       : chunk_high_weight(E, s);
@@ -577,7 +580,8 @@ __device__ __forceinline__ double2 item_partial(const KArgs &a, int job, long lo
                     uint32_t b = 0;
                     for (int j = 0; j < dl; j++)
                         b |= (((uint32_t)(Lp[j] >> 1) ^ (uint32_t)popc64(G[j] & s)) & 1u) << j;
-                    const double2 v = rot4d(E.ctab[(yy << E.DI) | b], m & 3u);
+                    double2 v = rot4d(E.ctab[(joint_pivots(E, yy) << E.DI) | b], m & 3u);
+                    if (E.thp) v = cmul_d(v, high_pivot_weight(E, yy));
                     const double2 chi = chunk_high_weight(E, s);
                     accx += v.x * chi.x - v.y * chi.y;
                     accy += v.x * chi.y + v.y * chi.x;
@@ -608,6 +612,7 @@ __device__ __forceinline__ double2 item_partial(const KArgs &a, int job, long lo
                 chunk_start(Lp, G, R, J.y0, s, m, yy);
                 uint64_t ss = s;
                 double vx, vy;  // the chunk's sum before the weight of the coordinates >= DI
+                double2 tph = make_double2(1.0, 0.0);  // weight of pivots outside a partial table
                 if (MODE == 1 || !E.joint) {
                     // FP64 weights and accumulation (verification mode, and engines with more
                     // pivots than the joint table holds)
@@ -635,10 +640,13 @@ __device__ __forceinline__ double2 item_partial(const KArgs &a, int job, long lo
                     float hx = 0.f, hy = 0.f, lx = 0.f, ly = 0.f;
                     const float4 *__restrict__ W = E.wtab;
                     const int DI = E.DI;
+                    // pivots outside the table: constant over the chunk (its walked coordinates
+                    // touch only pivots in pmask)
+                    tph = high_pivot_weight(E, yy);
                     for (uint32_t i = 1;; ++i) {
                         if (MODE == 2)
                             a.dbg[ss] = (uint8_t)((J.k0 + 2u * (m + 2u * quad_parity(G, ss & lomask))) & 7u);
-                        const float4 w = rot4q(__ldg(&W[(yy << DI) | (ss & lomask)]), m & 3u);
+                        const float4 w = rot4q(__ldg(&W[(joint_pivots(E, yy) << DI) | (ss & lomask)]), m & 3u);
                         hx += w.x;
                         hy += w.y;
                         lx += w.z;
@@ -652,7 +660,7 @@ __device__ __forceinline__ double2 item_partial(const KArgs &a, int job, long lo
                     vx = (double)hx + (double)lx;
                     vy = (double)hy + (double)ly;
                 }
-                const double2 chi = chunk_high_weight(E, s);
+                const double2 chi = cmul_d(chunk_high_weight(E, s), tph);
                 accx += vx * chi.x - vy * chi.y;
                 accy += vx * chi.y + vy * chi.x;
             }
@@ -756,11 +764,14 @@ __device__ __forceinline__ void job_finish(const KArgs &a, int j, double sx, dou
             // high-coordinate factor (nsl_th products of 8-factor slice products) and its
             // product with the entry, the 5-level warp reduction, the final scalings
             rel = (2.0 * (double)E.DI + 16.0 + 10.0 * (double)E.nsl_th + 5.0 + 64.0) * 2.0 * u64;
+            if (E.thp) rel += (2.0 * E.nsl_tp + 2.0) * 2.0 * u64;  // the chunk's other-pivot factor
         } else if (E.joint && !a.fp64_mode) {
             // + 1e-12: the FP32-pair combination of a unit's chunks (at most 8 terms, each with
             // error a few 2^-48 of its magnitude)
             const double g = n * u32 / (1.0 - n * u32);
             rel = g * g + 2.0 * n * u32 * u32 + 1.5e-14 + 64.0 * u64 + 1e-12;
+            // a partial table's pivot factor: nsl_tp FP64 complex products per unit
+            if (E.thp) rel += (2.0 * E.nsl_tp + 2.0) * 2.0 * u64;
         } else {
             rel = (n + 2.0 * E.nsl_tp + 8.0 + (double)E.nsl_th) * 2.0 * u64;
         }

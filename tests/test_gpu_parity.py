@@ -424,3 +424,62 @@ def test_unit_sizes_agree_within_bounds(gpu):
             assert_amps(got, ref, err)
     finally:
         set_tuning(unit_chunks=old["unit_chunks"], blocks_per_sm=old["blocks_per_sm"])
+
+
+def _many_pivot_circuits():
+    # members C of the serving pool sandwiched as C, (H T on the first k qubits), C^dagger: their
+    # cached engines have 13..15 pivots, more than one joint weight table indexes; the table then
+    # covers the pivots the walked coordinates touch and the rest enter as a per-unit FP64 factor
+    circs = [c for c, _ in workload_batch(64, seed=5, t_max=40)]
+    out = []
+    for i, k in ((12, 2), (5, 2), (11, 1), (37, 1), (3, 1)):
+        cc = circs[i].copy()
+        for q in range(k):
+            cc.h(q)
+            cc.t(q)
+        out.append(cc.extend(circs[i].inverse()))
+    return out
+
+
+def test_many_pivot_engines_walk_in_fp32(gpu):
+    checked = 0
+    for cc in _many_pivot_circuits():
+        s, r = Simulator(cc), O.OracleSim(cc)
+        nb = s.stats_full()["num_branches"]
+        sv = O.dense_statevector(cc, 0)
+        ys = [int(i) for i in np.argsort(-np.abs(sv))[:48]] + random_outputs(cc.num_qubits, 16, 3)
+        xs = [0] * len(ys)
+        for b in range(nb):
+            shp = s.engine_shape(b)
+            assert shp["rank"] > 10 and shp["joint"] == 1, shp
+            for y in ys[:2]:
+                want = r.branch_phases(0, y, b)
+                got = s.branch_phases(0, y, b)
+                assert (want is None) == (got is None)
+                if want is not None:
+                    assert np.array_equal(got, want)
+                    checked += 1
+        assert np.array_equal(s.prepare_info(xs, ys), r.prepare_info(xs, ys))
+        got, err = s.amplitudes(xs, ys, with_error=True)
+        assert_amps(got, r.amplitudes(xs, ys), err)
+        assert_amps(got, sv[ys], err)
+        p = s.probabilities(xs, ys)
+        assert np.max(np.abs(p - np.abs(sv[ys]) ** 2)) <= PROB_ABS
+    assert checked >= 5
+
+
+def test_many_pivot_engines_chunk_tables(gpu):
+    # the chunk-sum tables of a partial table (FP64, indexed like the table, the other pivots'
+    # weight applied per chunk) against the FP64 walk
+    old = get_tuning()
+    try:
+        set_tuning(chunk_tables=1)
+        for cc in _many_pivot_circuits()[:3]:
+            s = Simulator(cc)
+            sv = O.dense_statevector(cc, 0)
+            ys = [int(i) for i in np.argsort(-np.abs(sv))[:32]]
+            got = s.amplitudes([0] * len(ys), ys)
+            ref = s.amplitudes_fp64([0] * len(ys), ys)
+            assert np.max(np.abs(got - ref)) <= 1e-12 * float(np.max(np.abs(ref)))
+    finally:
+        set_tuning(chunk_tables=2)
