@@ -284,8 +284,10 @@ def run_gb300(args):
         # work of one step: branches enumerated (vanishing pairs excluded) and reference-form ops
         branches_step, ops_step, popc_step, logic_step, per_boundary = enumerated(L, N, sim, n)
         peaks = (ct.c_double * 4)()
+        fma2 = ct.c_double(0.0)
         tp0 = time.perf_counter()
         N.check(L.pq_measure_peaks(peaks))
+        N.check(L.pq_measure_fma2_rate(ct.byref(fma2)))
         peak_clocks = clk.summary(tp0, time.perf_counter())
         if dist:
             dist.barrier()
@@ -384,6 +386,10 @@ def run_gb300(args):
                      "peak_source": "measured fma.f32 rate on this device (pq_measure_peaks), not a vendor figure",
                      "peak_sm_mhz": peak_clocks.get("sm_mhz"),
                      "peak_nominal": fma_nominal / 1e12, "frac_of_nominal": achieved / fma_nominal,
+                     "peak_fma_f32x2": fma2.value / 1e12,
+                     "frac_of_fma_f32x2": achieved / fma2.value if fma2.value > 0 else None,
+                     "peak_fma_f32x2_source": "measured rate of the paired fma.rn.f32x2 form the walk issues "
+                                              "(pq_measure_fma2_rate), FP32 ops",
                      "peak_nominal_source": "%d SMs x 128 FP32 lanes x 2070 MHz" % int(peaks[3]),
                      "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one full-size launch, "
                                        "ncu capture in profiles/enum_kernel_many_boundaries.md",

@@ -262,6 +262,9 @@ PQ_API int64_t pq_sim_launch_items(pq_sim *sim, int64_t n);
 /* Issue rates measured on the current device: [0] lop3.b32 ops/s, [1] popc.b32 ops/s,
  * [2] fma.f32 ops/s, [3] SM count. */
 PQ_API pq_status pq_measure_peaks(double out[4]);
+/* FP32 FMA operations per second issued as paired fma.rn.f32x2 (two per instruction), the form
+ * the enumeration's even steps use. */
+PQ_API pq_status pq_measure_fma2_rate(double *out);
 
 /* ---- checks (bit-exact comparisons against a CPU restatement) ------------------------ */
 /* Canonical dump of branch engine `branch`: normal form, diagonal masks, kernel and

@@ -1061,10 +1061,37 @@ static std::vector<int> low_coordinates_many_pivots(const HostEngine& e, int di_
     return L;
 }
 
+// Low (walked) coordinates of an engine whose joint table holds all its pivots: any DI
+// coordinates will do, so those whose Z4 increment is even come first (an even step is one
+// paired FMA per accumulator pair, an odd one four scalar FMA plus a swap), keeping up to three
+// pivot-free coordinates high as the pair coordinates of the walk's units (odd ones kept first).
+// Returns them ascending.
+static std::vector<int> low_coordinates_even_first(const HostEngine& e, int DI) {
+    const int d = e.d;
+    std::vector<char> kept((size_t)d, 0);
+    int keep = 0;
+    for (int pass = 0; pass < 2; pass++)  // pivot-free odd coordinates, then pivot-free even ones
+        for (int j = d - 1; j >= 0 && keep < 3; j--)
+            if (e.R[(size_t)j] == 0 && (int)e.lp0[(size_t)j] == 1 - pass && !kept[(size_t)j]) {
+                kept[(size_t)j] = 1;
+                keep++;
+            }
+    std::vector<int> L;
+    for (int pass = 0; pass < 3 && (int)L.size() < DI; pass++)  // even, odd, then the kept ones
+        for (int j = 0; j < d && (int)L.size() < DI; j++) {
+            const bool take = pass == 0 ? (!kept[(size_t)j] && !e.lp0[(size_t)j])
+                                        : (pass == 1 ? (!kept[(size_t)j] && e.lp0[(size_t)j]) : kept[(size_t)j] != 0);
+            if (take) L.push_back(j);
+        }
+    std::sort(L.begin(), L.end());
+    return L;
+}
+
 HostEngine device_order(const HostEngine& e, int di_max, std::vector<int>& perm) {
-    // The low DI coordinates (the walked ones) are those of the joint table: the first DI in the
-    // reference order, or for an engine with more pivots than one table holds (and d <= 62)
-    // those low_coordinates_many_pivots picks, moved to the front.  Among them the coordinates
+    // The low DI coordinates (the walked ones) are those of the joint table, moved to the front:
+    // for an engine with d <= 62 those low_coordinates_even_first picks, or, with more pivots
+    // than one table holds, those low_coordinates_many_pivots picks; else the first DI in the
+    // reference order.  Among them the coordinates
     // whose Z4 increment is even come first (stable), then the odd ones: the walk's fixed-
     // position steps are then even quarter turns (paired FMA) for almost every engine.  The
     // other coordinates keep the reference order.  perm[j] = reference coordinate of device
@@ -1072,6 +1099,11 @@ HostEngine device_order(const HostEngine& e, int di_max, std::vector<int>& perm)
     const int d = e.d;
     std::vector<int> low;
     if (e.rank > kJointMaxPivots && d <= 62) low = low_coordinates_many_pivots(e, di_max);
+    else if (d <= 62) {
+        int DI = std::min(d, di_max);
+        if (DI + e.rank > kJointMaxBits) DI = std::max(0, kJointMaxBits - e.rank);
+        if (DI >= 3) low = low_coordinates_even_first(e, DI);
+    }
     if (low.size() < 3) {
         low.clear();
         int DI = std::min(d, di_max);

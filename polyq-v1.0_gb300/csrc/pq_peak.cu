@@ -50,9 +50,60 @@ __global__ void __launch_bounds__(256) peak_ffma(uint32_t *out, int iters) {
     out[blockIdx.x * blockDim.x + threadIdx.x] = __float_as_uint(a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7);
 }
 
+// Paired FP32 FMA (fma.rn.f32x2 on a 64-bit register pair: two FP32 FMA per instruction), the
+// form the enumeration's even quarter-turn steps issue.
+__global__ void __launch_bounds__(256) peak_ffma2(uint32_t *out, int iters) {
+    uint64_t a[8];
+    for (int k = 0; k < 8; k++) {
+        const float lo = threadIdx.x * 1e-3f + (float)k, hi = lo + 0.5f;
+        asm("mov.b64 %0, {%1, %2};" : "=l"(a[k]) : "f"(lo), "f"(hi));
+    }
+    uint64_t s2, c2;
+    {
+        const float s = 0.999f, c = 1e-7f * (float)(blockIdx.x + 1);
+        asm("mov.b64 %0, {%1, %1};" : "=l"(s2) : "f"(s));
+        asm("mov.b64 %0, {%1, %1};" : "=l"(c2) : "f"(c));
+    }
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int k = 0; k < 8; k++) asm volatile("fma.rn.f32x2 %0, %0, %1, %2;" : "+l"(a[k]) : "l"(s2), "l"(c2));
+    }
+    uint64_t x = 0;
+    for (int k = 0; k < 8; k++) x ^= a[k];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = (uint32_t)x ^ (uint32_t)(x >> 32);
+}
+
 }  // namespace pq
 
 using namespace pq;
+
+extern "C" PQ_API pq_status pq_measure_fma2_rate(double *out) {
+    // FP32 FMA operations per second issued as fma.rn.f32x2 (two per instruction)
+    if (!out) return PQ_ERR_INVALID_ARG;
+    int dev = 0;
+    cudaDeviceProp p;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&p, dev) != cudaSuccess) return PQ_ERR_NO_DEVICE;
+    const int block = 256, blocks_per_sm = 8, iters = 4096;
+    const int grid = p.multiProcessorCount * blocks_per_sm;
+    uint32_t *buf = nullptr;
+    if (cudaMalloc(&buf, (size_t)grid * block * sizeof(uint32_t)) != cudaSuccess) return PQ_ERR_OUT_OF_MEMORY;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    pq_status st = PQ_OK;
+    peak_ffma2<<<grid, block>>>(buf, iters);  // warm-up
+    cudaEventRecord(e0);
+    for (int r = 0; r < 5; r++) peak_ffma2<<<grid, block>>>(buf, iters);
+    cudaEventRecord(e1);
+    if (cudaEventSynchronize(e1) != cudaSuccess) st = PQ_ERR_DEVICE;
+    float ms = 0.f;
+    if (st == PQ_OK) cudaEventElapsedTime(&ms, e0, e1);
+    *out = ms > 0.f ? 5.0 * (double)grid * block * iters * 8.0 * 2.0 / (ms * 1e-3) : 0.0;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(buf);
+    return st;
+}
 
 extern "C" PQ_API pq_status pq_measure_peaks(double out[4]) {
     // out: lop3.b32 ops/s, popc.b32 ops/s, fma.f32 ops/s, SM count

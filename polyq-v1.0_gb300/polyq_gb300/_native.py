@@ -99,6 +99,7 @@ SIGNATURES = {
     "pq_sim_enumerated": (ct.c_int, [P, ct.c_int64, f64p, f64p]),
     "pq_batch_enumerated": (ct.c_int, [P, f64p]),
     "pq_measure_peaks": (ct.c_int, [f64p]),
+    "pq_measure_fma2_rate": (ct.c_int, [f64p]),
     "pq_sim_autotune": (ct.c_int, [P, ct.c_int64, u64p, u64p, ct.c_int32, ct.POINTER(Tuning), f64p]),
     "pq_sim_get_tuning": (ct.c_int, [P, ct.POINTER(Tuning)]),
     "pq_batch_autotune": (ct.c_int, [P, u64p, u64p, ct.c_int32, ct.POINTER(Tuning), f64p]),
