@@ -796,12 +796,35 @@ def leg_small(args, clk=None, cpu_runs=200):
         clat.append(time.perf_counter() - t1)
     kms = (ct.c_float * 3)()
     N.check(L.pq_sim_kernel_ms(sim.handle, 1, kms))
+    # resident mode: the same calls served by a kernel kept on one SM between requests
+    gcall()
+    a_regular = complex(ob[0], ob[1])
+    sim.set_resident(1.0)
+    for _ in range(20):
+        gcall()
+    rlat, rpy = [], []
+    for _ in range(max(200, cpu_runs)):
+        t1 = time.perf_counter()
+        gcall()
+        rlat.append(time.perf_counter() - t1)
+        t1 = time.perf_counter()
+        ar = sim.amplitudes([0], [0])[0]
+        rpy.append(time.perf_counter() - t1)
+    a_resident = complex(ob[0], ob[1])
+    sim.set_resident(0)
+    leg_res = {"c_abi_p50_ms": 1e3 * _pct(rlat, 0.5), "c_abi_p99_ms": 1e3 * _pct(rlat, 0.99),
+               "python_p50_ms": 1e3 * _pct(rpy, 0.5), "python_p99_ms": 1e3 * _pct(rpy, 0.99),
+               "runs": len(rlat), "identical_to_regular": bool(a_resident == a_regular and ar == a),
+               "c_abi_p50_over_cpu_p50": _pct(rlat, 0.5) / _pct(clat, 0.5),
+               "note": "pq_sim_set_resident(sim, 1.0): one block stays on one SM and serves one-boundary "
+                       "pq_amplitudes calls through mapped host memory"}
     leg_cabi = {"gpu_p50_ms": 1e3 * _pct(glat, 0.5), "gpu_p99_ms": 1e3 * _pct(glat, 0.99),
                 "device_ms_last_call": kms[0] + kms[1] + kms[2],
                 "cpu_p50_ms": 1e3 * _pct(clat, 0.5), "cpu_p99_ms": 1e3 * _pct(clat, 0.99), "runs": len(glat),
                 "note": "pq_amplitudes vs the CPU restatement's pqo_amplitudes (one thread), buffers packed once, "
                         "one ctypes call per amplitude"}
     leg = {"value": 1.0 / _pct(lat, 0.5), "unit": "amplitudes/s (serial calls)", "c_abi_level": leg_cabi,
+           "resident": leg_res,
            "amplitude": [a.real, a.imag], "probability": p, "p50_ms": 1e3 * _pct(lat, 0.5),
            "p99_ms": 1e3 * _pct(lat, 0.99), "probability_p50_ms": 1e3 * _pct(plat, 0.5),
            "abs_err_vs_fp64_oracle": abs(a - want), "abs_err_vs_dense": abs(a - dense),

@@ -109,6 +109,16 @@ PQ_API pq_status pq_sim_stats(const pq_sim *sim, pq_stats *out);
  * FP64 reduction). */
 PQ_API pq_status pq_amplitudes(pq_sim *sim, int64_t n, const uint64_t *x, const uint64_t *y, double *out,
                                double *errbound);
+/* Low-latency single amplitudes (no counterpart in the reference crate).  idle_seconds > 0:
+ * one-boundary pq_amplitudes calls are served by a kernel that stays resident on one SM (one
+ * block) and takes requests through mapped host memory, so a call costs no launch and finds the
+ * kernel's code and the engine's data in that SM's caches; the kernel returns after
+ * idle_seconds without a request and is launched again by the next one.  0 turns it off.  Only
+ * for simulators whose single amplitude is small (at most 2^14 branches over at most 64 branch
+ * engines; else PQ_ERR_UNSUPPORTED).  Results are those of the regular path.  While the kernel
+ * is resident, device-wide synchronisation in the process (cudaDeviceSynchronize, cudaFree)
+ * waits for it to return. */
+PQ_API pq_status pq_sim_set_resident(pq_sim *sim, double idle_seconds);
 /* Simulator::probability -- sim.rs:196-198: |amplitude|^2, n doubles. */
 PQ_API pq_status pq_probabilities(pq_sim *sim, int64_t n, const uint64_t *x, const uint64_t *y, double *out);
 /* Simulator::marginal_probability -- sim.rs:225-231, for one input x and nmeas (qubit, outcome)

@@ -802,7 +802,23 @@ struct pq_sim {
         std::map<int64_t, std::unique_ptr<Plan>> many;       // n boundaries (sampling)
     };
     std::map<std::vector<int>, std::unique_ptr<Marg>> marg;
+    // resident mode (pq_sim_set_resident): single-boundary amplitudes served by resident_kernel
+    struct Resident {
+        std::unique_ptr<Plan> plan;  // its own one-boundary plan (fused)
+        HostPinned box;              // ResidentBox + 2 nw boundary words, mapped
+        cudaStream_t stream = nullptr;
+        cudaEvent_t ev = nullptr;    // recorded after each launch: complete once the kernel returned
+        bool launched = false;
+        unsigned seq = 0;
+        double idle_s = 0.0;
+        ~Resident() {
+            if (ev) cudaEventDestroy(ev);
+            if (stream) cudaStreamDestroy(stream);
+        }
+    };
+    std::unique_ptr<Resident> res;
     ~pq_sim() {
+        res.reset();
         plans.clear();
         marg.clear();
         if (stream) cudaStreamDestroy(stream);
@@ -950,6 +966,8 @@ PQ_API pq_status pq_analyze(const pq_circuit_desc *c, int32_t strategy, int32_t 
     return PQ_OK;
 }
 
+static pq_status resident_stop(pq_sim *s);
+
 PQ_API void pq_sim_destroy(pq_sim *s) {
     if (!s) return;
     if (s->host_only) {
@@ -957,6 +975,10 @@ PQ_API void pq_sim_destroy(pq_sim *s) {
         return;
     }
     cudaSetDevice(s->device);
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        resident_stop(s);
+    }
     if (s->stream) cudaStreamSynchronize(s->stream);
     delete s;
 }
@@ -1014,6 +1036,122 @@ static pq_status check_n(int64_t n) {
     return PQ_OK;
 }
 
+// Resident mode.  Stop the resident kernel (it returns at its next poll) and wait for it.
+static pq_status resident_stop(pq_sim *s) {
+    if (!s->res || !s->res->launched) return PQ_OK;
+    pq_sim::Resident &R = *s->res;
+    reinterpret_cast<volatile ResidentBox *>(R.box.p)->stop = 1;
+    std::atomic_thread_fence(std::memory_order_seq_cst);
+    CU(cudaEventSynchronize(R.ev));
+    R.launched = false;
+    return PQ_OK;
+}
+
+// One boundary through the resident kernel (caller holds s->mu): the boundary and a new request
+// number into the mapped box, then a bounded wait for the request number to come back; the
+// kernel is launched (again) when it is not running.  The kernel's copy of the boundary it
+// evaluated must equal the one sent, else the request is made again (at most 8 times).
+static pq_status resident_eval(pq_sim *s, const uint64_t *x, const uint64_t *y, double *out, double *err) {
+    pq_sim::Resident &R = *s->res;
+    if (!R.plan) {
+        auto P = std::make_unique<Plan>();
+        std::vector<Segment> segs{{&s->main, 1}};
+        pq_status st = build_plan(segs, s->nw, R.stream, s->tu, *P);
+        if (st != PQ_OK) return st;
+        if (!P->fused) return fail(PQ_ERR_UNSUPPORTED, "resident mode needs single amplitudes of at most 2^14 branches");
+        R.plan = std::move(P);
+    }
+    Plan &P = *R.plan;
+    volatile ResidentBox *b = reinterpret_cast<volatile ResidentBox *>(R.box.p);
+    const int nw = s->nw;
+    for (int w = 0; w < nw; w++) {
+        b->words[w] = x[w];
+        b->words[nw + w] = y[w];
+    }
+    auto launch = [&]() -> pq_status {
+        b->stop = 0;
+        b->exited = 0;
+        KArgs a = P.args;
+        ResidentBox *bd = R.box.dev<ResidentBox>();
+        a.out = bd->out;
+        a.err = &bd->err;
+        const unsigned long long idle_ns = (unsigned long long)(R.idle_s * 1e9);
+        const unsigned long long max_polls = idle_ns + (1ull << 24);  // every poll takes > 1 ns
+        if (P.minb == 2)
+            resident_kernel<2><<<1, P.fused_block, P.fused_smem, R.stream>>>(a, bd, b->done_seq, idle_ns, max_polls);
+        else
+            resident_kernel<3><<<1, P.fused_block, P.fused_smem, R.stream>>>(a, bd, b->done_seq, idle_ns, max_polls);
+        CU(cudaGetLastError());
+        CU(cudaEventRecord(R.ev, R.stream));
+        R.launched = true;
+        return PQ_OK;
+    };
+    // `exited` is the kernel's last write: once set, the kernel takes no further request
+    if (!R.launched || b->exited) {
+        if (R.launched) CU(cudaEventSynchronize(R.ev));
+        pq_status st = launch();
+        if (st != PQ_OK) return st;
+    }
+    bool same = false;
+    for (int attempt = 0; attempt < 8 && !same; attempt++) {
+        const unsigned want = ++R.seq;
+        std::atomic_thread_fence(std::memory_order_seq_cst);  // the boundary before the request number
+        b->req_seq = want;
+        const double t0 = now_s();
+        for (unsigned long spins = 0; b->done_seq != want; spins++) {
+            if ((spins & 4095) == 4095) {
+                if (b->exited && b->done_seq != want) {  // returned (idle) before it saw the request
+                    CU(cudaEventSynchronize(R.ev));
+                    pq_status st = launch();
+                    if (st != PQ_OK) return st;
+                }
+                if (now_s() - t0 > 10.0) {
+                    const cudaError_t q = cudaEventQuery(R.ev);
+                    if (q != cudaSuccess && q != cudaErrorNotReady) return cuda_fail(q, "resident kernel");
+                    return fail(PQ_ERR_TIMEOUT, "resident kernel did not answer within 10 s");
+                }
+            }
+        }
+        std::atomic_thread_fence(std::memory_order_seq_cst);  // the result after the request number
+        same = true;
+        for (int w = 0; w < nw; w++) same = same && b->words[2 * nw + w] == x[w] && b->words[3 * nw + w] == y[w];
+    }
+    if (!same) return fail(PQ_ERR_INTERNAL, "resident kernel evaluated a boundary other than the one sent");
+    if (b->errflag) return fail(PQ_ERR_INTERNAL, "device self-check failed (odd Z8 increment)");
+    out[0] = b->out[0];
+    out[1] = b->out[1];
+    if (err) err[0] = b->err;
+    return PQ_OK;
+}
+
+PQ_API pq_status pq_sim_set_resident(pq_sim *s, double idle_seconds) {
+    if (!s || !(idle_seconds >= 0.0) || idle_seconds > 3600.0) return fail(PQ_ERR_INVALID_ARG, "idle_seconds in 0..3600");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->host_only) return fail(PQ_ERR_NO_DEVICE, "simulator was created by pq_analyze (host structures only)");
+    CU(cudaSetDevice(s->device));
+    pq_status st = resident_stop(s);
+    if (st != PQ_OK) return st;
+    if (idle_seconds == 0.0) {
+        s->res.reset();
+        return PQ_OK;
+    }
+    if (!s->res) {
+        auto R = std::make_unique<pq_sim::Resident>();
+        CU(R->box.alloc(sizeof(ResidentBox) + (size_t)4 * s->nw * 8));
+        std::memset(R->box.p, 0, R->box.n);
+        CU(cudaStreamCreateWithFlags(&R->stream, cudaStreamNonBlocking));
+        CU(cudaEventCreateWithFlags(&R->ev, cudaEventDisableTiming));
+        s->res = std::move(R);
+    }
+    s->res->idle_s = idle_seconds;
+    // the plan is built (and its fitness checked) now, so an unsuitable simulator fails here
+    std::vector<uint64_t> z((size_t)s->nw, 0ull);
+    double o[2];
+    st = resident_eval(s, z.data(), z.data(), o, nullptr);
+    if (st != PQ_OK) s->res.reset();
+    return st;
+}
+
 PQ_API pq_status pq_amplitudes(pq_sim *s, int64_t n, const uint64_t *x, const uint64_t *y, double *out,
                                double *errbound) {
     if (!s || !x || !y || !out) return fail(PQ_ERR_INVALID_ARG, "null argument");
@@ -1022,6 +1160,7 @@ PQ_API pq_status pq_amplitudes(pq_sim *s, int64_t n, const uint64_t *x, const ui
     std::lock_guard<std::mutex> lk(s->mu);
     if (s->host_only) return fail(PQ_ERR_NO_DEVICE, "simulator was created by pq_analyze (host structures only)");
     CU(cudaSetDevice(s->device));
+    if (n == 1 && s->res) return resident_eval(s, x, y, out, errbound);
     Plan *P = nullptr;
     st = sim_plan(s, n, &P);
     if (st != PQ_OK) return st;
@@ -1718,6 +1857,11 @@ PQ_API int64_t pq_sim_launch_items(pq_sim *s, int64_t n) {
 // layout depends on it); cached plans point into the old tables and are dropped first.
 static pq_status retable_sim(pq_sim *s, int di) {
     CU(cudaStreamSynchronize(s->stream));
+    if (s->res) {  // its plan points into the tables about to be rebuilt
+        pq_status st = resident_stop(s);
+        if (st != PQ_OK) return st;
+        s->res->plan.reset();
+    }
     s->plans.clear();
     s->main.dev.clear();
     s->main.mem.clear();

@@ -80,6 +80,7 @@ SIGNATURES = {
     "pq_amplitudes_fp64": (ct.c_int, [P, ct.c_int64, u64p, u64p, f64p]),
     "pq_amplitudes_noalloc": (ct.c_int, [P, ct.c_int64, P, P, P, P, P]),
     "pq_sim_device_check": (ct.c_int, [P, ct.c_int64, ct.POINTER(ct.c_int32)]),
+    "pq_sim_set_resident": (ct.c_int, [P, ct.c_double]),
     "pq_batch_create": (ct.c_int, [ct.c_int32, ct.POINTER(P), i64p, ct.POINTER(P)]),
     "pq_batch_destroy": (None, [P]),
     "pq_batch_run": (ct.c_int, [P, u64p, u64p, f64p, f64p]),

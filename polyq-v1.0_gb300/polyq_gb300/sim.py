@@ -127,6 +127,11 @@ class Simulator:
         """src/pybind.rs:155-157."""
         return float(self.probabilities([input], [output])[0])
 
+    def set_resident(self, idle_seconds: float):
+        """Low-latency single amplitudes: one-boundary calls served by a resident kernel that
+        returns after idle_seconds without a request (0 turns the mode off)."""
+        N.check(self._L.pq_sim_set_resident(self._h, float(idle_seconds)))
+
     def amplitudes_plain(self, inputs, outputs):
         xs = pack_bits(inputs, self.num_qubits)
         ys = pack_bits(outputs, self.num_qubits)
