@@ -24,7 +24,11 @@ cfg1_small, cfg3_batched, cfg5_serve
            per-circuit and per-boundary paths, CPU restatement per branch-dimension bucket) and
            the served Poisson stream (throughput, p50/p99 at the offered load, below saturation
            and saturated); each leg with its own clock summary (nvidia-smi every 50 ms)
+readme_statevector
+           at N=1 also the reference README's own benchmark table (statevectors of its two seeded
+           layered circuits, construction + statevector) beside the published CPU timings
 workloads  --workload many_boundaries (default) | batched | serve | small | rotations | sample | estimate
+           | readme
 cpu_baseline  the CPU oracle (a restatement of the reference engine) on all host threads
 --impl reference  times the same CPU restatement on the same workload (bounded sample)
 """
@@ -413,6 +417,7 @@ def run_gb300(args):
         line["cfg1_small"] = leg_small(args, clk)
         line["cfg3_batched"] = leg_batched(args, clk, cpu=not args.no_cpu)
         line["cfg5_serve"] = leg_serve(args, clk)
+        line["readme_statevector"] = leg_readme(args, clk)
     clk.__exit__(None, None, None)
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -839,6 +844,69 @@ def leg_small(args, clk=None, cpu_runs=200):
     return leg
 
 
+# The reference README's benchmark table (README.md:203-208; harness src/bin/benchmark.rs:10-28):
+# whole statevectors of random_layered(n, rounds) circuits from Rng::new(1000 + n), input 0,
+# timed from Simulator::with_options to the last amplitude, on an unspecified CPU ("sandbox").
+README_ROWS = [  # n, rounds, published dense / cached / auto ms
+    (10, 3, {"dense": 0.07, "cached": 62.0, "auto": 18.4}),
+    (12, 2, {"dense": 0.27, "cached": 8.6, "auto": 7.5}),
+]
+
+
+def leg_readme(args, clk=None, runs=10):
+    """The reference's own published timings, same circuits and the same timed span (simulator
+    construction + statevector), on the GPU beside the CPU restatement on all host threads and
+    the published numbers; every GPU statevector checked against the dense oracle (the harness
+    asserts max |diff| < 1e-7)."""
+    pq, N = _gpu_setup()
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import numpy as np
+
+    import oracle
+    from polyq_gb300.rng import Rng, random_layered
+    rows = []
+    w0 = time.perf_counter()
+    for n, rounds, pub in README_ROWS:
+        c = random_layered(n, rounds, Rng(1000 + n))
+        t1 = time.perf_counter()
+        dense = oracle.dense_statevector(c, 0)
+        dense_ms = 1e3 * (time.perf_counter() - t1)
+        row = {"n": n, "rounds": rounds, "t_count": c.t_count(), "published_ms": pub, "dense_port_ms": dense_ms}
+        for strat in ("cached", "auto"):
+            wall, sv_only, err = [], [], 0.0
+            sim = None
+            for r in range(runs):
+                t1 = time.perf_counter()
+                sim = pq.Simulator(c, strat)
+                sv = sim.statevector(0)
+                wall.append(time.perf_counter() - t1)
+                err = max(err, float(np.max(np.abs(sv - dense))))
+            for r in range(runs):
+                t1 = time.perf_counter()
+                sim.statevector(0)
+                sv_only.append(time.perf_counter() - t1)
+            cpu = []
+            for r in range(3):
+                t1 = time.perf_counter()
+                ref = oracle.OracleSim(c, strat)
+                ref.amplitudes([0] * (1 << n), list(range(1 << n)))
+                cpu.append(time.perf_counter() - t1)
+            st = sim.stats_full()
+            row[strat] = {"gpu_first_ms": 1e3 * wall[0], "gpu_ms": 1e3 * statistics.median(wall),
+                          "gpu_statevector_only_ms": 1e3 * statistics.median(sv_only),
+                          "cpu_port_ms": 1e3 * statistics.median(cpu), "cpu_threads": os.cpu_count(),
+                          "published_over_gpu": pub[strat] / (1e3 * statistics.median(wall)),
+                          "max_abs_err_vs_dense": err, "branch_dim": st["branch_dim"], "pairs": st["pairs"]}
+        rows.append(row)
+    w1 = time.perf_counter()
+    leg = {"rows": rows, "runs": runs,
+           "note": "gpu_ms: median over fresh simulators of construction + statevector (the harness's span); "
+                   "published_ms: the reference on an unspecified CPU; cpu_port_ms: the CPU restatement here"}
+    if clk is not None:
+        leg["clocks"] = clk.summary(w0, w1)
+    return leg
+
+
 def run_small(args):
     leg = leg_small(args)
     line = {"metric": METRIC, "workload": "small", "n_gpus": 1, "data": "synthetic", **leg}
@@ -986,7 +1054,8 @@ def main():
                     "blocks_per_sm[,unit_chunks] (implies --no-autotune)")
     ap.add_argument("--boundaries", type=int, default=4096, help="boundary count (profiling of smaller cases)")
     ap.add_argument("--workload", default="many_boundaries",
-                    choices=["many_boundaries", "batched", "serve", "small", "rotations", "sample", "estimate"])
+                    choices=["many_boundaries", "batched", "serve", "small", "rotations", "sample", "estimate",
+                             "readme"])
     ap.add_argument("--rate", type=float, default=5000.0, help="serve: offered requests/s")
     ap.add_argument("--duration", type=float, default=2.0, help="serve: seconds of arrivals")
     ap.add_argument("--slots", type=int, default=256, help="serve: requests per wave")
@@ -1007,6 +1076,10 @@ def main():
         return run_serve(args)
     if args.workload == "small":
         return run_small(args)
+    if args.workload == "readme":
+        print(json.dumps({"metric": METRIC, "workload": "readme", "n_gpus": 1, "data": "synthetic",
+                          **leg_readme(args)}), flush=True)
+        return 0
     if args.workload == "sample":
         return run_sample(args)
     if args.workload == "estimate":

@@ -32,6 +32,21 @@ def parse_strategy(strategy: str, pairs):
 def pack_bits(values, nq: int) -> np.ndarray:
     """Integer bitstrings -> (n, ceil(nq/64)) little-endian uint64 words."""
     nw = max(1, (nq + 63) // 64)
+    if nw == 1:
+        # one word per bitstring: converted and checked as an array
+        if isinstance(values, np.ndarray) and values.dtype.kind in "iu":
+            arr = values.reshape(-1)
+            if arr.dtype.kind == "i" and arr.size and int(arr.min()) < 0:
+                raise ValueError("negative bitstring")
+            arr = arr.astype(np.uint64)
+        else:
+            try:
+                arr = np.fromiter((int(v) for v in values), dtype=np.uint64)
+            except OverflowError:
+                raise ValueError("bitstring does not fit %d qubits" % nq) from None
+        if nq < 64 and arr.size and int((arr >> np.uint64(nq)).max()) != 0:
+            raise ValueError("bitstring %d does not fit %d qubits" % (int(arr[(arr >> np.uint64(nq)) != 0][0]), nq))
+        return arr.reshape(-1, 1)
     vals = [int(v) for v in values]
     out = np.zeros((len(vals), nw), dtype=np.uint64)
     for i, v in enumerate(vals):
@@ -225,7 +240,7 @@ class Simulator:
         n = self.num_qubits
         if n > 24:
             raise ValueError("statevector limited to 24 qubits")
-        return self.amplitudes([input] * (1 << n), list(range(1 << n)))
+        return self.amplitudes(np.full(1 << n, input, dtype=np.uint64), np.arange(1 << n, dtype=np.uint64))
 
     # ------------------------------------------------------------------ checks
     def engine_dump(self, branch: int = 0) -> np.ndarray:

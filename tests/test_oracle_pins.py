@@ -377,3 +377,25 @@ def test_prepare_integers_agree_with_branch_phases():
                     assert not lp[d:].any()
                     checked += 1
     assert checked > 100
+
+
+# The reference README's benchmark table (README.md:203-208, harness src/bin/benchmark.rs:10-28:
+# random_layered(n, rounds) from Rng::new(1000 + n), input 0): T count, the cached engine's
+# branch dimension d and the pairs Auto chooses are printed by the reference itself.
+README_TABLE = [(10, 3, 20, 12, 3), (12, 2, 16, 7, 0)]
+
+
+@pytest.mark.parametrize("n,rounds,t,d,pairs", README_TABLE)
+def test_readme_benchmark_structure(n, rounds, t, d, pairs):
+    c = random_layered(n, rounds, Rng(1000 + n))
+    assert c.t_count() == t
+    cached, auto = O.OracleSim(c, "cached"), O.OracleSim(c, "auto")
+    assert cached.stats()["branch_dim"] == d
+    assert auto.stats()["pairs"] == pairs
+    # the library's host producer (no device needed) builds the same structures
+    from polyq_gb300 import Simulator
+    hc = Simulator(c, "cached", host_only=True).stats_full()
+    ha = Simulator(c, "auto", host_only=True).stats_full()
+    assert hc["branch_dim"] == d and ha["pairs"] == pairs
+    for k in ("free_vars", "planes", "lines", "radical", "terms"):
+        assert hc[k] == cached.stats()[k] and ha[k] == auto.stats()[k]
