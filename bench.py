@@ -873,13 +873,15 @@ def leg_readme(args, clk=None, runs=10):
         dense_ms = 1e3 * (time.perf_counter() - t1)
         row = {"n": n, "rounds": rounds, "t_count": c.t_count(), "published_ms": pub, "dense_port_ms": dense_ms}
         for strat in ("cached", "auto"):
-            wall, sv_only, err = [], [], 0.0
+            wall, built, sv_only, err = [], [], [], 0.0
             sim = None
             for r in range(runs):
                 t1 = time.perf_counter()
                 sim = pq.Simulator(c, strat)
+                t2 = time.perf_counter()
                 sv = sim.statevector(0)
                 wall.append(time.perf_counter() - t1)
+                built.append(t2 - t1)
                 err = max(err, float(np.max(np.abs(sv - dense))))
             for r in range(runs):
                 t1 = time.perf_counter()
@@ -893,6 +895,7 @@ def leg_readme(args, clk=None, runs=10):
                 cpu.append(time.perf_counter() - t1)
             st = sim.stats_full()
             row[strat] = {"gpu_first_ms": 1e3 * wall[0], "gpu_ms": 1e3 * statistics.median(wall),
+                          "construction_ms": 1e3 * statistics.median(built),
                           "gpu_statevector_only_ms": 1e3 * statistics.median(sv_only),
                           "cpu_port_ms": 1e3 * statistics.median(cpu), "cpu_threads": os.cpu_count(),
                           "published_over_gpu": pub[strat] / (1e3 * statistics.median(wall)),

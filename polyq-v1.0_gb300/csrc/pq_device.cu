@@ -84,17 +84,25 @@ struct DevMem {
     void *p = nullptr;
     size_t n = 0;
     cudaStream_t astream = nullptr;  // set: stream-ordered allocation from the device memory pool
+    bool view = false;  // a part of another allocation (not freed here)
     DevMem() = default;
     DevMem(const DevMem &) = delete;
     DevMem &operator=(const DevMem &) = delete;
     ~DevMem() { reset(); }
     void reset() {
-        if (p) {
+        if (p && !view) {
             if (astream) cudaFreeAsync(p, astream);
             else cudaFree(p);
         }
         p = nullptr;
         n = 0;
+        view = false;
+    }
+    void set_view(void *ptr, size_t bytes) {
+        reset();
+        p = ptr;
+        n = bytes;
+        view = true;
     }
     cudaError_t alloc(size_t bytes) {
         reset();
@@ -109,14 +117,23 @@ struct HostPinned {
     void *p = nullptr;
     void *d = nullptr;  // the device's address of the same memory
     size_t n = 0;
+    bool view = false;  // a part of another allocation (not freed here)
     HostPinned() = default;
     HostPinned(const HostPinned &) = delete;
     HostPinned &operator=(const HostPinned &) = delete;
     ~HostPinned() {
-        if (p) cudaFreeHost(p);
+        if (p && !view) cudaFreeHost(p);
+    }
+    void set_view(const HostPinned &whole, size_t off, size_t bytes) {
+        if (p && !view) cudaFreeHost(p);
+        p = static_cast<uint8_t *>(whole.p) + off;
+        d = static_cast<uint8_t *>(whole.d) + off;
+        n = bytes;
+        view = true;
     }
     cudaError_t alloc(size_t bytes) {
-        if (p) cudaFreeHost(p);
+        if (p && !view) cudaFreeHost(p);
+        view = false;
         p = d = nullptr;
         n = std::max<size_t>(bytes, 16);
         cudaError_t e = cudaHostAlloc(&p, n, cudaHostAllocMapped);
@@ -298,6 +315,7 @@ struct Plan {
     double fp32_floor = 0.0;  // largest over the launch's targets of Target::fp32_floor
     uint64_t last_use = 0;  // recency in the owning simulator's plan cache
     bool graph_ready = false;
+    bool eager_used = false, eager_host_used = false;  // first launches, enqueued without a graph
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     cudaGraph_t graph = nullptr;
@@ -313,6 +331,9 @@ struct Plan {
     bool last_host_io = false;  // the last launch was a fused one on the mapped host buffers
     cudaGraph_t graph_host = nullptr;
     cudaGraphExec_t gexec_host = nullptr;
+    // one device allocation and one mapped host allocation hold all of the plan's buffers
+    DevMem arena;
+    HostPinned harena;
     DevMem engines, maps, jobs, perm, kinv, istart, jdl, jcpi, jnch, partials, counter, job_vals, job_err, out_jobs,
         x, y, out, err, errflag, ioff;
     HostPinned hx, hy, hout, herr, herrflag;
@@ -359,12 +380,7 @@ static pq_status build_plan(const std::vector<Segment> &segs, int nw, cudaStream
         CU(cudaStreamCreateWithFlags(&P.stream, cudaStreamNonBlocking));
         P.own_stream = true;
     }
-    if (light) {
-        for (DevMem *m : {&P.engines, &P.maps, &P.jobs, &P.perm, &P.kinv, &P.istart, &P.jdl, &P.jcpi, &P.jnch,
-                          &P.partials, &P.counter, &P.job_vals, &P.job_err, &P.out_jobs, &P.x, &P.y, &P.out, &P.err,
-                          &P.errflag, &P.ioff})
-            m->astream = P.stream;
-    }
+    if (light) P.arena.astream = P.stream;  // one-shot plans: from the stream-ordered pool
     {
         // (boundary, branch engine) jobs are indexed with 32-bit integers on the device
         double total = 0.0;
@@ -459,35 +475,65 @@ static pq_status build_plan(const std::vector<Segment> &segs, int nw, cudaStream
         P.fp32_rest = P.fp32_rest || (E.joint && !covered);
     }
     P.nitems = istart[P.njobs];
-    CU(upload(P.engines, eng));
-    CU(upload(P.maps, maps));
-    CU(upload(P.jobs, jobs));
-    CU(upload(P.perm, perm));
-    CU(upload(P.kinv, kinv));
-    CU(upload(P.istart, istart));
-    CU(upload(P.jdl, jdl));
-    CU(upload(P.jcpi, jcpi));
-    CU(upload(P.jnch, jnch));
-    CU(upload(P.out_jobs, out_jobs));
-    if (ranged) CU(upload(P.ioff, jib));
-    CU(P.partials.alloc((size_t)P.nitems * sizeof(double2)));
-    CU(P.counter.alloc(sizeof(unsigned long long)));
-    CU(P.job_vals.alloc((size_t)P.njobs * sizeof(double2)));
-    CU(P.job_err.alloc((size_t)P.njobs * sizeof(double)));
-    CU(P.x.alloc((size_t)P.nreq * nw * 8));
-    CU(P.y.alloc((size_t)P.nreq * nw * 8));
-    CU(P.out.alloc((size_t)P.nout * 2 * sizeof(double)));
-    CU(P.err.alloc((size_t)P.nout * sizeof(double)));
-    CU(P.errflag.alloc(sizeof(int)));
+    {
+        // every device buffer is a 256-byte aligned part of one allocation; the records go up in
+        // one copy (pageable source: the call returns once the data is staged)
+        struct Part {
+            DevMem *m;
+            size_t bytes;
+            const void *src;
+        };
+        auto vb = [](const auto &v) { return v.size() * sizeof(v[0]); };
+        std::vector<Part> parts = {{&P.engines, vb(eng), eng.data()},   {&P.maps, vb(maps), maps.data()},
+                                   {&P.jobs, vb(jobs), jobs.data()},    {&P.perm, vb(perm), perm.data()},
+                                   {&P.kinv, vb(kinv), kinv.data()},    {&P.istart, vb(istart), istart.data()},
+                                   {&P.jdl, vb(jdl), jdl.data()},       {&P.jcpi, vb(jcpi), jcpi.data()},
+                                   {&P.jnch, vb(jnch), jnch.data()},    {&P.out_jobs, vb(out_jobs), out_jobs.data()}};
+        if (ranged) parts.push_back({&P.ioff, vb(jib), jib.data()});
+        const size_t nup = parts.size();
+        parts.push_back({&P.partials, (size_t)P.nitems * sizeof(double2), nullptr});
+        parts.push_back({&P.counter, sizeof(unsigned long long), nullptr});
+        parts.push_back({&P.job_vals, (size_t)P.njobs * sizeof(double2), nullptr});
+        parts.push_back({&P.job_err, (size_t)P.njobs * sizeof(double), nullptr});
+        parts.push_back({&P.x, (size_t)P.nreq * nw * 8, nullptr});
+        parts.push_back({&P.y, (size_t)P.nreq * nw * 8, nullptr});
+        parts.push_back({&P.out, (size_t)P.nout * 2 * sizeof(double), nullptr});
+        parts.push_back({&P.err, (size_t)P.nout * sizeof(double), nullptr});
+        parts.push_back({&P.errflag, sizeof(int), nullptr});
+        std::vector<size_t> off(parts.size());
+        size_t total = 0, up_end = 0;
+        for (size_t i = 0; i < parts.size(); i++) {
+            off[i] = total;
+            total += (std::max<size_t>(parts[i].bytes, 16) + 255) & ~(size_t)255;
+            if (i + 1 == nup) up_end = total;
+        }
+        CU(P.arena.alloc(total));
+        std::vector<uint8_t> stage(up_end, 0);
+        for (size_t i = 0; i < nup; i++)
+            if (parts[i].bytes) std::memcpy(stage.data() + off[i], parts[i].src, parts[i].bytes);
+        for (size_t i = 0; i < parts.size(); i++)
+            parts[i].m->set_view(P.arena.as<uint8_t>() + off[i], std::max<size_t>(parts[i].bytes, 16));
+        if (light) CU(cudaMemcpyAsync(P.arena.p, stage.data(), up_end, cudaMemcpyHostToDevice, P.stream));
+        else CU(cudaMemcpy(P.arena.p, stage.data(), up_end, cudaMemcpyHostToDevice));
+    }
     CU(cudaEventCreateWithFlags(&P.ev_in, cudaEventDisableTiming));
     CU(cudaEventCreateWithFlags(&P.ev_out, cudaEventDisableTiming));
     for (auto &e : P.tev) CU(cudaEventCreate(&e));
     if (!light) {
-        CU(P.hx.alloc((size_t)P.nreq * nw * 8));
-        CU(P.hy.alloc((size_t)P.nreq * nw * 8));
-        CU(P.hout.alloc((size_t)P.nout * 2 * sizeof(double)));
-        CU(P.herr.alloc((size_t)P.nout * sizeof(double)));
-        CU(P.herrflag.alloc(sizeof(int)));
+        // mapped host buffers of the fused host-buffer path, parts of one pinned allocation
+        const size_t bx = (size_t)P.nreq * nw * 8, bo = (size_t)P.nout * 16, be = (size_t)P.nout * 8;
+        auto r = [](size_t b) { return (std::max<size_t>(b, 16) + 255) & ~(size_t)255; };
+        CU(P.harena.alloc(2 * r(bx) + r(bo) + r(be) + r(4)));
+        size_t o = 0;
+        P.hx.set_view(P.harena, o, bx);
+        o += r(bx);
+        P.hy.set_view(P.harena, o, bx);
+        o += r(bx);
+        P.hout.set_view(P.harena, o, bo);
+        o += r(bo);
+        P.herr.set_view(P.harena, o, be);
+        o += r(be);
+        P.herrflag.set_view(P.harena, o, sizeof(int));
     }
     P.jobs_host = jobs;
     KArgs &a = P.args;
@@ -618,7 +664,16 @@ static pq_status capture(Plan &P, const KArgs *io, cudaGraph_t &graph, cudaGraph
     return PQ_OK;
 }
 
+// A plan's first launch is enqueued directly (a plan used once pays for no graph); later
+// launches replay the graph captured at the second.
 static pq_status launch_graph(Plan &P) {
+    if (!P.graph_ready && !P.eager_used) {
+        CU(enqueue_core(P, 0, -1, nullptr));
+        P.eager_used = true;
+        P.ran = true;
+        P.last_host_io = false;
+        return PQ_OK;
+    }
     if (!P.graph_ready) {
         pq_status st = capture(P, nullptr, P.graph, P.gexec);
         if (st != PQ_OK) return st;
@@ -633,6 +688,13 @@ static pq_status launch_graph(Plan &P) {
 // Fused plans on host buffers: the kernel reads the boundaries from, and writes the results to,
 // the plan's mapped pinned buffers.  The timing events are shared with launch_graph's graph.
 static pq_status launch_graph_host(Plan &P) {
+    if (!P.graph_host_ready && !P.eager_host_used) {
+        CU(enqueue_core(P, 0, -1, &P.args_host));
+        P.eager_host_used = true;
+        P.ran = true;
+        P.last_host_io = true;
+        return PQ_OK;
+    }
     if (!P.graph_host_ready) {
         pq_status st = capture(P, &P.args_host, P.graph_host, P.gexec_host);
         if (st != PQ_OK) return st;
