@@ -1094,8 +1094,8 @@ HostEngine device_order(const HostEngine& e, int di_max, std::vector<int>& perm)
     // reference order.  Among them the coordinates
     // whose Z4 increment is even come first (stable), then the odd ones: the walk's fixed-
     // position steps are then even quarter turns (paired FMA) for almost every engine.  The
-    // other coordinates keep the reference order.  perm[j] = reference coordinate of device
-    // coordinate j.
+    // other coordinates follow, those that touch no pivot first, each group in reference order.
+    // perm[j] = reference coordinate of device coordinate j.
     const int d = e.d;
     std::vector<int> low;
     if (e.rank > kJointMaxPivots && d <= 62) low = low_coordinates_many_pivots(e, di_max);
@@ -1111,16 +1111,56 @@ HostEngine device_order(const HostEngine& e, int di_max, std::vector<int>& perm)
         for (int j = 0; j < DI; j++) low.push_back(j);
     }
     const int DI = (int)low.size();
+    // Units of chunks that differ in the pair coordinates (the first three coordinates outside
+    // the walked ones that touch no pivot) are walked as sums bucketed by the parities of the
+    // walked point with the pair coordinates' G rows (the bucket walk).  Three walked coordinates
+    // with even Z4 increments whose G bits at the pair coordinates agree, placed first, keep the
+    // eight points of every group of steps in two buckets.
+    std::vector<int> even;
+    for (int j : low)
+        if (!e.lp0[(size_t)j]) even.push_back(j);
+    {
+        std::vector<char> in_low0((size_t)d, 0);
+        for (int j : low) in_low0[(size_t)j] = 1;
+        std::vector<int> pr;
+        for (int j = 0; j < d && pr.size() < 3; j++)
+            if (!in_low0[(size_t)j] && e.R[(size_t)j] == 0) pr.push_back(j);
+        if (pr.size() >= 2 && even.size() >= 3) {
+            auto gof = [&](int j) {
+                int g = 0;
+                for (size_t i = 0; i < pr.size(); i++)
+                    g |= (int)((e.Gw[(size_t)pr[i] * e.dw + (size_t)(j >> 6)] >> (j & 63)) & 1ull) << i;
+                return g;
+            };
+            int cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            for (int j : even) cnt[gof(j)]++;
+            int best = -1;
+            for (int g = 0; g < 8; g++)  // a shared value of zero first (one bucket per group)
+                if (cnt[g] >= 3 && (best < 0 || (best != 0 && cnt[g] > cnt[best]))) best = g;
+            if (best >= 0) {
+                std::vector<int> front, rest;
+                for (int j : even) (front.size() < 3 && gof(j) == best ? front : rest).push_back(j);
+                even = front;
+                even.insert(even.end(), rest.begin(), rest.end());
+            }
+        }
+    }
     perm.resize((size_t)d);
     int k = 0;
-    for (int j : low)
-        if (!e.lp0[(size_t)j]) perm[(size_t)k++] = j;
+    for (int j : even) perm[(size_t)k++] = j;
     for (int j : low)
         if (e.lp0[(size_t)j]) perm[(size_t)k++] = j;
     std::vector<char> in_low((size_t)d, 0);
     for (int j : low) in_low[(size_t)j] = 1;
-    for (int j = 0; j < d; j++)
-        if (!in_low[(size_t)j]) perm[(size_t)k++] = j;
+    // high coordinates that touch no pivot first: the lowest chunk-index bits above the pair
+    // coordinates are the lane bits of a warp's units, so a warp's 32 lanes then read the same
+    // table entry at every step (a warp-wide load costs L1 data-path time per distinct entry)
+    // (engines the enumeration handles, d <= 62; above, only the first 64 coordinates may move:
+    // the Monte-Carlo sampler maps its draws through a 64-entry coordinate table)
+    for (int pass = 0; pass < 2; pass++)
+        for (int j = 0; j < d; j++)
+            if (!in_low[(size_t)j] && (d > 62 ? pass == 0 : (e.R[(size_t)j] == 0) == (pass == 0)))
+                perm[(size_t)k++] = j;
     HostEngine p = e;
     const int abo = e.L.abo();
     std::vector<int> inv((size_t)d);

@@ -380,6 +380,155 @@ __device__ __forceinline__ void gray_chunk_rot_any(const float4 *__restrict__ W,
     }
 }
 
+// ------------------------------------------------------------------------------ bucket walk
+// The K chunks of a unit differ only in pair coordinates, so chunk k's sign for a walked
+// coordinate j is a common one times (-1)^{k . g_j}, g_j the bits of coordinate j in the pair
+// coordinates' G rows.  Its sum is therefore
+//     S_k = i^{m_k(0)} sum_x (-1)^{popc(x & k)} T_x,   T_x = sum_{s: x(s) = x} i^{e(s)} w(s),
+// x(s) = XOR of g_j over the set walked coordinates of s, e(s) the Z4 index of chunk 0 relative
+// to the walk's start: every branch point s adds its table entry to ONE bucket T_{x(s)}, and a
+// Walsh-Hadamard transform over the K buckets gives the K chunk sums -- the arithmetic of one
+// chunk for K.  With coordinates 0..2 of even Z4 increment and equal g (= gam; the host orders
+// them so), the eight points of a group (coordinates 0..2 walked, the others fixed) fall in two
+// buckets, x0 (even positions) and x0 ^ gam (odd positions), with per-lane signs that repeat
+// every group: they are summed in two local pairs and added into their buckets once per group,
+// turned by the group's start index i^{e0}.  Hi parts stay on the exact grid (every partial sum
+// is a signed sub-sum of the chunk's terms); lo parts are summed in at most 2^dl / 8 + 6
+// roundings per term, inside the walk's 2^dl-term bound.
+template <int K>
+__device__ __forceinline__ void bucket_add(uint64_t (&T)[K][2], uint32_t x, uint64_t s2, uint64_t h, uint64_t l) {
+    switch (x) {
+#define PQ_BA(c)                             \
+    case c:                                  \
+        if (c < K) {                         \
+            T[c % K][0] = ffma2(s2, h, T[c % K][0]); \
+            T[c % K][1] = ffma2(s2, l, T[c % K][1]); \
+        }                                    \
+        break;
+        PQ_BA(0) PQ_BA(1) PQ_BA(2) PQ_BA(3) PQ_BA(4) PQ_BA(5) PQ_BA(6) PQ_BA(7)
+#undef PQ_BA
+    }
+}
+
+// i * (re, im) = (-im, re) on a pair
+__device__ __forceinline__ uint64_t times_i(uint64_t p) {
+    float a, b;
+    up2(p, a, b);
+    return pk2(-b, a);
+}
+
+// Bucket walk of one unit: on return S[k] = (hi.re, hi.im, lo.re, lo.im) of chunk k's sum
+// without its start factor i^{m_k(0)}.  P1: c_j of chunk 0; grow[i]: pair coordinate i's G row
+// over the walked coordinates; wad0: the start point's entry address.
+template <int K>
+__device__ __forceinline__ void bucket_walk(uint64_t wad, uint32_t P1, const uint32_t (&grow)[3],
+                                            const uint32_t *Tg, const uint8_t *Lp, int dl, float (&S)[K][4]) {
+    constexpr int NP = K == 8 ? 3 : (K == 4 ? 2 : 1);
+    auto gbits = [&](int j) -> uint32_t {
+        uint32_t g = 0;
+#pragma unroll
+        for (int i = 0; i < NP; i++) g |= ((grow[i] >> j) & 1u) << i;
+        return g;
+    };
+    const uint32_t gam = gbits(0);
+    const uint32_t T0 = Tg[0], T1 = Tg[1], T2 = Tg[2];
+    // sign of group position p (relative coordinates gray(p) = 0,1,3,2,6,7,5,4): parity of b & gray(p)
+    const uint32_t b = ((((uint32_t)Lp[0] >> 1) ^ P1) & 1u) | (((((uint32_t)Lp[1] >> 1) ^ (P1 >> 1)) & 1u) << 1) |
+                       (((((uint32_t)Lp[2] >> 1) ^ (P1 >> 2)) & 1u) << 2);
+    auto sgn = [&](uint32_t gp) -> uint64_t {
+        const float f = __uint_as_float(((__popc(b & gp) & 1u) << 31) | 0x3F800000u);
+        return pk2(f, f);
+    };
+    const uint64_t s1p = sgn(1), s2p = sgn(3), s3p = sgn(2), s4p = sgn(6), s5p = sgn(7), s6p = sgn(5), s7p = sgn(4);
+    const uint64_t one2 = pk2(1.f, 1.f), zero2 = 0ull;
+    uint64_t T[K][2];
+#pragma unroll
+    for (int k = 0; k < K; k++) T[k][0] = T[k][1] = 0ull;
+    // the eight entries of a group are loaded one group ahead: each position's register is
+    // refilled with the next group's entry as soon as it has been added
+#define PQ_LD(a) __ldg(reinterpret_cast<const ulonglong2 *>(a))
+    uint64_t base = wad;  // the group's first point
+    ulonglong2 q0, q1, q2, q3, q4, q5, q6, q7;
+    {
+        uint64_t a = base;
+        q0 = PQ_LD(a);
+        a ^= T0; q1 = PQ_LD(a);
+        a ^= T1; q2 = PQ_LD(a);
+        a ^= T0; q3 = PQ_LD(a);
+        a ^= T2; q4 = PQ_LD(a);
+        a ^= T0; q5 = PQ_LD(a);
+        a ^= T1; q6 = PQ_LD(a);
+        a ^= T0; q7 = PQ_LD(a);
+    }
+    uint32_t e0 = 0, x0 = 0;
+    const uint32_t b2 = (b >> 2) & 1u;
+    const uint32_t ngroups = 1u << (dl - 3);
+    int jo = ngroups > 1 ? 3 : 0;  // the coordinate flipped after the group (0: none)
+    uint32_t TJ = Tg[jo];
+    for (uint32_t g = 0;; ++g) {
+        const bool last = g + 1 == ngroups;
+        // the next group starts at this group's last point (coordinate 2 flipped) with jo flipped
+        const uint64_t nb = base ^ (uint64_t)T2 ^ (uint64_t)TJ;
+        const uint32_t down = (uint32_t)(base >> (jo + 4)) & 1u;
+        const uint32_t Lpj = Lp[jo], gj = gbits(jo), cj = (P1 >> jo) & 1u;
+        const int jo2 = g + 2 < ngroups ? 3 + ctz32(g + 2) : 0;
+        const uint32_t TJ2 = Tg[jo2];
+        uint64_t a = nb;
+        uint64_t AH = q0.x, AL = q0.y, BH, BL;
+        q0 = PQ_LD(a);
+        a ^= T0; BH = ffma2(s1p, q1.x, zero2); BL = ffma2(s1p, q1.y, zero2); q1 = PQ_LD(a);
+        a ^= T1; AH = ffma2(s2p, q2.x, AH); AL = ffma2(s2p, q2.y, AL); q2 = PQ_LD(a);
+        a ^= T0; BH = ffma2(s3p, q3.x, BH); BL = ffma2(s3p, q3.y, BL); q3 = PQ_LD(a);
+        a ^= T2; AH = ffma2(s4p, q4.x, AH); AL = ffma2(s4p, q4.y, AL); q4 = PQ_LD(a);
+        a ^= T0; BH = ffma2(s5p, q5.x, BH); BL = ffma2(s5p, q5.y, BL); q5 = PQ_LD(a);
+        a ^= T1; AH = ffma2(s6p, q6.x, AH); AL = ffma2(s6p, q6.y, AL); q6 = PQ_LD(a);
+        a ^= T0; BH = ffma2(s7p, q7.x, BH); BL = ffma2(s7p, q7.y, BL); q7 = PQ_LD(a);
+        // the group's two sums, turned by i^{e0}, into their buckets
+        if (e0 & 1u) {
+            AH = times_i(AH);
+            AL = times_i(AL);
+            BH = times_i(BH);
+            BL = times_i(BL);
+        }
+        const float sg = __uint_as_float(((e0 & 2u) << 30) | 0x3F800000u);
+        const uint64_t sg2 = pk2(sg, sg);
+        if (gam == 0u) {
+            bucket_add<K>(T, x0, sg2, ffma2(one2, AH, BH), ffma2(one2, AL, BL));
+        } else {
+            bucket_add<K>(T, x0, sg2, AH, AL);
+            bucket_add<K>(T, x0 ^ gam, sg2, BH, BL);
+        }
+        if (last) break;
+        // flip jo from the group's last point (coordinate 2 set relative to its first): index
+        // + 2 b_2, then +-Lp_jo (direction from its bit) + 2 c_jo
+        e0 += 2u * b2 + (down ? 4u - Lpj : Lpj) + 2u * cj;
+        x0 ^= gam ^ gj;
+        base = nb;
+        jo = jo2;
+        TJ = TJ2;
+    }
+#undef PQ_LD
+    // Walsh-Hadamard transform over the buckets: S_k = sum_x (-1)^{popc(x & k)} T_x
+    const uint64_t neg2 = pk2(-1.f, -1.f);
+#pragma unroll
+    for (int h = 1; h < K; h <<= 1)
+#pragma unroll
+        for (int x = 0; x < K; x++)
+            if (!(x & h)) {
+#pragma unroll
+                for (int c = 0; c < 2; c++) {
+                    const uint64_t a = T[x][c], bb = T[x | h][c];
+                    T[x][c] = ffma2(one2, bb, a);
+                    T[x | h][c] = ffma2(neg2, bb, a);
+                }
+            }
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        up2(T[k][0], S[k][0], S[k][1]);
+        up2(T[k][1], S[k][2], S[k][3]);
+    }
+}
+
 // One unit of K chunks (K = 2^np: the chunk at s1 and those that differ from it in the first np
 // pair coordinates) on the FP32 joint-table path: folded start indices, c_j of the walked
 // coordinates, the rotating-frame walk, each chunk's sum rotated to its last index, the chunks
@@ -428,6 +577,27 @@ __device__ __forceinline__ void walk_unit(const EngineDev &E, const JobDev &J, c
             if ((1 << i) < K && ((k >> i) & 1)) sk |= 1ull << E.pairc[i];
         return sk;
     };
+    float acc[K][4];
+    uint32_t qk[K];  // quarter turns from each chunk's walk result to its sum
+    // bucket walk: units of 4 or 8 chunks whose first three walked coordinates have even Z4
+    // increments and equal bits in the pair coordinates' G rows
+    bool bucket = false;
+    if (MODE == 0 && (K == 4 || K == 8) && dl >= 3 && !((Lp[0] | Lp[1] | Lp[2]) & 1)) {
+        constexpr int NPK = K == 8 ? 3 : 2;
+        bool same = true;
+#pragma unroll
+        for (int i = 0; i < NPK; i++) {
+            const uint32_t gi = grow[i] & 7u;
+            same = same && (gi == 0u || gi == 7u);
+        }
+        bucket = same;
+    }
+    if (bucket) {
+        const uint64_t wad = reinterpret_cast<uint64_t>(E.wtab) | ((uint64_t)sidx << 4);
+        bucket_walk<K>(wad, P1, grow, Tg, Lp, dl, acc);
+#pragma unroll
+        for (int k = 0; k < K; k++) qk[k] = chunk_m(k) & 3u;
+    } else {
     uint32_t Pc[K], mm[K];
     uint64_t sb[K];
 #pragma unroll
@@ -445,8 +615,11 @@ __device__ __forceinline__ void walk_unit(const EngineDev &E, const JobDev &J, c
             sb[k] = 0ull;
         }
     }
-    float acc[K][4];
     gray_chunk_rot_any<MODE, K>(E.wtab, sidx, Pc, Tg, Lp, dl, acc, dbg, sb, J.k0, mm, G, (uint32_t)lomask);
+    const int jl = dl - 1;
+#pragma unroll
+    for (int k = 0; k < K; k++) qk[k] = (chunk_m(k) + (uint32_t)Lp[jl] + (((Pc[k] >> jl) & 1u) << 1)) & 3u;
+    }
     // The unit's chunks differ only in pair coordinates: their high-coordinate weights are
     // chi_rest(s1) P(pattern), so the unit sum is chi_rest(s1) sum_k P(k | pat) S_k.  The inner
     // sum runs in FP32 pairs (exact products by FMA, two-sums), the outer product in FP64 once
@@ -455,11 +628,11 @@ __device__ __forceinline__ void walk_unit(const EngineDev &E, const JobDev &J, c
     uint32_t pat = 0;  // bits of s1 at the pair coordinates the unit does not vary
     for (int i = npk; i < E.npairc; i++) pat |= (uint32_t)((s1 >> E.pairc[i]) & 1ull) << i;
     float urh = 0.f, url = 0.f, uih = 0.f, uil = 0.f;
-    const int jl = dl - 1;
 #pragma unroll
     for (int k = 0; k < K; k++) {
-        // S = i^{m_end} A, m_end = m + L'_{dl-1}: an exact quarter turn of the FP32 pairs
-        const uint32_t q = (chunk_m(k) + (uint32_t)Lp[jl] + (((Pc[k] >> jl) & 1u) << 1)) & 3u;
+        // the chunk's sum: an exact quarter turn of the FP32 pairs (walk: i^{m_end} A, m_end =
+        // m + L'_{dl-1}; bucket walk: i^{m_k(0)} S)
+        const uint32_t q = qk[k];
         float hx = acc[k][0], hy = acc[k][1], lx = acc[k][2], ly = acc[k][3];
         if (q & 1u) {
             const float t = hx; hx = -hy; hy = t;
