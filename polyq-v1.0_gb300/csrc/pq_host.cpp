@@ -1113,9 +1113,9 @@ HostEngine device_order(const HostEngine& e, int di_max, std::vector<int>& perm)
     const int DI = (int)low.size();
     // Units of chunks that differ in the pair coordinates (the first three coordinates outside
     // the walked ones that touch no pivot) are walked as sums bucketed by the parities of the
-    // walked point with the pair coordinates' G rows (the bucket walk).  Three walked coordinates
-    // with even Z4 increments whose G bits at the pair coordinates agree, placed first, keep the
-    // eight points of every group of steps in two buckets.
+    // walked point with the pair coordinates' G rows (the bucket walk).  Walked coordinates with
+    // even Z4 increments whose G bits at the pair coordinates agree, placed first (three, else
+    // two and any third), keep the eight points of every group of steps in two buckets (four).
     std::vector<int> even;
     for (int j : low)
         if (!e.lp0[(size_t)j]) even.push_back(j);
@@ -1134,9 +1134,12 @@ HostEngine device_order(const HostEngine& e, int di_max, std::vector<int>& perm)
             };
             int cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
             for (int j : even) cnt[gof(j)]++;
-            int best = -1;
-            for (int g = 0; g < 8; g++)  // a shared value of zero first (one bucket per group)
-                if (cnt[g] >= 3 && (best < 0 || (best != 0 && cnt[g] > cnt[best]))) best = g;
+            // three coordinates with one value (two buckets per group, one for the value 0),
+            // else two (four buckets) followed by any third
+            int best = -1, need = 3;
+            for (; need >= 2 && best < 0; need--)
+                for (int g = 0; g < 8; g++)
+                    if (cnt[g] >= need && (best < 0 || (best != 0 && cnt[g] > cnt[best]))) best = g;
             if (best >= 0) {
                 std::vector<int> front, rest;
                 for (int j : even) (front.size() < 3 && gof(j) == best ? front : rest).push_back(j);

@@ -388,11 +388,12 @@ __device__ __forceinline__ void gray_chunk_rot_any(const float4 *__restrict__ W,
 // x(s) = XOR of g_j over the set walked coordinates of s, e(s) the Z4 index of chunk 0 relative
 // to the walk's start: every branch point s adds its table entry to ONE bucket T_{x(s)}, and a
 // Walsh-Hadamard transform over the K buckets gives the K chunk sums -- the arithmetic of one
-// chunk for K.  With coordinates 0..2 of even Z4 increment and equal g (= gam; the host orders
-// them so), the eight points of a group (coordinates 0..2 walked, the others fixed) fall in two
-// buckets, x0 (even positions) and x0 ^ gam (odd positions), with per-lane signs that repeat
-// every group: they are summed in two local pairs and added into their buckets once per group,
-// turned by the group's start index i^{e0}.  Hi parts stay on the exact grid (every partial sum
+// chunk for K.  With coordinates 0..2 of even Z4 increment and g_0 = g_1 = gam (the host orders
+// them so; del = g_2), the eight points of a group (coordinates 0..2 walked, the others fixed)
+// fall in at most four buckets -- x0, x0 ^ gam, x0 ^ gam ^ del, x0 ^ del, two points each -- with
+// per-lane signs that repeat every group: they are summed in local pairs and added into their
+// buckets once per group (merged where buckets coincide: two when del = gam, one when both are
+// 0), turned by the group's start index i^{e0}.  Hi parts stay on the exact grid (every partial sum
 // is a signed sub-sum of the chunk's terms); lo parts are summed in at most 2^dl / 8 + 6
 // roundings per term, inside the walk's 2^dl-term bound.
 template <int K>
@@ -430,7 +431,7 @@ __device__ __forceinline__ void bucket_walk(uint64_t wad, uint32_t P1, const uin
         for (int i = 0; i < NP; i++) g |= ((grow[i] >> j) & 1u) << i;
         return g;
     };
-    const uint32_t gam = gbits(0);
+    const uint32_t gam = gbits(0), del = gbits(2);  // gbits(1) == gam
     const uint32_t T0 = Tg[0], T1 = Tg[1], T2 = Tg[2];
     // sign of group position p (relative coordinates gray(p) = 0,1,3,2,6,7,5,4): parity of b & gray(p)
     const uint32_t b = ((((uint32_t)Lp[0] >> 1) ^ P1) & 1u) | (((((uint32_t)Lp[1] >> 1) ^ (P1 >> 1)) & 1u) << 1) |
@@ -474,35 +475,52 @@ __device__ __forceinline__ void bucket_walk(uint64_t wad, uint32_t P1, const uin
         const int jo2 = g + 2 < ngroups ? 3 + ctz32(g + 2) : 0;
         const uint32_t TJ2 = Tg[jo2];
         uint64_t a = nb;
-        uint64_t AH = q0.x, AL = q0.y, BH, BL;
+        // positions 0, 2 -> x0 (A); 1, 3 -> x0 ^ gam (B); 4, 6 -> x0 ^ gam ^ del (C); 5, 7 -> x0 ^ del (D)
+        uint64_t AH = q0.x, AL = q0.y, BH, BL, CH, CL, DH, DL;
         q0 = PQ_LD(a);
         a ^= T0; BH = ffma2(s1p, q1.x, zero2); BL = ffma2(s1p, q1.y, zero2); q1 = PQ_LD(a);
         a ^= T1; AH = ffma2(s2p, q2.x, AH); AL = ffma2(s2p, q2.y, AL); q2 = PQ_LD(a);
         a ^= T0; BH = ffma2(s3p, q3.x, BH); BL = ffma2(s3p, q3.y, BL); q3 = PQ_LD(a);
-        a ^= T2; AH = ffma2(s4p, q4.x, AH); AL = ffma2(s4p, q4.y, AL); q4 = PQ_LD(a);
-        a ^= T0; BH = ffma2(s5p, q5.x, BH); BL = ffma2(s5p, q5.y, BL); q5 = PQ_LD(a);
-        a ^= T1; AH = ffma2(s6p, q6.x, AH); AL = ffma2(s6p, q6.y, AL); q6 = PQ_LD(a);
-        a ^= T0; BH = ffma2(s7p, q7.x, BH); BL = ffma2(s7p, q7.y, BL); q7 = PQ_LD(a);
-        // the group's two sums, turned by i^{e0}, into their buckets
-        if (e0 & 1u) {
-            AH = times_i(AH);
-            AL = times_i(AL);
-            BH = times_i(BH);
-            BL = times_i(BL);
+        a ^= T2; CH = ffma2(s4p, q4.x, zero2); CL = ffma2(s4p, q4.y, zero2); q4 = PQ_LD(a);
+        a ^= T0; DH = ffma2(s5p, q5.x, zero2); DL = ffma2(s5p, q5.y, zero2); q5 = PQ_LD(a);
+        a ^= T1; CH = ffma2(s6p, q6.x, CH); CL = ffma2(s6p, q6.y, CL); q6 = PQ_LD(a);
+        a ^= T0; DH = ffma2(s7p, q7.x, DH); DL = ffma2(s7p, q7.y, DL); q7 = PQ_LD(a);
+        // the group's sums, turned by i^{e0}, into their buckets (merged where buckets coincide)
+        if (del == gam) {
+            AH = ffma2(one2, CH, AH);
+            AL = ffma2(one2, CL, AL);
+            BH = ffma2(one2, DH, BH);
+            BL = ffma2(one2, DL, BL);
         }
+        if (gam == 0u) {
+            AH = ffma2(one2, BH, AH);
+            AL = ffma2(one2, BL, AL);
+            if (del != gam) {
+                CH = ffma2(one2, DH, CH);
+                CL = ffma2(one2, DL, CL);
+            }
+        }
+        const bool odd = (e0 & 1u) != 0u;
         const float sg = __uint_as_float(((e0 & 2u) << 30) | 0x3F800000u);
         const uint64_t sg2 = pk2(sg, sg);
-        if (gam == 0u) {
-            bucket_add<K>(T, x0, sg2, ffma2(one2, AH, BH), ffma2(one2, AL, BL));
-        } else {
-            bucket_add<K>(T, x0, sg2, AH, AL);
-            bucket_add<K>(T, x0 ^ gam, sg2, BH, BL);
+        auto flush = [&](uint32_t x, uint64_t h, uint64_t l) {
+            if (odd) {
+                h = times_i(h);
+                l = times_i(l);
+            }
+            bucket_add<K>(T, x, sg2, h, l);
+        };
+        flush(x0, AH, AL);
+        if (gam != 0u) flush(x0 ^ gam, BH, BL);
+        if (del != gam) {
+            flush(x0 ^ gam ^ del, CH, CL);
+            if (gam != 0u) flush(x0 ^ del, DH, DL);
         }
         if (last) break;
         // flip jo from the group's last point (coordinate 2 set relative to its first): index
         // + 2 b_2, then +-Lp_jo (direction from its bit) + 2 c_jo
         e0 += 2u * b2 + (down ? 4u - Lpj : Lpj) + 2u * cj;
-        x0 ^= gam ^ gj;
+        x0 ^= del ^ gj;
         base = nb;
         jo = jo2;
         TJ = TJ2;
@@ -580,15 +598,15 @@ __device__ __forceinline__ void walk_unit(const EngineDev &E, const JobDev &J, c
     float acc[K][4];
     uint32_t qk[K];  // quarter turns from each chunk's walk result to its sum
     // bucket walk: units of 4 or 8 chunks whose first three walked coordinates have even Z4
-    // increments and equal bits in the pair coordinates' G rows
+    // increments and whose first two have equal bits in the pair coordinates' G rows
     bool bucket = false;
     if (MODE == 0 && (K == 4 || K == 8) && dl >= 3 && !((Lp[0] | Lp[1] | Lp[2]) & 1)) {
         constexpr int NPK = K == 8 ? 3 : 2;
         bool same = true;
 #pragma unroll
         for (int i = 0; i < NPK; i++) {
-            const uint32_t gi = grow[i] & 7u;
-            same = same && (gi == 0u || gi == 7u);
+            const uint32_t gi = grow[i] & 3u;
+            same = same && (gi == 0u || gi == 3u);
         }
         bucket = same;
     }
