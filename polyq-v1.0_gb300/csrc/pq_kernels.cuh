@@ -421,7 +421,9 @@ __device__ __forceinline__ uint64_t times_i(uint64_t p) {
 // Bucket walk of one unit: on return S[k] = (hi.re, hi.im, lo.re, lo.im) of chunk k's sum
 // without its start factor i^{m_k(0)}.  P1: c_j of chunk 0; grow[i]: pair coordinate i's G row
 // over the walked coordinates; wad0: the start point's entry address.
-template <int K>
+// PAT: which of a group's four bucket offsets coincide -- 0: gam = del = 0 (one bucket), 1:
+// del = gam != 0 (x0, x0 ^ gam), 2: gam = 0 != del (x0, x0 ^ del), 3: all four distinct.
+template <int K, int PAT>
 __device__ __forceinline__ void bucket_walk(uint64_t wad, uint32_t P1, const uint32_t (&grow)[3],
                                             const uint32_t *Tg, const uint8_t *Lp, int dl, float (&S)[K][4]) {
     constexpr int NP = K == 8 ? 3 : (K == 4 ? 2 : 1);
@@ -485,36 +487,48 @@ __device__ __forceinline__ void bucket_walk(uint64_t wad, uint32_t P1, const uin
         a ^= T0; DH = ffma2(s5p, q5.x, zero2); DL = ffma2(s5p, q5.y, zero2); q5 = PQ_LD(a);
         a ^= T1; CH = ffma2(s6p, q6.x, CH); CL = ffma2(s6p, q6.y, CL); q6 = PQ_LD(a);
         a ^= T0; DH = ffma2(s7p, q7.x, DH); DL = ffma2(s7p, q7.y, DL); q7 = PQ_LD(a);
-        // the group's sums, turned by i^{e0}, into their buckets (merged where buckets coincide)
-        if (del == gam) {
+        // the group's sums (merged where buckets coincide), turned by i^{e0}, into their buckets
+        if (PAT == 0 || PAT == 1) {  // C -> x0, D -> x0 ^ gam
             AH = ffma2(one2, CH, AH);
             AL = ffma2(one2, CL, AL);
             BH = ffma2(one2, DH, BH);
             BL = ffma2(one2, DL, BL);
         }
-        if (gam == 0u) {
+        if (PAT == 0 || PAT == 2) {  // B -> x0, D -> x0 ^ del
             AH = ffma2(one2, BH, AH);
             AL = ffma2(one2, BL, AL);
-            if (del != gam) {
-                CH = ffma2(one2, DH, CH);
-                CL = ffma2(one2, DL, CL);
+        }
+        if (PAT == 2) {
+            CH = ffma2(one2, DH, CH);
+            CL = ffma2(one2, DL, CL);
+        }
+        if (e0 & 1u) {
+            AH = times_i(AH);
+            AL = times_i(AL);
+            if (PAT != 0) {
+                if (PAT == 2) {
+                    CH = times_i(CH);
+                    CL = times_i(CL);
+                } else {
+                    BH = times_i(BH);
+                    BL = times_i(BL);
+                }
+            }
+            if (PAT == 3) {
+                CH = times_i(CH);
+                CL = times_i(CL);
+                DH = times_i(DH);
+                DL = times_i(DL);
             }
         }
-        const bool odd = (e0 & 1u) != 0u;
         const float sg = __uint_as_float(((e0 & 2u) << 30) | 0x3F800000u);
         const uint64_t sg2 = pk2(sg, sg);
-        auto flush = [&](uint32_t x, uint64_t h, uint64_t l) {
-            if (odd) {
-                h = times_i(h);
-                l = times_i(l);
-            }
-            bucket_add<K>(T, x, sg2, h, l);
-        };
-        flush(x0, AH, AL);
-        if (gam != 0u) flush(x0 ^ gam, BH, BL);
-        if (del != gam) {
-            flush(x0 ^ gam ^ del, CH, CL);
-            if (gam != 0u) flush(x0 ^ del, DH, DL);
+        bucket_add<K>(T, x0, sg2, AH, AL);
+        if (PAT == 1 || PAT == 3) bucket_add<K>(T, x0 ^ gam, sg2, BH, BL);
+        if (PAT == 2) bucket_add<K>(T, x0 ^ del, sg2, CH, CL);
+        if (PAT == 3) {
+            bucket_add<K>(T, x0 ^ gam ^ del, sg2, CH, CL);
+            bucket_add<K>(T, x0 ^ del, sg2, DH, DL);
         }
         if (last) break;
         // flip jo from the group's last point (coordinate 2 set relative to its first): index
@@ -612,7 +626,17 @@ __device__ __forceinline__ void walk_unit(const EngineDev &E, const JobDev &J, c
     }
     if (bucket) {
         const uint64_t wad = reinterpret_cast<uint64_t>(E.wtab) | ((uint64_t)sidx << 4);
-        bucket_walk<K>(wad, P1, grow, Tg, Lp, dl, acc);
+        constexpr int NPB = K == 8 ? 3 : 2;
+        uint32_t g0 = 0, g2 = 0;
+#pragma unroll
+        for (int i = 0; i < NPB; i++) {
+            g0 |= (grow[i] & 1u) << i;
+            g2 |= ((grow[i] >> 2) & 1u) << i;
+        }
+        if (g0 == 0u && g2 == 0u) bucket_walk<K, 0>(wad, P1, grow, Tg, Lp, dl, acc);
+        else if (g2 == g0) bucket_walk<K, 1>(wad, P1, grow, Tg, Lp, dl, acc);
+        else if (g0 == 0u) bucket_walk<K, 2>(wad, P1, grow, Tg, Lp, dl, acc);
+        else bucket_walk<K, 3>(wad, P1, grow, Tg, Lp, dl, acc);
 #pragma unroll
         for (int k = 0; k < K; k++) qk[k] = chunk_m(k) & 3u;
     } else {
