@@ -592,7 +592,8 @@ static pq_status build_plan(const std::vector<Segment> &segs, int nw, cudaStream
         }
         const int wpb = std::min(maxj, 8);
         const size_t smem = (size_t)(2 * nw + wpb * P.smem_words) * 8;
-        if (small && smem <= 32 * 1024) {
+        // static (SmallShared) plus dynamic shared memory within the 48 KB a launch gets without opt-in
+        if (small && smem + sizeof(SmallShared) + 256 <= 48 * 1024) {
             P.fused = true;
             P.fused_block = 32 * wpb;
             P.fused_smem = smem;

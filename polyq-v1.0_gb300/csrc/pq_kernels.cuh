@@ -381,6 +381,10 @@ __device__ __forceinline__ void gray_chunk_rot_any(const float4 *__restrict__ W,
 }
 
 // ------------------------------------------------------------------------------ bucket walk
+// Walks of up to 2^kGroupTableMaxDl steps keep their group table (two words per group of eight
+// steps) after the 32 stride words of a warp's staging array.
+static constexpr int kGroupTableMaxDl = 10;
+static constexpr int kTgWords = 32 + 2 * (1 << (kGroupTableMaxDl - 3));
 // The K chunks of a unit differ only in pair coordinates, so chunk k's sign for a walked
 // coordinate j is a common one times (-1)^{k . g_j}, g_j the bits of coordinate j in the pair
 // coordinates' G rows.  Its sum is therefore
@@ -450,10 +454,9 @@ __device__ __forceinline__ void bucket_walk(uint64_t wad, uint32_t P1, const uin
     // the eight entries of a group are loaded one group ahead: each position's register is
     // refilled with the next group's entry as soon as it has been added
 #define PQ_LD(a) __ldg(reinterpret_cast<const ulonglong2 *>(a))
-    uint64_t base = wad;  // the group's first point
     ulonglong2 q0, q1, q2, q3, q4, q5, q6, q7;
     {
-        uint64_t a = base;
+        uint64_t a = wad;
         q0 = PQ_LD(a);
         a ^= T0; q1 = PQ_LD(a);
         a ^= T1; q2 = PQ_LD(a);
@@ -463,20 +466,20 @@ __device__ __forceinline__ void bucket_walk(uint64_t wad, uint32_t P1, const uin
         a ^= T1; q6 = PQ_LD(a);
         a ^= T0; q7 = PQ_LD(a);
     }
-    uint32_t e0 = 0, x0 = 0;
-    const uint32_t b2 = (b >> 2) & 1u;
+    // group g starts at S = gray(8 g); the job's group table (stage_job) holds, per group, the
+    // XOR of S's coordinate strides, the bucket x(S) and the Z4 sum of Lp over S: the group's
+    // entry addresses, bucket and start index i^{e0}, e0 = sum Lp S + 2 parity(P1 & S), follow
+    // without any state carried from group to group
+    const uint2 *Gt = reinterpret_cast<const uint2 *>(Tg + 32);
     const uint32_t ngroups = 1u << (dl - 3);
-    int jo = ngroups > 1 ? 3 : 0;  // the coordinate flipped after the group (0: none)
-    uint32_t TJ = Tg[jo];
+    uint2 gcur = Gt[0];
     for (uint32_t g = 0;; ++g) {
         const bool last = g + 1 == ngroups;
-        // the next group starts at this group's last point (coordinate 2 flipped) with jo flipped
-        const uint64_t nb = base ^ (uint64_t)T2 ^ (uint64_t)TJ;
-        const uint32_t down = (uint32_t)(base >> (jo + 4)) & 1u;
-        const uint32_t Lpj = Lp[jo], gj = gbits(jo), cj = (P1 >> jo) & 1u;
-        const int jo2 = g + 2 < ngroups ? 3 + ctz32(g + 2) : 0;
-        const uint32_t TJ2 = Tg[jo2];
-        uint64_t a = nb;
+        const uint2 gnext = Gt[last ? g : g + 1];
+        const uint32_t Sg = (g << 3) ^ (g << 2);
+        const uint32_t x0 = gcur.y & (uint32_t)(K - 1);
+        const uint32_t e0 = (gcur.y >> 8) + ((__popc(P1 & Sg) & 1u) << 1);
+        uint64_t a = wad ^ (uint64_t)gnext.x;  // the next group's first point
         // positions 0, 2 -> x0 (A); 1, 3 -> x0 ^ gam (B); 4, 6 -> x0 ^ gam ^ del (C); 5, 7 -> x0 ^ del (D)
         uint64_t AH = q0.x, AL = q0.y, BH, BL, CH, CL, DH, DL;
         q0 = PQ_LD(a);
@@ -531,13 +534,7 @@ __device__ __forceinline__ void bucket_walk(uint64_t wad, uint32_t P1, const uin
             bucket_add<K>(T, x0 ^ del, sg2, DH, DL);
         }
         if (last) break;
-        // flip jo from the group's last point (coordinate 2 set relative to its first): index
-        // + 2 b_2, then +-Lp_jo (direction from its bit) + 2 c_jo
-        e0 += 2u * b2 + (down ? 4u - Lpj : Lpj) + 2u * cj;
-        x0 ^= del ^ gj;
-        base = nb;
-        jo = jo2;
-        TJ = TJ2;
+        gcur = gnext;
     }
 #undef PQ_LD
     // Walsh-Hadamard transform over the buckets: S_k = sum_x (-1)^{popc(x & k)} T_x
@@ -614,7 +611,7 @@ __device__ __forceinline__ void walk_unit(const EngineDev &E, const JobDev &J, c
     // bucket walk: units of 4 or 8 chunks whose first three walked coordinates have even Z4
     // increments and whose first two have equal bits in the pair coordinates' G rows
     bool bucket = false;
-    if (MODE == 0 && (K == 4 || K == 8) && dl >= 3 && !((Lp[0] | Lp[1] | Lp[2]) & 1)) {
+    if (MODE == 0 && (K == 4 || K == 8) && dl >= 3 && dl <= kGroupTableMaxDl && !((Lp[0] | Lp[1] | Lp[2]) & 1)) {
         constexpr int NPK = K == 8 ? 3 : 2;
         bool same = true;
 #pragma unroll
@@ -708,6 +705,25 @@ __device__ __forceinline__ void stage_job(const KArgs &a, int jb, uint64_t *G, u
         if (j < dlj) Tg[j] = ((1u << j) | ((uint32_t)E.Rc[j] << E.DI)) << 4;
     }
     __syncwarp();
+    // the bucket walk's group table, after the 32 stride words: for group g its start point
+    // S = gray(8 g) (bits 2 .. dl - 1): the XOR of S's strides, the parities of S with the pair
+    // coordinates' G rows (bucket) and, from bit 8, the sum of Lp over S mod 4
+    const int npj = (a.jdl[jb] >> 8) & 3;
+    if (E.joint && npj >= 2 && dlj >= 3 && dlj <= kGroupTableMaxDl) {
+        uint2 *Gt = reinterpret_cast<uint2 *>(Tg + 32);
+        for (int g = lane; g < (1 << (dlj - 3)); g += 32) {
+            const uint32_t S = ((uint32_t)g << 3) ^ ((uint32_t)g << 2);
+            uint32_t off = 0, u = 0, x = 0;
+            for (int j = 2; j < dlj; j++)
+                if ((S >> j) & 1u) {
+                    off ^= Tg[j];
+                    u += Lp[j];
+                }
+            for (int i = 0; i < npj; i++) x |= (uint32_t)(popc64(G[E.pairc[i]] & (uint64_t)S) & 1) << i;
+            Gt[g] = make_uint2(off, x | ((u & 3u) << 8));
+        }
+        __syncwarp();
+    }
 }
 
 // Sum of work item iin of job `job` (its staged data in G, R, Lp, Lm, Tg): every lane walks its
@@ -900,7 +916,9 @@ __global__ void __launch_bounds__(256, MINB) enum_kernel(KArgs a) {
     __shared__ uint64_t sR[8][64];
     __shared__ uint8_t sLp[8][64];
     __shared__ uint8_t sLm[8][64];
-    __shared__ uint32_t sTg[8][32];  // byte stride of coordinate j in the table: ((1 << j) | (R_j << DI)) * 16
+    // byte stride of coordinate j in the table, ((1 << j) | (R_j << DI)) * 16, then the bucket
+    // walk's group table
+    __shared__ __align__(16) uint32_t sTg[8][kTgWords];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     uint64_t *G = sG[wib];
     uint64_t *R = sR[wib];
@@ -1065,7 +1083,7 @@ struct SmallShared {
     uint64_t R[8][64];
     uint8_t Lp[8][64];
     uint8_t Lm[8][64];
-    uint32_t Tg[8][32];
+    alignas(16) uint32_t Tg[8][kTgWords];
     double2 val[kSmallMaxJobs];
     double err[kSmallMaxJobs];
 };
