@@ -50,6 +50,10 @@ WORKLOAD = {"n_qubits": 50, "gates": 2000, "t_count": 32, "circuit_seed": 0, "bo
             "output_seed": 1, "strategy": "auto"}
 # FP32 FMA-pipe operations per enumerated branch in the enumeration kernel's walk
 FMA_OPS_PER_BRANCH = 4
+# FP32 FMA-pipe ops the bucket walk issues per branch: per group of 8 walked points of a unit of
+# 8 chunks (64 branches), 16 paired FMA for the group sums and 8 to merge and add them into their
+# buckets, 2 FP32 ops each
+BUCKET_OPS_PER_BRANCH = 0.75
 # DRAM bytes of one full-size enumeration launch (ncu, dram__bytes_read.sum + dram__bytes_write.sum)
 TRAFFIC_BYTES_PER_LAUNCH = 8934656
 
@@ -341,9 +345,12 @@ def run_gb300(args):
     e2e_ms = 1e3 * sum(e2e_s) / len(e2e_s)
     e2e_ms = max_over_ranks(dist, e2e_ms)
     e2e_value = replica_rate(ws, branches_step, e2e_ms)
-    # roofline of the enumeration kernel.  Its arithmetic per branch is two quarter-turn-and-add
-    # updates (hi and lo complex pairs), four FP32 FMA-pipe ops; table loads and index xors are
-    # shared by the chunks of a unit.  Peak: the measured fma.f32 rate of this device.
+    # roofline of the enumeration kernel against the FP32 FMA pipe.  The per-branch form of the
+    # walk adds every branch's hi and lo complex weight pair: four FP32 FMA-pipe ops per branch,
+    # the figure the line keeps as its unit so that rates stay comparable.  The bucket walk adds a
+    # walked point's entry once for the eight chunks of its unit and issues 0.75 of them per
+    # branch (48 per group of 8 points x 8 chunks: 32 for the group sums, 16 to merge them and
+    # add them into their buckets); both fractions are reported.  Peak: the measured fma.f32 rate.
     enum_avg = sum(enum_ms) / len(enum_ms)
     lop3, popcr, fmar = peaks[0], peaks[1], peaks[2]
     # nominal FP32 FMA rate: 128 FP32 lanes per SM at the maximum SM clock (2070 MHz)
@@ -386,7 +393,14 @@ def run_gb300(args):
         "roofline": {"bound": "fp32", "achieved": achieved / 1e12, "peak": fmar / 1e12, "unit": "Tops/s",
                      "frac": achieved / fmar, "traffic": TRAFFIC_BYTES_PER_LAUNCH,
                      "kernel": "enum_kernel", "kernel_ms": enum_avg,
-                     "ops": "%d FP32 FMA-pipe ops per enumerated branch" % FMA_OPS_PER_BRANCH,
+                     "ops": "%d FP32 FMA-pipe ops per enumerated branch: the per-branch form (every branch's hi "
+                            "and lo complex weight pair added)" % FMA_OPS_PER_BRANCH,
+                     "executed_ops_per_branch": BUCKET_OPS_PER_BRANCH,
+                     "frac_executed": achieved * BUCKET_OPS_PER_BRANCH / FMA_OPS_PER_BRANCH / fmar,
+                     "executed_note": "the bucket walk adds each walked point's table entry once for the 8 chunks "
+                                      "of its unit (one bucket per point, a Walsh-Hadamard transform per unit), "
+                                      "0.75 FP32 FMA-pipe ops per branch: the FMA pipe is not its bound (ncu: "
+                                      "profiles/enum_kernel_many_boundaries.md)",
                      "peak_source": "measured fma.f32 rate on this device (pq_measure_peaks), not a vendor figure",
                      "peak_sm_mhz": peak_clocks.get("sm_mhz"),
                      "peak_nominal": fma_nominal / 1e12, "frac_of_nominal": achieved / fma_nominal,
