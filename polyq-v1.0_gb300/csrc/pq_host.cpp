@@ -1114,8 +1114,9 @@ HostEngine device_order(const HostEngine& e, int di_max, std::vector<int>& perm)
     // Units of chunks that differ in the pair coordinates (the first three coordinates outside
     // the walked ones that touch no pivot) are walked as sums bucketed by the parities of the
     // walked point with the pair coordinates' G rows (the bucket walk).  Walked coordinates with
-    // even Z4 increments whose G bits at the pair coordinates agree, placed first (three, else
-    // two and any third), keep the eight points of every group of steps in two buckets (four).
+    // even Z4 increments whose G bits at the pair coordinates agree, placed first -- two pairs
+    // (16-point groups), else three or two and any third (8-point groups) -- keep every group's
+    // points in at most four buckets.
     std::vector<int> even;
     for (int j : low)
         if (!e.lp0[(size_t)j]) even.push_back(j);
@@ -1134,17 +1135,39 @@ HostEngine device_order(const HostEngine& e, int di_max, std::vector<int>& perm)
             };
             int cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
             for (int j : even) cnt[gof(j)]++;
-            // three coordinates with one value (two buckets per group, one for the value 0),
-            // else two (four buckets) followed by any third
-            int best = -1, need = 3;
-            for (; need >= 2 && best < 0; need--)
-                for (int g = 0; g < 8; g++)
-                    if (cnt[g] >= need && (best < 0 || (best != 0 && cnt[g] > cnt[best]))) best = g;
-            if (best >= 0) {
-                std::vector<int> front, rest;
-                for (int j : even) (front.size() < 3 && gof(j) == best ? front : rest).push_back(j);
-                even = front;
+            // 16-point groups: two pairs, coordinates 0, 1 of one value (gam) and 2, 3 of one value
+            // (del); fewest buckets first (gam = del = 0: one; gam = del or gam = 0: two; else four)
+            int bg = -1, bd = -1, bscore = 99;
+            for (int g = 0; g < 8; g++)
+                for (int h = 0; h < 8; h++) {
+                    if (cnt[g] < 2 || cnt[h] < 2 || (g == h && cnt[g] < 4)) continue;
+                    const int score = (g == 0 && h == 0) ? 0 : ((g == h || g == 0) ? 1 : 2);
+                    if (score < bscore) { bscore = score; bg = g; bd = h; }
+                }
+            if (bg >= 0) {
+                std::vector<int> p0, p1, rest;
+                for (int j : even) {
+                    const int v = gof(j);
+                    if (v == bg && p0.size() < 2) p0.push_back(j);
+                    else if (v == bd && p1.size() < 2) p1.push_back(j);
+                    else rest.push_back(j);
+                }
+                even = p0;
+                even.insert(even.end(), p1.begin(), p1.end());
                 even.insert(even.end(), rest.begin(), rest.end());
+            } else {
+                // 8-point groups: three coordinates with one value (two buckets per group, one for
+                // the value 0), else two (four buckets) followed by any third
+                int best = -1, need = 3;
+                for (; need >= 2 && best < 0; need--)
+                    for (int g = 0; g < 8; g++)
+                        if (cnt[g] >= need && (best < 0 || (best != 0 && cnt[g] > cnt[best]))) best = g;
+                if (best >= 0) {
+                    std::vector<int> front, rest;
+                    for (int j : even) (front.size() < 3 && gof(j) == best ? front : rest).push_back(j);
+                    even = front;
+                    even.insert(even.end(), rest.begin(), rest.end());
+                }
             }
         }
     }

@@ -384,7 +384,7 @@ __device__ __forceinline__ void gray_chunk_rot_any(const float4 *__restrict__ W,
 // Walks of up to 2^kGroupTableMaxDl steps keep their group table (two words per group of eight
 // steps) after the 32 stride words of a warp's staging array.
 static constexpr int kGroupTableMaxDl = 10;
-static constexpr int kTgWords = 32 + 2 * (1 << (kGroupTableMaxDl - 3));
+static constexpr int kTgWords = 32 + 2 * (1 << (kGroupTableMaxDl - 3)) + 2 * (1 << (kGroupTableMaxDl - 4));
 // The K chunks of a unit differ only in pair coordinates, so chunk k's sign for a walked
 // coordinate j is a common one times (-1)^{k . g_j}, g_j the bits of coordinate j in the pair
 // coordinates' G rows.  Its sum is therefore
@@ -420,6 +420,30 @@ __device__ __forceinline__ uint64_t times_i(uint64_t p) {
     float a, b;
     up2(p, a, b);
     return pk2(-b, a);
+}
+
+// Walsh-Hadamard transform over the buckets, S_k = sum_x (-1)^{popc(x & k)} T_x, unpacked to
+// (hi.re, hi.im, lo.re, lo.im) per chunk
+template <int K>
+__device__ __forceinline__ void bucket_transform(uint64_t (&T)[K][2], float (&S)[K][4]) {
+    const uint64_t one2 = pk2(1.f, 1.f), neg2 = pk2(-1.f, -1.f);
+#pragma unroll
+    for (int h = 1; h < K; h <<= 1)
+#pragma unroll
+        for (int x = 0; x < K; x++)
+            if (!(x & h)) {
+#pragma unroll
+                for (int c = 0; c < 2; c++) {
+                    const uint64_t a = T[x][c], bb = T[x | h][c];
+                    T[x][c] = ffma2(one2, bb, a);
+                    T[x | h][c] = ffma2(neg2, bb, a);
+                }
+            }
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        up2(T[k][0], S[k][0], S[k][1]);
+        up2(T[k][1], S[k][2], S[k][3]);
+    }
 }
 
 // Bucket walk of one unit: on return S[k] = (hi.re, hi.im, lo.re, lo.im) of chunk k's sum
@@ -537,25 +561,134 @@ __device__ __forceinline__ void bucket_walk(uint64_t wad, uint32_t P1, const uin
         gcur = gnext;
     }
 #undef PQ_LD
-    // Walsh-Hadamard transform over the buckets: S_k = sum_x (-1)^{popc(x & k)} T_x
-    const uint64_t neg2 = pk2(-1.f, -1.f);
+    bucket_transform<K>(T, S);
+}
+
+// 16-point groups: coordinates 0..3 walked inside a group, g_0 = g_1 = gam and g_2 = g_3 = del,
+// all four of even Z4 increment.  The group's 16 points fall in the same four buckets as an
+// 8-point group, four points each; its second eight points (coordinates 2 and 3 both flipped
+// relative to the first eight) repeat the first eight's buckets and signs times one per-lane
+// sign s23 = (-1)^{b_2 ^ b_3}: the locals are multiplied by s23 between the halves and the
+// group's sums added with s23 again.  The group table (stage_job, after the 8-point one) holds
+// the same three fields for S = gray(16 g).
+template <int K, int PAT>
+__device__ __forceinline__ void bucket_walk16(uint64_t wad, uint32_t P1, const uint32_t (&grow)[3],
+                                              const uint32_t *Tg, const uint8_t *Lp, int dl, float (&S)[K][4]) {
+    constexpr int NP = K == 8 ? 3 : (K == 4 ? 2 : 1);
+    auto gbits = [&](int j) -> uint32_t {
+        uint32_t g = 0;
 #pragma unroll
-    for (int h = 1; h < K; h <<= 1)
+        for (int i = 0; i < NP; i++) g |= ((grow[i] >> j) & 1u) << i;
+        return g;
+    };
+    const uint32_t gam = gbits(0), del = gbits(2);  // gbits(1) == gam, gbits(3) == del
+    const uint32_t T0 = Tg[0], T1 = Tg[1], T2 = Tg[2], T23 = Tg[2] ^ Tg[3];
+    uint32_t b = 0;
 #pragma unroll
-        for (int x = 0; x < K; x++)
-            if (!(x & h)) {
+    for (int j = 0; j < 4; j++) b |= ((((uint32_t)Lp[j] >> 1) ^ (P1 >> j)) & 1u) << j;
+    auto sgn = [&](uint32_t gp) -> uint64_t {
+        const float f = __uint_as_float(((__popc(b & gp) & 1u) << 31) | 0x3F800000u);
+        return pk2(f, f);
+    };
+    const uint64_t s1p = sgn(1), s2p = sgn(3), s3p = sgn(2), s4p = sgn(6), s5p = sgn(7), s6p = sgn(5), s7p = sgn(4);
+    const uint32_t s23bit = (((b >> 2) ^ (b >> 3)) & 1u) << 31;
+    const uint64_t s23p = sgn(12);
+    const uint64_t one2 = pk2(1.f, 1.f), zero2 = 0ull;
+    uint64_t T[K][2];
 #pragma unroll
-                for (int c = 0; c < 2; c++) {
-                    const uint64_t a = T[x][c], bb = T[x | h][c];
-                    T[x][c] = ffma2(one2, bb, a);
-                    T[x | h][c] = ffma2(neg2, bb, a);
+    for (int k = 0; k < K; k++) T[k][0] = T[k][1] = 0ull;
+#define PQ_LD(a) __ldg(reinterpret_cast<const ulonglong2 *>(a))
+    ulonglong2 q0, q1, q2, q3, q4, q5, q6, q7;
+    {
+        uint64_t a = wad;
+        q0 = PQ_LD(a);
+        a ^= T0; q1 = PQ_LD(a);
+        a ^= T1; q2 = PQ_LD(a);
+        a ^= T0; q3 = PQ_LD(a);
+        a ^= T2; q4 = PQ_LD(a);
+        a ^= T0; q5 = PQ_LD(a);
+        a ^= T1; q6 = PQ_LD(a);
+        a ^= T0; q7 = PQ_LD(a);
+    }
+    const uint2 *Gt = reinterpret_cast<const uint2 *>(Tg + 32) + (1 << (kGroupTableMaxDl - 3));
+    const uint32_t ngroups = 1u << (dl - 4);
+    uint2 gcur = Gt[0];
+    uint64_t AH, AL, BH, BL, CH, CL, DH, DL;
+    // one half of a group: its eight entries (in q0..q7) into the locals, each register
+    // refilled from the half that follows (first point at address nxt)
+#define PQ_HALF(FIRST, nxt)                                                                              \
+    {                                                                                                    \
+        uint64_t a = (nxt);                                                                              \
+        if (FIRST) { AH = q0.x; AL = q0.y; } else { AH = ffma2(one2, q0.x, AH); AL = ffma2(one2, q0.y, AL); } \
+        q0 = PQ_LD(a);                                                                                   \
+        a ^= T0; BH = ffma2(s1p, q1.x, FIRST ? zero2 : BH); BL = ffma2(s1p, q1.y, FIRST ? zero2 : BL); q1 = PQ_LD(a); \
+        a ^= T1; AH = ffma2(s2p, q2.x, AH); AL = ffma2(s2p, q2.y, AL); q2 = PQ_LD(a);                    \
+        a ^= T0; BH = ffma2(s3p, q3.x, BH); BL = ffma2(s3p, q3.y, BL); q3 = PQ_LD(a);                    \
+        a ^= T2; CH = ffma2(s4p, q4.x, FIRST ? zero2 : CH); CL = ffma2(s4p, q4.y, FIRST ? zero2 : CL); q4 = PQ_LD(a); \
+        a ^= T0; DH = ffma2(s5p, q5.x, FIRST ? zero2 : DH); DL = ffma2(s5p, q5.y, FIRST ? zero2 : DL); q5 = PQ_LD(a); \
+        a ^= T1; CH = ffma2(s6p, q6.x, CH); CL = ffma2(s6p, q6.y, CL); q6 = PQ_LD(a);                    \
+        a ^= T0; DH = ffma2(s7p, q7.x, DH); DL = ffma2(s7p, q7.y, DL); q7 = PQ_LD(a);                    \
+    }
+    for (uint32_t g = 0;; ++g) {
+        const bool last = g + 1 == ngroups;
+        const uint2 gnext = Gt[last ? g : g + 1];
+        const uint32_t Sg = (g << 4) ^ (g << 3);
+        const uint32_t x0 = gcur.y & (uint32_t)(K - 1);
+        const uint32_t e0 = (gcur.y >> 8) + ((__popc(P1 & Sg) & 1u) << 1);
+        PQ_HALF(true, wad ^ (uint64_t)gcur.x ^ (uint64_t)T23)
+        AH = ffma2(s23p, AH, zero2); AL = ffma2(s23p, AL, zero2);
+        BH = ffma2(s23p, BH, zero2); BL = ffma2(s23p, BL, zero2);
+        CH = ffma2(s23p, CH, zero2); CL = ffma2(s23p, CL, zero2);
+        DH = ffma2(s23p, DH, zero2); DL = ffma2(s23p, DL, zero2);
+        PQ_HALF(false, wad ^ (uint64_t)gnext.x)
+        if (PAT == 0 || PAT == 1) {
+            AH = ffma2(one2, CH, AH);
+            AL = ffma2(one2, CL, AL);
+            BH = ffma2(one2, DH, BH);
+            BL = ffma2(one2, DL, BL);
+        }
+        if (PAT == 0 || PAT == 2) {
+            AH = ffma2(one2, BH, AH);
+            AL = ffma2(one2, BL, AL);
+        }
+        if (PAT == 2) {
+            CH = ffma2(one2, DH, CH);
+            CL = ffma2(one2, DL, CL);
+        }
+        if (e0 & 1u) {
+            AH = times_i(AH);
+            AL = times_i(AL);
+            if (PAT != 0) {
+                if (PAT == 2) {
+                    CH = times_i(CH);
+                    CL = times_i(CL);
+                } else {
+                    BH = times_i(BH);
+                    BL = times_i(BL);
                 }
             }
-#pragma unroll
-    for (int k = 0; k < K; k++) {
-        up2(T[k][0], S[k][0], S[k][1]);
-        up2(T[k][1], S[k][2], S[k][3]);
+            if (PAT == 3) {
+                CH = times_i(CH);
+                CL = times_i(CL);
+                DH = times_i(DH);
+                DL = times_i(DL);
+            }
+        }
+        const float sg = __uint_as_float((((e0 & 2u) << 30) ^ s23bit) | 0x3F800000u);
+        const uint64_t sg2 = pk2(sg, sg);
+        bucket_add<K>(T, x0, sg2, AH, AL);
+        if (PAT == 1 || PAT == 3) bucket_add<K>(T, x0 ^ gam, sg2, BH, BL);
+        if (PAT == 2) bucket_add<K>(T, x0 ^ del, sg2, CH, CL);
+        if (PAT == 3) {
+            bucket_add<K>(T, x0 ^ gam ^ del, sg2, CH, CL);
+            bucket_add<K>(T, x0 ^ del, sg2, DH, DL);
+        }
+        if (last) break;
+        gcur = gnext;
     }
+#undef PQ_HALF
+#undef PQ_LD
+    bucket_transform<K>(T, S);
 }
 
 // One unit of K chunks (K = 2^np: the chunk at s1 and those that differ from it in the first np
@@ -625,15 +758,26 @@ __device__ __forceinline__ void walk_unit(const EngineDev &E, const JobDev &J, c
         const uint64_t wad = reinterpret_cast<uint64_t>(E.wtab) | ((uint64_t)sidx << 4);
         constexpr int NPB = K == 8 ? 3 : 2;
         uint32_t g0 = 0, g2 = 0;
+        bool pair23 = dl >= 4 && !(Lp[3] & 1);  // coordinates 2 and 3 agree: 16-point groups
 #pragma unroll
         for (int i = 0; i < NPB; i++) {
             g0 |= (grow[i] & 1u) << i;
             g2 |= ((grow[i] >> 2) & 1u) << i;
+            const uint32_t h = (grow[i] >> 2) & 3u;
+            pair23 = pair23 && (h == 0u || h == 3u);
         }
-        if (g0 == 0u && g2 == 0u) bucket_walk<K, 0>(wad, P1, grow, Tg, Lp, dl, acc);
-        else if (g2 == g0) bucket_walk<K, 1>(wad, P1, grow, Tg, Lp, dl, acc);
-        else if (g0 == 0u) bucket_walk<K, 2>(wad, P1, grow, Tg, Lp, dl, acc);
-        else bucket_walk<K, 3>(wad, P1, grow, Tg, Lp, dl, acc);
+        const int pat = (g0 == 0u && g2 == 0u) ? 0 : (g2 == g0 ? 1 : (g0 == 0u ? 2 : 3));
+        if (pair23) {
+            if (pat == 0) bucket_walk16<K, 0>(wad, P1, grow, Tg, Lp, dl, acc);
+            else if (pat == 1) bucket_walk16<K, 1>(wad, P1, grow, Tg, Lp, dl, acc);
+            else if (pat == 2) bucket_walk16<K, 2>(wad, P1, grow, Tg, Lp, dl, acc);
+            else bucket_walk16<K, 3>(wad, P1, grow, Tg, Lp, dl, acc);
+        } else {
+            if (pat == 0) bucket_walk<K, 0>(wad, P1, grow, Tg, Lp, dl, acc);
+            else if (pat == 1) bucket_walk<K, 1>(wad, P1, grow, Tg, Lp, dl, acc);
+            else if (pat == 2) bucket_walk<K, 2>(wad, P1, grow, Tg, Lp, dl, acc);
+            else bucket_walk<K, 3>(wad, P1, grow, Tg, Lp, dl, acc);
+        }
 #pragma unroll
         for (int k = 0; k < K; k++) qk[k] = chunk_m(k) & 3u;
     } else {
@@ -709,10 +853,13 @@ __device__ __forceinline__ void stage_job(const KArgs &a, int jb, uint64_t *G, u
     // S = gray(8 g) (bits 2 .. dl - 1): the XOR of S's strides, the parities of S with the pair
     // coordinates' G rows (bucket) and, from bit 8, the sum of Lp over S mod 4
     const int npj = (a.jdl[jb] >> 8) & 3;
+    // (8-point groups, S = gray(8 g), then 16-point groups, S = gray(16 g))
     if (E.joint && npj >= 2 && dlj >= 3 && dlj <= kGroupTableMaxDl) {
         uint2 *Gt = reinterpret_cast<uint2 *>(Tg + 32);
-        for (int g = lane; g < (1 << (dlj - 3)); g += 32) {
-            const uint32_t S = ((uint32_t)g << 3) ^ ((uint32_t)g << 2);
+        const int n8 = 1 << (dlj - 3), n16 = dlj >= 4 ? 1 << (dlj - 4) : 0;
+        for (int e = lane; e < n8 + n16; e += 32) {
+            const uint32_t g = (uint32_t)(e < n8 ? e : e - n8);
+            const uint32_t S = e < n8 ? (g << 3) ^ (g << 2) : (g << 4) ^ (g << 3);
             uint32_t off = 0, u = 0, x = 0;
             for (int j = 2; j < dlj; j++)
                 if ((S >> j) & 1u) {
@@ -720,7 +867,7 @@ __device__ __forceinline__ void stage_job(const KArgs &a, int jb, uint64_t *G, u
                     u += Lp[j];
                 }
             for (int i = 0; i < npj; i++) x |= (uint32_t)(popc64(G[E.pairc[i]] & (uint64_t)S) & 1) << i;
-            Gt[g] = make_uint2(off, x | ((u & 3u) << 8));
+            Gt[e < n8 ? g : (1u << (kGroupTableMaxDl - 3)) + g] = make_uint2(off, x | ((u & 3u) << 8));
         }
         __syncwarp();
     }
