@@ -23,7 +23,7 @@ cfg1_small, cfg3_batched, cfg5_serve
            CPU restatement's), the uneven 256-circuit batch (one graph launch vs the plain
            per-circuit and per-boundary paths, CPU restatement per branch-dimension bucket) and
            the served Poisson stream (throughput, p50/p99 at the offered load, below saturation
-           and saturated); each leg with its own clock summary (nvidia-smi every 50 ms)
+           and saturated); each leg with its own clock summary (nvidia-smi every 10 ms)
 readme_statevector
            at N=1 also the reference README's own benchmark table (statevectors of its two seeded
            layered circuits, construction + statevector) beside the published CPU timings
@@ -77,7 +77,8 @@ def config(extra=None):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 50 ms while running."""
+    """nvidia-smi clocks and throttle reasons sampled every 10 ms while running (a timed region of
+    20 headline steps lasts about 70 ms)."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -90,7 +91,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", self.gpu, "--query-gpu=" + self.FIELDS,
-                                          "--format=csv,noheader,nounits", "-lms", "50"],
+                                          "--format=csv,noheader,nounits", "-lms", "10"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -121,7 +122,7 @@ class ClockSampler:
         samples when no window is given or none fell inside it)."""
         sm, mx, reasons = [], [], set()
         names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
-        lines = [ln for t, ln in self.lines if t0 is None or (t0 <= t <= t1 + 0.06)]
+        lines = [ln for t, ln in self.lines if t0 is None or (t0 <= t <= t1 + 0.015)]
         if not lines:
             lines = [ln for _, ln in self.lines]
         for ln in lines:
