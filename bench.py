@@ -601,6 +601,9 @@ def leg_batched(args, clk=None, cpu=True):
            "batched_equals_per_circuit_bitwise": same, "batched_vs_per_circuit_max_rel_diff": max_rel_diff,
            "enum_kernel_ms": enum_avg,
            "fma_pipe_frac_of_measured": achieved / peaks[2],
+           "fma_pipe_frac_note": "per-branch form (4 FP32 FMA-pipe ops per branch) over the measured fma.f32 rate; "
+                                 "the bucket walk executes 0.75 per branch (fraction %.3f)"
+                                 % (achieved * BUCKET_OPS_PER_BRANCH / FMA_OPS_PER_BRANCH / peaks[2]),
            "per_d_bucket_amps_per_s_plain_per_circuit": {k: v[0] / v[1] for k, v in sorted(buckets.items())},
            "config": {"workload": "256 circuits, n~U[16,64], 40n gates, T~U[8,36] (seed 3), 64 uniform y each, "
                                   "x=0, strategy auto", "branches_enumerated_per_step": benum[0],
