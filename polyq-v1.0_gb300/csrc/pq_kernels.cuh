@@ -773,10 +773,9 @@ __device__ __forceinline__ void walk_unit(const EngineDev &E, const JobDev &J, c
             else if (pat == 2) bucket_walk16<K, 2>(wad, P1, grow, Tg, Lp, dl, acc);
             else bucket_walk16<K, 3>(wad, P1, grow, Tg, Lp, dl, acc);
         } else {
-            if (pat == 0) bucket_walk<K, 0>(wad, P1, grow, Tg, Lp, dl, acc);
-            else if (pat == 1) bucket_walk<K, 1>(wad, P1, grow, Tg, Lp, dl, acc);
-            else if (pat == 2) bucket_walk<K, 2>(wad, P1, grow, Tg, Lp, dl, acc);
-            else bucket_walk<K, 3>(wad, P1, grow, Tg, Lp, dl, acc);
+            // 8-point groups (engines without two equally coupled pairs): one variant for all
+            // bucket patterns keeps the kernel's hot code small
+            bucket_walk<K, 3>(wad, P1, grow, Tg, Lp, dl, acc);
         }
 #pragma unroll
         for (int k = 0; k < K; k++) qk[k] = chunk_m(k) & 3u;
