@@ -381,8 +381,9 @@ __device__ __forceinline__ void gray_chunk_rot_any(const float4 *__restrict__ W,
 }
 
 // ------------------------------------------------------------------------------ bucket walk
-// Walks of up to 2^kGroupTableMaxDl steps keep their group table (two words per group of eight
-// steps) after the 32 stride words of a warp's staging array.
+// Walks of up to 2^kGroupTableMaxDl steps keep their group tables (two words per group: the
+// table of 8-point groups, then that of 16-point groups) after the 32 stride words of a warp's
+// staging array.
 static constexpr int kGroupTableMaxDl = 10;
 static constexpr int kTgWords = 32 + 2 * (1 << (kGroupTableMaxDl - 3)) + 2 * (1 << (kGroupTableMaxDl - 4));
 // The K chunks of a unit differ only in pair coordinates, so chunk k's sign for a walked
@@ -396,8 +397,8 @@ static constexpr int kTgWords = 32 + 2 * (1 << (kGroupTableMaxDl - 3)) + 2 * (1 
 // them so; del = g_2), the eight points of a group (coordinates 0..2 walked, the others fixed)
 // fall in at most four buckets -- x0, x0 ^ gam, x0 ^ gam ^ del, x0 ^ del, two points each -- with
 // per-lane signs that repeat every group: they are summed in local pairs and added into their
-// buckets once per group (merged where buckets coincide: two when del = gam, one when both are
-// 0), turned by the group's start index i^{e0}.  Hi parts stay on the exact grid (every partial sum
+// buckets once per group (merged where buckets coincide, PAT below: two when del = gam, one when
+// both are 0), turned by the group's start index i^{e0}.  Hi parts stay on the exact grid (every partial sum
 // is a signed sub-sum of the chunk's terms); lo parts are summed in at most 2^dl / 8 + 6
 // roundings per term, inside the walk's 2^dl-term bound.
 template <int K>
@@ -448,9 +449,10 @@ __device__ __forceinline__ void bucket_transform(uint64_t (&T)[K][2], float (&S)
 
 // Bucket walk of one unit: on return S[k] = (hi.re, hi.im, lo.re, lo.im) of chunk k's sum
 // without its start factor i^{m_k(0)}.  P1: c_j of chunk 0; grow[i]: pair coordinate i's G row
-// over the walked coordinates; wad0: the start point's entry address.
+// over the walked coordinates; wad: the start point's entry address.
 // PAT: which of a group's four bucket offsets coincide -- 0: gam = del = 0 (one bucket), 1:
-// del = gam != 0 (x0, x0 ^ gam), 2: gam = 0 != del (x0, x0 ^ del), 3: all four distinct.
+// del = gam != 0 (x0, x0 ^ gam), 2: gam = 0 != del (x0, x0 ^ del), 3: none assumed (four adds,
+// correct for every pattern; the one the enumeration instantiates for 8-point groups).
 template <int K, int PAT>
 __device__ __forceinline__ void bucket_walk(uint64_t wad, uint32_t P1, const uint32_t (&grow)[3],
                                             const uint32_t *Tg, const uint8_t *Lp, int dl, float (&S)[K][4]) {
