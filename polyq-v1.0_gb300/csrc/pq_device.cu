@@ -300,6 +300,9 @@ struct Segment {
     int engines() const { return (ee < 0 ? (int)tg->dev.size() : ee) - eb; }
 };
 
+static const int kMaxSlices = 256;  // item slices of a plan's enumeration (one per SM)
+static const size_t kSliceMinEngines = 64;  // launches over more branch engines use slices
+
 struct Plan {
     int nw = 1;
     int64_t nreq = 0;
@@ -492,7 +495,7 @@ static pq_status build_plan(const std::vector<Segment> &segs, int nw, cudaStream
         if (ranged) parts.push_back({&P.ioff, vb(jib), jib.data()});
         const size_t nup = parts.size();
         parts.push_back({&P.partials, (size_t)P.nitems * sizeof(double2), nullptr});
-        parts.push_back({&P.counter, sizeof(unsigned long long), nullptr});
+        parts.push_back({&P.counter, sizeof(unsigned long long) * kMaxSlices, nullptr});
         parts.push_back({&P.job_vals, (size_t)P.njobs * sizeof(double2), nullptr});
         parts.push_back({&P.job_err, (size_t)P.njobs * sizeof(double), nullptr});
         parts.push_back({&P.x, (size_t)P.nreq * nw * 8, nullptr});
@@ -550,6 +553,9 @@ static pq_status build_plan(const std::vector<Segment> &segs, int nw, cudaStream
     a.nitems = P.nitems;
     a.partials = P.partials.as<double2>();
     a.counter = P.counter.as<unsigned long long>();
+    // item slices per SM where the launch spans many engines' tables (batches): with few
+    // engines their tables stay in L1 anyway and one counter balances best
+    a.nslices = eng.size() > kSliceMinEngines ? std::min(sm_count(), kMaxSlices) : 1;
     a.use_ctab = tu.chunk_tables == 1 ? 1 : 0;
     a.job_vals = P.job_vals.as<double2>();
     a.job_err = P.job_err.as<double>();
@@ -634,7 +640,7 @@ static cudaError_t enqueue_core(Plan &P, int mode, int ctab = -1, const KArgs *i
     }
     e = cudaMemsetAsync(P.errflag.p, 0, sizeof(int), P.stream);
     if (e != cudaSuccess) return e;
-    e = cudaMemsetAsync(P.counter.p, 0, sizeof(unsigned long long), P.stream);
+    e = cudaMemsetAsync(P.counter.p, 0, P.counter.n, P.stream);
     if (e != cudaSuccess) return e;
     KArgs args = P.args;
     args.fp64_mode = mode == 1 ? 1 : 0;
@@ -2188,7 +2194,7 @@ PQ_API int32_t pq_debug_branch_phases(pq_sim *s, int32_t branch, const uint64_t 
     if (cudaMemcpyAsync(P.x.p, x, bw, cudaMemcpyHostToDevice, P.stream) != cudaSuccess) return -2;
     if (cudaMemcpyAsync(P.y.p, y, bw, cudaMemcpyHostToDevice, P.stream) != cudaSuccess) return -2;
     prepare_kernel<<<P.grid_prep, 128, (size_t)4 * P.smem_words * 8, P.stream>>>(P.args);
-    cudaMemsetAsync(P.counter.p, 0, sizeof(unsigned long long), P.stream);
+    cudaMemsetAsync(P.counter.p, 0, P.counter.n, P.stream);
     enum_kernel<2><<<P.grid_enum, P.block_enum, 0, P.stream>>>(P.args);
     JobDev J;
     std::vector<uint8_t> dev((size_t)1 << d);

@@ -41,7 +41,8 @@ struct KArgs {
     const unsigned long long *jnch;  // per job: chunks
     long long nitems;
     double2 *partials;
-    unsigned long long *counter;
+    unsigned long long *counter;  // nslices counters (item slices, enum_kernel)
+    int nslices;                  // 0 or 1: one counter over all items
     double2 *job_vals;
     double *job_err;
     const int *out_jobs;        // nout + 1: jobs of output o are [out_jobs[o], out_jobs[o+1])
@@ -1075,11 +1076,25 @@ __global__ void __launch_bounds__(256, MINB) enum_kernel(KArgs a) {
     uint32_t *Tg = sTg[wib];
     int cur_k = -1;  // position (item order) of the job whose data is staged
     long long kbeg = 0, kend = 0;
+    // The items (jobs in engine order) are cut into nslices contiguous slices, one per SM: the
+    // warps of an SM take the items of its slice in order -- neighbouring items, mostly one
+    // engine's jobs, so they share its table in L1 -- and then those of the following slices.
+    // Each slice's counter hands out every item of it once; a warp stops after it has found
+    // every slice exhausted.
+    const int ns = a.nslices > 1 ? a.nslices : 1;
+    unsigned smid;
+    asm("mov.u32 %0, %%smid;" : "=r"(smid));
+    int sl = (int)(smid % (unsigned)ns), left = ns;
     while (true) {
+        const long long sb = a.nitems * sl / ns, se = a.nitems * (sl + 1) / ns;
         unsigned long long it0 = 0;
-        if (lane == 0) it0 = atomicAdd(a.counter, 1ull);
-        const long long it = (long long)__shfl_sync(PQ_FULL, it0, 0);
-        if (it >= a.nitems) break;
+        if (lane == 0) it0 = atomicAdd(a.counter + sl, 1ull);
+        const long long it = sb + (long long)__shfl_sync(PQ_FULL, it0, 0);
+        if (it >= se) {
+            if (--left == 0) break;
+            sl = sl + 1 == ns ? 0 : sl + 1;
+            continue;
+        }
         if (!(it >= kbeg && it < kend)) {
             int lo = 0, hi = a.njobs - 1;  // last k with istart[k] <= it
             while (lo < hi) {
